@@ -1,0 +1,188 @@
+/*
+ * skills_gb300.h -- C ABI of the GB300 (sm_103a) Ski-LLS solver.
+ *
+ * Plain pointers and sizes only; no exceptions cross this boundary.  Every
+ * entry point returns an skl_status and, on failure, leaves a message for
+ * skl_last_error().  The C++ drop-in header ski-lls.h re-exposes the three
+ * reference signatures over these calls.
+ *
+ * Reference interfaces replaced (file:line in numericalalgorithmsgroup/Ski-LLS):
+ *   skl_sparse_solve  <- ls_sparse_spqr                 include/ski-lls.h:24-28,
+ *                                                        src/ls_sparse_spqr.cpp:79-214
+ *   skl_dense_solve   <- ls_dense_hashing_blendenpik    include/ski-lls.h:15-17,
+ *                                                        src/ls_dense_hashing_blendenpik.cpp:23-149
+ *   skl_dense_solve with opts.use_cpqr = 0
+ *                     <- ls_dense_hashing_blendenpik_noCPQR  include/ski-lls.h:19-21
+ *   skl_srand / skl_hash_generate
+ *                     <- srand() + gen_hashing_matrix   src/sparse_helpers.cpp:66-116
+ *   skl_sketch_sparse <- sparse_sketch(A,k,gamma,b,bs)  src/sketching.cpp:90-112
+ *   skl_sketch_dense  <- rand_hashing_dct(A,b,..)       src/dense_helpers.cpp:83-112
+ *   skl_dht           <- fast_unitary_transform         src/fast_unitary_transform.cpp:42-121
+ *   skl_cpqr          <- column_pivoted_qr(A,E,tau)     src/column_pivoted_QR.cpp:35-58
+ *   skl_trsv_upper    <- cs_usolve/utsolve_cholmod_structure, dtrsv
+ *                                                        src/sparse_helpers.cpp:122-181,
+ *                                                        src/IterSolver.cpp:89,95
+ */
+#ifndef SKILLS_GB300_H
+#define SKILLS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SKL_OK = 0,
+    SKL_ERR_INVALID = 1,            /* bad argument (null pointer, size, csc structure) */
+    SKL_ERR_NOT_OVERDETERMINED = 2, /* rows < cols: "Matrix is not overdetermined." */
+    SKL_ERR_RANK_ZERO = 3,          /* factorization found rank 0: "SPQR Factorization fails" */
+    SKL_ERR_CUDA = 4,               /* CUDA runtime error */
+    SKL_ERR_NO_DEVICE = 5,          /* no usable sm_103 device */
+    SKL_ERR_TIMEOUT = 6,            /* a bounded device-side wait gave up */
+    SKL_ERR_ALLOC = 7,              /* device or host allocation failed */
+    SKL_ERR_NONFINITE = 8           /* NaN/Inf in A or b */
+} skl_status;
+
+typedef enum { SKL_PREC_MIXED = 0, SKL_PREC_FP64 = 1 } skl_precision;
+
+/* Compressed sparse column matrix with the cs_dl field layout of CSparse
+ * (m rows, n cols, p[n+1] column pointers, i[nnz] row indices, x[nnz]
+ * values, 64-bit integers), as the reference passes it
+ * (test/ski-llsSparseExample.cpp:15-20). */
+typedef struct {
+    int64_t m, n, nzmax;
+    const int64_t* p;
+    const int64_t* i;
+    const double* x;
+} skl_csc;
+
+typedef struct {
+    double gamma;            /* over-sampling ratio, m = ceil(gamma*d)           */
+    int64_t k;               /* nonzeros per column of the hashing matrix        */
+    double abs_tol;          /* early exit if ||b - A xs|| < abs_tol             */
+    double it_tol;           /* LSQR relative tolerance                           */
+    int64_t max_it;          /* LSQR iteration limit                              */
+    double rcond_threshold;  /* sparse path: preconditioner 'well conditioned'    */
+    double perturb;          /* sparse path: pivot perturbation when ill cond.    */
+    double rcond;            /* dense path: minimal |R_ii| kept (absolute rule)   */
+    double rank_tol;         /* sparse path: relative rank tolerance on |R_ii|;
+                                <= 0 selects 20*(m+d)*eps(working precision)     */
+    int precision;           /* skl_precision                                     */
+    int use_cpqr;            /* dense path: 1 = CPQR + rank (ls_dense_hashing_blendenpik),
+                                0 = unpivoted QR (..._noCPQR)                     */
+    int seed_mode;           /* 0: continue the library's glibc-compatible stream
+                                   (sparse path; a fresh process is seed 1),
+                                1: reseed with `seed` before drawing              */
+    uint32_t seed;           /* dense path seed (the reference uses time(NULL));
+                                0 selects time(NULL)                              */
+    int wisdom;              /* dense path: pad the DHT length to a 2^a3^b5^c size */
+    double backward_tol;     /* >0: keep iterating until ||A^T r||/(||A||_F||r||)
+                                <= backward_tol (checked in FP64)                 */
+    int64_t max_refine;      /* restarts allowed to meet backward_tol            */
+    int device;              /* CUDA device ordinal                               */
+} skl_opts;
+
+typedef struct {
+    int64_t rank;            /* detected rank                                     */
+    int flag;                /* 0 = converged or early exit, 1 = max_it reached   */
+    int64_t it;              /* LSQR iterations (0 on early exit)                 */
+    int success;             /* sparse path: rcond(R11) > rcond_threshold         */
+    int64_t sketch_rows;     /* m                                                 */
+    double rcond_r11;        /* 1/(||R11||_inf ||R11^{-1}||_inf)                   */
+    double explicit_residual;/* ||b - A xs|| of the sketch solution               */
+    double residual_norm;    /* ||b - A x|| (FP64)                                */
+    double backward_error;   /* ||A^T r|| / (||A||_F ||r||) (FP64)                */
+    double t_total_ms;       /* device time of the whole solve (CUDA events)      */
+    double t_upload_ms;      /* host->device copies                               */
+    double t_setup_ms;       /* format conversion, norms, hashing upload          */
+    double t_sketch_ms;      /* S*A, S*b (and DHT on the dense path)              */
+    double t_qr_ms;          /* randomized CPQR + Q^T c                           */
+    double t_precond_ms;     /* rank, R11^{-1}, condition estimate, explicit x    */
+    double t_lsqr_ms;        /* LSQR iterations                                   */
+    double t_host_hash_ms;   /* host wall time generating the hash stream         */
+    int64_t kernel_launches; /* kernels launched by this solve                    */
+} skl_info;
+
+/* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,
+ * gamma 1.1, k 3, PERTURB 1e-10, RCOND_THRESHOLD 1e-10, ABS_TOL 1e-8). */
+void skl_default_opts(skl_opts* opts);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* skl_last_error(void);
+
+/* Library version string. */
+const char* skl_version(void);
+
+/* Reseed the library's glibc-compatible random stream (srand semantics). */
+void skl_srand(uint32_t seed);
+
+/* ---------------------------------------------------------------- solvers */
+
+/* Sparse least squares min ||Ax-b||, A in CSC (host memory).  x (host, A->n
+ * entries) receives the solution.  Sketch: s-hashing with opts->k nonzeros
+ * per column, m = ceil(gamma*n); CPQR of the sketch; LSQR preconditioned by
+ * R11. */
+skl_status skl_sparse_solve(const skl_csc* A, const double* b, double* x,
+                            const skl_opts* opts, skl_info* info);
+
+/* Same with A, b and x already in device memory (CSC with 64-bit indices). */
+skl_status skl_sparse_solve_device(const skl_csc* A_dev, const double* b_dev, double* x_dev,
+                                   const skl_opts* opts, skl_info* info);
+
+/* Dense least squares, A column-major n x d with leading dimension lda (host). */
+skl_status skl_dense_solve(const double* A, int64_t lda, int64_t n, int64_t d,
+                           const double* b, double* x, const skl_opts* opts, skl_info* info);
+
+/* Same with A, b, x in device memory. */
+skl_status skl_dense_solve_device(const double* A_dev, int64_t lda, int64_t n, int64_t d,
+                                  const double* b_dev, double* x_dev, const skl_opts* opts,
+                                  skl_info* info);
+
+/* ------------------------------------------------------- building blocks */
+
+/* Hash rows and values of an m x n s-hashing matrix drawn from the library
+ * stream (seed_mode/seed as in skl_opts): rows[i*k+j], vals[i*k+j] =
+ * +-1/sqrt(k).  Bit-exact with gen_hashing_matrix for the same stream. */
+skl_status skl_hash_generate(int64_t m, int64_t n, int64_t k, int seed_mode, uint32_t seed,
+                             int64_t* rows, double* vals);
+
+/* S*A (m x d, column-major, FP32 or FP64 per `precision`, written as double
+ * to SA) and S*b for host CSC A and host hash arrays; equilibrate != 0 scales
+ * column j of SA by 1/||A(:,j)||_2. */
+skl_status skl_sketch_sparse(const skl_csc* A, const double* b, int64_t m, int64_t k,
+                             const int64_t* rows, const double* vals, int precision,
+                             int equilibrate, double* SA, double* Sb);
+
+/* Orthonormal DHT of the columns of D*A (n x d host, column-major), padded
+ * to N rows (N >= n; zeros below n): Y = H_N [D A; 0] / sqrt(N). */
+skl_status skl_dht(const double* A, int64_t lda, int64_t n, int64_t d, const double* D,
+                   int64_t N, double* Y);
+
+/* alpha*S*(H D A) for the dense path (alpha = 1/sqrt(k), as sketch() applies
+ * on top of S's +-1/sqrt(k) values): SA is m x d, Sb is m. */
+skl_status skl_sketch_dense(const double* A, int64_t lda, int64_t n, int64_t d,
+                            const double* b, const double* D, int64_t N, int64_t m, int64_t k,
+                            const int64_t* rows, const double* vals, int precision,
+                            double* SA, double* Sb);
+
+/* Randomized column-pivoted QR of the m x d column-major matrix A (host, in
+ * place): R in the upper triangle, Householder vectors below, tau[min(m,d)],
+ * jpvt[d] 0-based.  precision selects FP32 or FP64 arithmetic. */
+skl_status skl_cpqr(double* A, int64_t m, int64_t d, int precision, int64_t* jpvt,
+                    double* tau);
+
+/* x <- R^{-1} x (trans = 'n') or R^{-T} x (trans = 't') for the r x r upper
+ * triangle of R (column-major, ld), computed on the GPU through the explicit
+ * inverse used by the LSQR operator. */
+skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, int precision,
+                          double* x);
+
+/* Release all device memory and streams held by the library. */
+void skl_finalize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKILLS_GB300_H */

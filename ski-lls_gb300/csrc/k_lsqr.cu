@@ -1,0 +1,889 @@
+// k_lsqr.cu -- preconditioned LSQR on the GPU.
+//
+// Restates the Paige-Saunders recurrences of lsqr() (src/IterSolver.cpp:160-284)
+// for the operator Abar = A * P1 * D * M of LinOP_sparse_preconditioner /
+// LinOP_dense_preconditioner (src/IterSolver.cpp:21-108), where P1 selects the
+// first `rank` pivoted columns, D is the column equilibration and M = R11^{-1}.
+//
+// One iteration is five kernels, all reading their scalars from a device
+// state block so that the loop runs without host round trips and can be
+// captured in a CUDA graph:
+//   tri_n   z = D P1 (M v)                 (triangular mat-vec, row-major M)
+//   spmv_n  uh = A z - (alpha/beta) uh     (CSR rows / dense columns), beta'
+//   spmv_t  t = D P1^T A^T uh / beta'      (CSC columns / dense columns)
+//   tri_t   vh = M^T t - (beta'/alpha) vh  (triangular mat-vec, column-major M), alpha'
+//   update  Givens rotation, x += (phi/rho) w, w = v - (theta/rho) w, stop test
+// u and v are kept unnormalised (uh = beta u, vh = alpha v) so normalisation
+// folds into the next product.  Norms are reduced by the last block of each
+// kernel in a fixed order, so every run is bitwise reproducible.
+//
+// Mixed precision: the products accumulate in float-float (see common.cuh):
+// matrix values are stored as (hi, lo) float pairs (8 bytes, like FP64), the
+// input vectors as (hi, lo) pairs, and the scalar recurrences stay in FP64.
+// The all-FP64 path uses plain double values and DFMA.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "skl_internal.hpp"
+#include "common.cuh"
+
+namespace skl {
+
+struct LsqrState {
+    double alpha, beta, alpha_new, rhobar, phibar, nrm_a, nrm_ar, tol;
+    long long it, max_it;
+    int done, flag;
+    unsigned cnt[4];
+};
+
+constexpr int kLThreads = 256;
+
+// Fixed-order reduction of partials[0..np) by one block; result to *out.
+SKL_DEV double block_reduce_partials(const double* partials, int np)
+{
+    __shared__ double red[kLThreads / 32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+    return block_sum(s, red);
+}
+
+// Returns true in the last block to arrive (all blocks' partials visible).
+SKL_DEV bool arrive_last(unsigned* counter)
+{
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
+template <bool MIXED>
+struct VecT {
+    using type = double;
+};
+template <>
+struct VecT<true> {
+    using type = float2;
+};
+
+template <bool MIXED>
+SKL_DEV typename VecT<MIXED>::type store_val(double x)
+{
+    if constexpr (MIXED) {
+        ff f = ff_from_double(x);
+        return make_float2(f.hi, f.lo);
+    } else {
+        return x;
+    }
+}
+
+template <bool MIXED>
+struct Acc {
+    ff a{0.f, 0.f};
+    SKL_DEV void fma_mv(float2 m, float2 x) { ff_fma(a, ff{m.x, m.y}, ff{x.x, x.y}); }
+    SKL_DEV void fma_f(float m, float2 x) { ff_fma_f(a, m, ff{x.x, x.y}); }
+    SKL_DEV void add(const Acc& o) { ff_add(a, o.a); }
+    SKL_DEV Acc shfl_xor(int o) const { Acc r; r.a = ff_shfl_xor(a, o); return r; }
+    SKL_DEV double value() const { return ff_to_double(a); }
+};
+template <>
+struct Acc<false> {
+    double a = 0.0;
+    SKL_DEV void fma_mv(double m, double x) { a = fma(m, x, a); }
+    SKL_DEV void fma_f(double m, double x) { a = fma(m, x, a); }
+    SKL_DEV void add(const Acc& o) { a += o.a; }
+    SKL_DEV Acc shfl_xor(int o) const { Acc r; r.a = __shfl_xor_sync(0xffffffffu, a, o); return r; }
+    SKL_DEV double value() const { return a; }
+};
+
+template <bool MIXED>
+using MatT = typename std::conditional<MIXED, float, double>::type;
+template <bool MIXED>
+using ValT = typename VecT<MIXED>::type;   // stored A values: float2 (hi,lo) or double
+
+// ------------------------------------------------------------- tri_n -----
+// z[cols[i]] = colscale[cols[i]] * sum_{j>=i} M[i][j] v[j]   (Mr row-major)
+// Warp w handles rows w and r-1-w so every warp sees ~r+1 entries.
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED>* __restrict__ v,
+        const int* __restrict__ cols, const double* __restrict__ colscale,
+        ValT<MIXED>* __restrict__ z, const LsqrState* __restrict__ S, int plain_out,
+        double* __restrict__ zplain)
+{
+    if (S && S->done) return;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int npairs = (r + 1) / 2;
+    for (int pidx = gw; pidx < npairs; pidx += nw) {
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            int i = h == 0 ? pidx : r - 1 - pidx;
+            if (h == 1 && i == pidx) break;
+            const MatT<MIXED>* row = Mr + (int64_t)i * ldm;
+            Acc<MIXED> acc;
+            for (int j = i + lane; j < r; j += 32) acc.fma_f(row[j], v[j]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+            if (lane == 0) {
+                int c = cols[i];
+                double val = colscale[c] * acc.value();
+                if (plain_out) zplain[c] = val;
+                else z[c] = store_val<MIXED>(val);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- tri_t -----
+// vh[j] = sum_{i<=j} M[i][j] t[i] - coef * vh[j], coef = beta'/alpha (0 at init)
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED>* __restrict__ t,
+        double* __restrict__ vh, LsqrState* __restrict__ S, int init, double* __restrict__ partials)
+{
+    if (S->done) return;
+    __shared__ double wsum[kLThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const double coef = init ? 0.0 : (S->alpha > 0.0 ? S->beta / S->alpha : 0.0);
+    const int npairs = (r + 1) / 2;
+    double ss = 0.0;
+    for (int pidx = gw; pidx < npairs; pidx += nw) {
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            int j = h == 0 ? pidx : r - 1 - pidx;
+            if (h == 1 && j == pidx) break;
+            const MatT<MIXED>* col = Mc + (int64_t)j * ldm;
+            Acc<MIXED> acc;
+            for (int i = lane; i <= j; i += 32) acc.fma_f(col[i], t[i]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+            if (lane == 0) {
+                double nv = acc.value() - coef * vh[j];
+                vh[j] = nv;
+                ss += nv * nv;
+            }
+        }
+    }
+    if (lane == 0) wsum[wid] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += wsum[q];
+        partials[blockIdx.x] = s;
+    }
+    if (arrive_last(&S->cnt[1])) {
+        double tot = block_reduce_partials(partials, gridDim.x);
+        if (threadIdx.x == 0) {
+            S->alpha_new = sqrt(tot);
+            S->cnt[1] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------- spmv_n (CSR) --
+// uh[i] = sum_j A[i][j] z[j] - coef * uh[i], coef = alpha/beta (0 at init with
+// z = 0 replaced by rhs b);  usplit = split(uh);  beta' = ||uh||.
+template <bool MIXED, int L>
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<MIXED>* __restrict__ cv,
+             int n, int rows_per_block, const ValT<MIXED>* __restrict__ z, double* __restrict__ uh,
+             ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S, double* __restrict__ partials)
+{
+    if (S->done) return;
+    __shared__ double wsum[kLThreads / 32];
+    // Each warp owns 32/L consecutive row slots per pass; the pass count is
+    // uniform across the warp so the full-mask shuffles below always see all
+    // 32 lanes (groups past the last row contribute zero).
+    const int lane = threadIdx.x % L;
+    const int grp = threadIdx.x / L;
+    const int ngrp = kLThreads / L;
+    const double coef = S->beta > 0.0 ? S->alpha / S->beta : 0.0;
+    const int r0 = blockIdx.x * rows_per_block;
+    const int r1 = min(n, r0 + rows_per_block);
+    const int warp_grp0 = (threadIdx.x >> 5) * (32 / L);
+    double ss = 0.0;
+    for (int base = r0 + warp_grp0; base < r1; base += ngrp) {
+        const int i = base + (grp - warp_grp0);
+        const bool active = i < r1;
+        Acc<MIXED> acc;
+        if (active) {
+            const int p1 = rp[i + 1];
+            for (int p = rp[i] + lane; p < p1; p += L) acc.fma_mv(cv[p], z[ci[p]]);
+        }
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+        if (active && lane == 0) {
+            double nv = acc.value() - coef * uh[i];
+            uh[i] = nv;
+            us[i] = store_val<MIXED>(nv);
+            ss += nv * nv;
+        }
+    }
+    ss = warp_sum(ss);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < kLThreads / 32; ++q) s += wsum[q];
+        partials[blockIdx.x] = s;
+    }
+    if (arrive_last(&S->cnt[0])) {
+        double tot = block_reduce_partials(partials, gridDim.x);
+        if (threadIdx.x == 0) {
+            S->beta = sqrt(tot);
+            S->cnt[0] = 0;
+        }
+    }
+}
+
+// --------------------------------------------------------- spmv_t (CSC) --
+// t[i] = colscale[c] * (sum_{p in col c} A[p] u[row p]) / beta,  c = cols[i]
+template <bool MIXED, int L>
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<MIXED>* __restrict__ cv,
+             const int* __restrict__ cols, const double* __restrict__ colscale, int r,
+             const ValT<MIXED>* __restrict__ us, ValT<MIXED>* __restrict__ t,
+             const LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    const int lane = threadIdx.x % L;
+    const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L;
+    const int ng = (gridDim.x * blockDim.x) / L;
+    const int gw0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 / L);  // first group of this warp
+    const double ib = S->beta > 0.0 ? 1.0 / S->beta : 0.0;
+    // warp-uniform trip count (see k_spmv_n_csr)
+    for (int base = gw0; base < r; base += ng) {
+        const int i = base + (g - gw0);
+        const bool active = i < r;
+        Acc<MIXED> acc;
+        int c = 0;
+        if (active) {
+            c = cols[i];
+            const int p1 = cp[c + 1];
+            for (int p = cp[c] + lane; p < p1; p += L) acc.fma_mv(cv[p], us[ri[p]]);
+        }
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+        if (active && lane == 0) t[i] = store_val<MIXED>(colscale[c] * acc.value() * ib);
+    }
+}
+
+// ------------------------------------------------- dense A (column-major) --
+// spmv_n: uh = A(:, cols) z(cols) - coef uh.  Block = 256 rows x all columns
+// of its column chunk; chunk partials are combined by spmv_n_dense_reduce.
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_n_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int* __restrict__ cols,
+               int r, int chunk, const ValT<MIXED>* __restrict__ z, double* __restrict__ part,
+               const LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    const int i = blockIdx.x * kLThreads + threadIdx.x;
+    const int c0 = blockIdx.y * chunk, c1 = min(r, c0 + chunk);
+    if (i >= n) return;
+    Acc<MIXED> acc;
+    for (int c = c0; c < c1; ++c) {
+        const int col = cols[c];
+        acc.fma_mv(A[i + (int64_t)col * lda], z[col]);
+    }
+    part[(int64_t)blockIdx.y * n + i] = acc.value();
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_n_dense_reduce(const double* __restrict__ part, int nchunks, int n, double* __restrict__ uh,
+                      ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S,
+                      double* __restrict__ partials)
+{
+    if (S->done) return;
+    __shared__ double red[kLThreads / 32];
+    const double coef = S->beta > 0.0 ? S->alpha / S->beta : 0.0;
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int q = 0; q < nchunks; ++q) s += part[(int64_t)q * n + i];
+        double nv = s - coef * uh[i];
+        uh[i] = nv;
+        us[i] = store_val<MIXED>(nv);
+        ss += nv * nv;
+    }
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = ss;
+    if (arrive_last(&S->cnt[0])) {
+        double tot = block_reduce_partials(partials, gridDim.x);
+        if (threadIdx.x == 0) {
+            S->beta = sqrt(tot);
+            S->cnt[0] = 0;
+        }
+    }
+}
+
+// spmv_t: one block per selected column, contiguous dot over n rows.
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_t_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int* __restrict__ cols,
+               const double* __restrict__ colscale, int r, const ValT<MIXED>* __restrict__ us,
+               ValT<MIXED>* __restrict__ t, const LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    __shared__ Acc<MIXED> red[kLThreads / 32];
+    const double ib = S->beta > 0.0 ? 1.0 / S->beta : 0.0;
+    for (int i = blockIdx.x; i < r; i += gridDim.x) {
+        const int c = cols[i];
+        const ValT<MIXED>* col = A + (int64_t)c * lda;
+        Acc<MIXED> acc;
+        for (int q = threadIdx.x; q < n; q += kLThreads) acc.fma_mv(col[q], us[q]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Acc<MIXED> s = red[0];
+            for (int q = 1; q < kLThreads / 32; ++q) s.add(red[q]);
+            t[i] = store_val<MIXED>(colscale[c] * s.value() * ib);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- init --
+// uh = b, usplit = split(b), beta = ||b||
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_lsqr_init_u(const double* __restrict__ b, int n, double* __restrict__ uh,
+              ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S, double* __restrict__ partials)
+{
+    __shared__ double red[kLThreads / 32];
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double x = b[i];
+        uh[i] = x;
+        us[i] = store_val<MIXED>(x);
+        ss += x * x;
+    }
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = ss;
+    if (arrive_last(&S->cnt[0])) {
+        double tot = block_reduce_partials(partials, gridDim.x);
+        if (threadIdx.x == 0) {
+            S->beta = sqrt(tot);
+            S->cnt[0] = 0;
+        }
+    }
+}
+
+// After the init products: alpha = ||vh||, v = vh/alpha, w = v, y = 0.
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_lsqr_init_v(int r, double* __restrict__ vh, ValT<MIXED>* __restrict__ vs, double* __restrict__ w,
+              double* __restrict__ y, LsqrState* __restrict__ S)
+{
+    const double alpha = S->alpha_new;
+    const double beta = S->beta;
+    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
+        double v = vh[i] * ia;
+        vs[i] = store_val<MIXED>(v);
+        w[i] = v;
+        y[i] = 0.0;
+    }
+    if (arrive_last(&S->cnt[2])) {
+        if (threadIdx.x == 0) {
+            S->alpha = alpha;
+            S->rhobar = alpha;
+            S->phibar = beta;
+            S->nrm_a = 0.0;
+            S->it = 0;
+            S->flag = 1;
+            S->done = (alpha * beta == 0.0) ? 1 : 0;
+            if (S->done) S->flag = 0;
+            S->cnt[2] = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------- update ---
+template <bool MIXED>
+__global__ void __launch_bounds__(kLThreads)
+k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs,
+              double* __restrict__ w, double* __restrict__ y, LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    const double alpha_old = S->alpha;
+    const double beta = S->beta;
+    // the reference skips the A^T u step when beta == 0 (IterSolver.cpp:242)
+    const double alpha = beta > 0.0 ? S->alpha_new : alpha_old;
+    const double rho = sqrt(S->rhobar * S->rhobar + beta * beta);
+    const double cs = S->rhobar / rho, sn = beta / rho;
+    const double theta = sn * alpha;
+    const double phi = cs * S->phibar;
+    const double t1 = phi / rho, t2 = -theta / rho;
+    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
+        double v = (beta > 0.0) ? vh[i] * ia : 0.0;
+        if (beta > 0.0) vs[i] = store_val<MIXED>(v);
+        double wi = w[i];
+        y[i] += t1 * wi;
+        w[i] = t2 * wi + v;
+    }
+    if (arrive_last(&S->cnt[3])) {
+        if (threadIdx.x == 0) {
+            double nrm_a = S->nrm_a;
+            if (beta > 0.0) nrm_a = sqrt(nrm_a * nrm_a + alpha_old * alpha_old + beta * beta);
+            const double phibar = sn * S->phibar;
+            S->rhobar = -cs * alpha;
+            S->phibar = phibar;
+            S->nrm_a = nrm_a;
+            S->alpha = alpha;
+            S->it += 1;
+            const double nrm_ar = phibar * alpha * fabs(cs);
+            S->nrm_ar = nrm_ar;
+            if (nrm_ar < S->tol * nrm_a * phibar) {
+                S->done = 1;
+                S->flag = 0;
+            } else if (S->it >= S->max_it) {
+                S->done = 1;
+                S->flag = 1;
+            }
+            S->cnt[3] = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side --
+struct LsqrBufs {
+    LsqrState* S;
+    double *uh, *vh, *w, *y, *partials, *dpart;
+    void *us, *vs, *t, *z;
+    int nparts;
+};
+
+static int lanes_for(double avg)
+{
+    if (avg >= 24) return 32;
+    if (avg >= 10) return 16;
+    if (avg >= 5) return 8;
+    return 4;
+}
+
+static const int kRowsPerBlock = 256;
+static const int kDenseChunk = 128;
+
+static int64_t spmv_n_blocks(const LsqrProblem& P)
+{
+    if (P.Ad) return (P.n + kLThreads - 1) / kLThreads;
+    return (P.n + kRowsPerBlock - 1) / kRowsPerBlock;
+}
+
+size_t lsqr_workspace_bytes(const LsqrProblem& P)
+{
+    const size_t vs = P.precision == SKL_PREC_MIXED ? sizeof(float2) : sizeof(double);
+    size_t b = sizeof(LsqrState) + 256;
+    b += 2 * (P.n * sizeof(double) + 256);                   // uh, us
+    b += P.n * vs + 256;
+    b += 4 * (P.r * sizeof(double) + 256);                   // vh, w, y, spare
+    b += 2 * (P.r * vs + 256);                               // vs, t
+    b += P.d * vs + 256;                                     // z
+    int64_t nb = spmv_n_blocks(P);
+    b += (nb + 4096) * sizeof(double) + 256;                 // partials
+    if (P.Ad) b += (size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double) + 256;
+    return b;
+}
+
+static LsqrBufs carve(const LsqrProblem& P, void* work)
+{
+    char* base = (char*)work;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        void* r = base + off;
+        off += (bytes + 255) & ~(size_t)255;
+        return r;
+    };
+    const size_t vsz = P.precision == SKL_PREC_MIXED ? sizeof(float2) : sizeof(double);
+    LsqrBufs B;
+    B.S = (LsqrState*)take(sizeof(LsqrState));
+    B.uh = (double*)take(P.n * sizeof(double));
+    B.us = take(P.n * vsz);
+    B.vh = (double*)take(P.r * sizeof(double));
+    B.w = (double*)take(P.r * sizeof(double));
+    B.y = (double*)take(P.r * sizeof(double));
+    B.vs = take(P.r * vsz);
+    B.t = take(P.r * vsz);
+    B.z = take(P.d * vsz);
+    int64_t nb = spmv_n_blocks(P);
+    B.nparts = (int)(nb + 4096);
+    B.partials = (double*)take(B.nparts * sizeof(double));
+    B.dpart = P.Ad ? (double*)take((size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double))
+                   : nullptr;
+    return B;
+}
+
+template <bool MIXED>
+static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
+{
+    using V = ValT<MIXED>;
+    if (P.Ad) {
+        const int nchunks = (int)((P.r + kDenseChunk - 1) / kDenseChunk);
+        dim3 g((unsigned)((P.n + kLThreads - 1) / kLThreads), nchunks);
+        k_spmv_n_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
+                                                       (int)P.r, kDenseChunk, (const V*)B.z, B.dpart,
+                                                       B.S);
+        k_spmv_n_dense_reduce<MIXED><<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 1024), kLThreads,
+                                       0, st>>>(B.dpart, nchunks, (int)P.n, B.uh, (V*)B.us, B.S,
+                                                B.partials);
+        SKL_LAUNCHED();
+        SKL_LAUNCHED();
+        return;
+    }
+    const unsigned g = (unsigned)spmv_n_blocks(P);
+    const double avg = P.n ? (double)P.nnz / P.n : 0.0;
+    const int L = lanes_for(avg);
+#define SPMV_N(LL) k_spmv_n_csr<MIXED, LL><<<g, kLThreads, 0, st>>>(P.rp, P.ci, (const V*)P.cx, (int)P.n, kRowsPerBlock, (const V*)B.z, B.uh, (V*)B.us, B.S, B.partials)
+    if (L == 32) SPMV_N(32);
+    else if (L == 16) SPMV_N(16);
+    else if (L == 8) SPMV_N(8);
+    else SPMV_N(4);
+#undef SPMV_N
+    SKL_LAUNCHED();
+}
+
+template <bool MIXED>
+static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
+{
+    using V = ValT<MIXED>;
+    if (P.Ad) {
+        unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
+        k_spmv_t_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
+                                                       P.colscale, (int)P.r, (const V*)B.us,
+                                                       (V*)B.t, B.S);
+        SKL_LAUNCHED();
+        return;
+    }
+    const double avg = P.d ? (double)P.nnz / P.d : 0.0;
+    const int L = lanes_for(avg);
+    const int64_t threads = (int64_t)P.r * L;
+    unsigned g = (unsigned)std::min<int64_t>((threads + kLThreads - 1) / kLThreads, 152 * 32);
+#define SPMV_T(LL) k_spmv_t_csc<MIXED, LL><<<g, kLThreads, 0, st>>>(P.cp, P.ri, (const V*)P.rx, P.cols, P.colscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
+    if (L == 32) SPMV_T(32);
+    else if (L == 16) SPMV_T(16);
+    else if (L == 8) SPMV_T(8);
+    else SPMV_T(4);
+#undef SPMV_T
+    SKL_LAUNCHED();
+}
+
+static unsigned tri_blocks(int64_t r)
+{
+    int64_t warps = (r + 1) / 2;
+    int64_t blocks = (warps + (kLThreads / 32) - 1) / (kLThreads / 32);
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * 8));
+}
+
+template <bool MIXED>
+static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
+{
+    using V = ValT<MIXED>;
+    using MT = MatT<MIXED>;
+    const unsigned gt = tri_blocks(P.r);
+    k_tri_n<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
+                                              P.cols, P.colscale, (V*)B.z, B.S, 0, nullptr);
+    SKL_LAUNCHED();
+    launch_spmv_n<MIXED>(P, B, st);
+    launch_spmv_t<MIXED>(P, B, st);
+    k_tri_t<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+                                              B.S, 0, B.partials);
+    SKL_LAUNCHED();
+    unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
+    k_lsqr_update<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
+    SKL_LAUNCHED();
+}
+
+template <bool MIXED>
+static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, int64_t max_it,
+                           double* y_out, void* work, void* host_pinned, cudaStream_t st)
+{
+    using V = ValT<MIXED>;
+    using MT = MatT<MIXED>;
+    LsqrBufs B = carve(P, work);
+    LsqrState init{};
+    init.tol = tol;
+    init.max_it = max_it;
+    SKL_CUDA(cudaMemcpyAsync(B.S, &init, sizeof(LsqrState), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(B.z, 0, P.d * sizeof(V), st));
+    // beta_1 u_1 = b ; alpha_1 v_1 = Abar^T u_1
+    unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.n + 255) / 256, 1024));
+    k_lsqr_init_u<MIXED><<<gi, kLThreads, 0, st>>>(b, (int)P.n, B.uh, (V*)B.us, B.S, B.partials);
+    SKL_LAUNCHED();
+    launch_spmv_t<MIXED>(P, B, st);
+    const unsigned gt = tri_blocks(P.r);
+    k_tri_t<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+                                              B.S, 1, B.partials);
+    SKL_LAUNCHED();
+    unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
+    k_lsqr_init_v<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
+    SKL_LAUNCHED();
+
+    // Capture a block of iterations once, replay until the device says done.
+    const int kIterPerGraph = 4;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = st;
+    SKL_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int q = 0; q < kIterPerGraph; ++q) launch_iteration<MIXED>(P, B, cap);
+    SKL_CUDA(cudaStreamEndCapture(cap, &graph));
+    SKL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    struct Flags { int done; int flag; long long it; };
+    volatile LsqrState* hs = (volatile LsqrState*)host_pinned;
+    int64_t launched = 0;
+    cudaEvent_t ev;
+    SKL_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    bool done = false;
+    trace_phase(st, "lsqr: init");
+    const auto t_start = std::chrono::steady_clock::now();
+    while (!done) {
+        // host-side bound: a replay loop that runs past a minute reports a timeout
+        if (std::chrono::steady_clock::now() - t_start > std::chrono::seconds(60)) {
+            cudaEventDestroy(ev);
+            cudaGraphExecDestroy(exec);
+            cudaGraphDestroy(graph);
+            fail(SKL_ERR_TIMEOUT, "LSQR replay loop exceeded 60 s");
+        }
+        SKL_CUDA(cudaGraphLaunch(exec, st));
+        launched += kIterPerGraph;
+        for (int q = 0; q < 5 * kIterPerGraph; ++q) SKL_LAUNCHED();
+        SKL_CUDA(cudaMemcpyAsync((void*)hs, B.S, sizeof(LsqrState), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaEventRecord(ev, st));
+        SKL_CUDA(cudaEventSynchronize(ev));
+        done = hs->done != 0 || launched >= max_it + kIterPerGraph;
+    }
+    trace_phase(st, "lsqr: done");
+    LsqrResult res;
+    res.flag = hs->flag;
+    res.it = hs->it;
+    SKL_CUDA(cudaEventDestroy(ev));
+    SKL_CUDA(cudaGraphExecDestroy(exec));
+    SKL_CUDA(cudaGraphDestroy(graph));
+    SKL_CUDA(cudaMemcpyAsync(y_out, B.y, P.r * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    return res;
+}
+
+LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t max_it, double* y,
+                    void* work, unsigned* status, void* host_pinned, cudaStream_t st)
+{
+    (void)status;
+    if (P.precision == SKL_PREC_MIXED) return run_impl<true>(P, b, tol, max_it, y, work, host_pinned, st);
+    return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st);
+}
+
+// x_full[cols[i]] = colscale[cols[i]] * (M yv)[i] (FP64 output), other entries untouched.
+__global__ void k_split_vec(const double* __restrict__ x, int n, float2* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        ff f = ff_from_double(x[i]);
+        out[i] = make_float2(f.hi, f.lo);
+    }
+}
+
+void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
+                   cudaStream_t st)
+{
+    if (P.r <= 0) return;
+    const unsigned gt = tri_blocks(P.r);
+    if (P.precision == SKL_PREC_MIXED) {
+        float2* ys = (float2*)scratch;
+        k_split_vec<<<(unsigned)((P.r + 255) / 256), 256, 0, st>>>(yv, (int)P.r, ys);
+        k_tri_n<true><<<gt, kLThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, ys, P.cols,
+                                                 P.colscale, nullptr, nullptr, 1, xfull);
+        SKL_LAUNCHED();
+    } else {
+        k_tri_n<false><<<gt, kLThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv, P.cols,
+                                                  P.colscale, nullptr, nullptr, 1, xfull);
+    }
+    SKL_LAUNCHED();
+}
+
+// ------------------------------------------------- FP64 residual checks --
+// r = b - A x with plain FP64 (CSR rows or dense columns); partial ||r||^2.
+__global__ void __launch_bounds__(kLThreads)
+k_residual_csr(const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ cx,
+               int n, const double* __restrict__ x, const double* __restrict__ b,
+               double* __restrict__ r, double* __restrict__ part)
+{
+    __shared__ double red[kLThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double ss = 0.0;
+    for (int i = gw; i < n; i += nw) {
+        double acc = 0.0;
+        for (int p = rp[i] + lane; p < rp[i + 1]; p += 32) acc = fma(cx[p], x[ci[p]], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            double v = b[i] - acc;
+            r[i] = v;
+            ss += v * v;
+        }
+    }
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+__global__ void __launch_bounds__(kLThreads)
+k_residual_dense(const double* __restrict__ A, int64_t lda, int n, int d,
+                 const double* __restrict__ x, const double* __restrict__ b,
+                 double* __restrict__ r, double* __restrict__ part)
+{
+    __shared__ double red[kLThreads / 32];
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int j = 0; j < d; ++j) acc = fma(A[i + (int64_t)j * lda], x[j], acc);
+        double v = b[i] - acc;
+        r[i] = v;
+        ss += v * v;
+    }
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+// g = A^T r over all d columns, partial ||g||^2
+__global__ void __launch_bounds__(kLThreads)
+k_atr_csc(const int* __restrict__ cp, const int* __restrict__ ri, const double* __restrict__ rx,
+          int d, const double* __restrict__ r, double* __restrict__ part)
+{
+    __shared__ double red[kLThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double ss = 0.0;
+    for (int j = gw; j < d; j += nw) {
+        double acc = 0.0;
+        for (int p = cp[j] + lane; p < cp[j + 1]; p += 32) acc = fma(rx[p], r[ri[p]], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) ss += acc * acc;
+    }
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+__global__ void __launch_bounds__(kLThreads)
+k_atr_dense(const double* __restrict__ A, int64_t lda, int n, int d, const double* __restrict__ r,
+            double* __restrict__ part)
+{
+    __shared__ double red[kLThreads / 32];
+    double ss = 0.0;
+    for (int j = blockIdx.x; j < d; j += gridDim.x) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(A[i + (int64_t)j * lda], r[i], acc);
+        acc = block_sum(acc, red);
+        ss += acc * acc;
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+__global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out)
+{
+    __shared__ double red[kLThreads / 32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = sqrt(s);
+}
+
+// out[0] = ||b - A x||, out[1] = ||A^T (b - A x)||; FP64 throughout.
+void residual_and_backward(const LsqrProblem& P, const double* x, const double* b, double* r,
+                           double* part, double* out, cudaStream_t st)
+{
+    const int np = 512;
+    if (P.Ad64) {
+        k_residual_dense<<<np, kLThreads, 0, st>>>(P.Ad64, P.lda64, (int)P.n, (int)P.d, x, b, r, part);
+        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
+        k_atr_dense<<<np, kLThreads, 0, st>>>(P.Ad64, P.lda64, (int)P.n, (int)P.d, r, part);
+        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out + 1);
+    } else {
+        k_residual_csr<<<np, kLThreads, 0, st>>>(P.rp, P.ci, P.cx64, (int)P.n, x, b, r, part);
+        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
+        k_atr_csc<<<np, kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, (int)P.d, r, part);
+        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out + 1);
+    }
+    for (int q = 0; q < 4; ++q) SKL_LAUNCHED();
+}
+
+// (hi, lo) float pairs of FP64 values (matrix storage of the mixed path).
+__global__ void k_split_vals(const double* __restrict__ x, int64_t n, float2* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        ff f = ff_from_double(x[i]);
+        out[i] = make_float2(f.hi, f.lo);
+    }
+}
+
+void split_values(const double* x, int64_t n, float2* out, cudaStream_t st)
+{
+    if (n <= 0) return;
+    unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32);
+    k_split_vals<<<g, 256, 0, st>>>(x, n, out);
+    SKL_LAUNCHED();
+}
+
+// Dense matrix variant: column-major n x d with lda -> packed n x d float2.
+__global__ void k_split_dense(const double* __restrict__ A, int64_t lda, int64_t n, int64_t d,
+                              float2* __restrict__ out)
+{
+    int64_t total = n * d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = e % n, j = e / n;
+        ff f = ff_from_double(A[i + j * lda]);
+        out[e] = make_float2(f.hi, f.lo);
+    }
+}
+
+void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out, cudaStream_t st)
+{
+    if (n * d <= 0) return;
+    k_split_dense<<<152 * 32, 256, 0, st>>>(A, lda, n, d, out);
+    SKL_LAUNCHED();
+}
+
+// Row-major copy of the r x r upper triangle (for the forward triangular product).
+template <typename T>
+__global__ void k_transpose_upper(const T* __restrict__ Mc, int64_t ldm, int r, T* __restrict__ Mr)
+{
+    __shared__ T tile[32][33];
+    const int bi = blockIdx.x * 32, bj = blockIdx.y * 32;
+    if (bi > bj + 31) return;   // tile entirely below the diagonal
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        int i = bi + threadIdx.x, j = bj + q;
+        tile[q][threadIdx.x] = (i < r && j < r) ? Mc[i + (int64_t)j * ldm] : T(0);
+    }
+    __syncthreads();
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        int j = bj + threadIdx.x, i = bi + q;
+        if (i < r && j < r) Mr[j + (int64_t)i * ldm] = tile[threadIdx.x][q];
+    }
+}
+
+template <typename T>
+void transpose_upper(const T* Mc, int64_t ldm, int64_t r, T* Mr, cudaStream_t st)
+{
+    if (r <= 0) return;
+    dim3 g((unsigned)((r + 31) / 32), (unsigned)((r + 31) / 32));
+    k_transpose_upper<T><<<g, dim3(32, 8), 0, st>>>(Mc, ldm, (int)r, Mr);
+    SKL_LAUNCHED();
+}
+template void transpose_upper<float>(const float*, int64_t, int64_t, float*, cudaStream_t);
+template void transpose_upper<double>(const double*, int64_t, int64_t, double*, cudaStream_t);
+
+}  // namespace skl

@@ -1,0 +1,574 @@
+// skl_api.cpp -- C ABI entry points and the solve pipelines.
+//
+// Sparse pipeline (ls_sparse_spqr, src/ls_sparse_spqr.cpp:79-214):
+//   upload + validate CSC, CSR copy                    (device)
+//   hash stream (glibc-compatible, bit-exact)          (host thread, overlapped)
+//   SA = S*A (equilibrated), Sb = S*b                  k_sketch.cu
+//   randomized CPQR of SA, c = Q^T Sb                  k_qr.cu
+//   rank (relative |R_ii| rule), M = R11^{-1}, rcond   k_trinv.cu
+//   xs = D P1 M c, r_s = b - A xs, early exit          k_lsqr.cu
+//   LSQR on A P1 D M from r_s, x = D P1 M (c + y)      k_lsqr.cu
+//   FP64 residual / backward error, optional restarts
+// Dense pipeline (ls_dense_hashing_blendenpik, src/ls_dense_hashing_blendenpik.cpp:23-149)
+// follows the same steps with the DHT-hashing sketch and dense products.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <mutex>
+#include <thread>
+#include <type_traits>
+#include <vector>
+
+#include "skl_internal.hpp"
+
+namespace skl {
+
+// ------------------------------------------------------------- errors ----
+static thread_local std::string t_last_error;
+static thread_local int64_t t_launches = 0;
+
+void fail(skl_status s, const std::string& msg) { throw Error(s, msg); }
+
+void check_cuda(cudaError_t e, const char* what, const char* file, int line)
+{
+    if (e != cudaSuccess) {
+        char buf[512];
+        snprintf(buf, sizeof buf, "CUDA error %s (%d) in %s at %s:%d", cudaGetErrorString(e),
+                 (int)e, what, file, line);
+        throw Error(SKL_ERR_CUDA, buf);
+    }
+}
+
+static int trace_enabled()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("SKILLS_TRACE");
+        v = (e && e[0] == '1') ? 1 : 0;
+    }
+    return v;
+}
+
+void trace_phase(cudaStream_t st, const char* name)
+{
+    if (!trace_enabled()) return;
+    static auto t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaStreamSynchronize(st);
+    double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    fprintf(stderr, "[skl] %10.3f ms  %s  (%s)\n", ms, name, cudaGetErrorString(e));
+    fflush(stderr);
+}
+
+void note_launch() { ++t_launches; }
+int64_t launches_since_reset() { return t_launches; }
+void reset_launch_count() { t_launches = 0; }
+
+template <typename F>
+static skl_status guarded(F&& fn)
+{
+    try {
+        t_last_error.clear();
+        fn();
+        return SKL_OK;
+    } catch (const Error& e) {
+        t_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        t_last_error = "host allocation failed";
+        return SKL_ERR_ALLOC;
+    } catch (const std::exception& e) {
+        t_last_error = e.what();
+        return SKL_ERR_INVALID;
+    }
+}
+
+skl_status run_guarded(void (*fn)(void*), void* arg)
+{
+    return guarded([&] { fn(arg); });
+}
+
+// -------------------------------------------------------------- arena ----
+void Arena::reserve(size_t bytes)
+{
+    if (bytes <= cap_) return;
+    release();
+    bytes = (bytes + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+    cudaError_t e = cudaMalloc((void**)&base_, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        base_ = nullptr;
+        fail(SKL_ERR_ALLOC, "device allocation of " + std::to_string(bytes >> 20) + " MiB failed");
+    }
+    cap_ = bytes;
+    used_ = 0;
+}
+
+void* Arena::take(size_t bytes)
+{
+    size_t b = (bytes + 255) & ~(size_t)255;
+    if (used_ + b > cap_) fail(SKL_ERR_ALLOC, "arena exhausted (internal sizing error)");
+    void* p = base_ + used_;
+    used_ += b;
+    return p;
+}
+
+void Arena::release()
+{
+    if (base_) cudaFree(base_);
+    base_ = nullptr;
+    cap_ = used_ = 0;
+}
+
+// ------------------------------------------------------------ contexts ----
+static std::mutex g_ctx_mu;
+static std::vector<Context*> g_ctx;
+
+Context& context(int device)
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        fail(SKL_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= ndev) fail(SKL_ERR_INVALID, "device ordinal out of range");
+    if ((int)g_ctx.size() < ndev) g_ctx.resize(ndev, nullptr);
+    SKL_CUDA(cudaSetDevice(device));
+    if (!g_ctx[device]) {
+        cudaDeviceProp prop;
+        SKL_CUDA(cudaGetDeviceProperties(&prop, device));
+        if (prop.major != 10)
+            fail(SKL_ERR_NO_DEVICE, std::string("device is not a Blackwell sm_10x part: ") + prop.name);
+        Context* c = new Context();
+        c->device = device;
+        SKL_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        for (auto& e : c->ev) SKL_CUDA(cudaEventCreate(&e));
+        SKL_CUDA(cudaMalloc((void**)&c->dev_status, 256));
+        SKL_CUDA(cudaMemset(c->dev_status, 0, 256));
+        c->host_pinned_bytes = 4096;
+        SKL_CUDA(cudaMallocHost(&c->host_pinned, c->host_pinned_bytes));
+        g_ctx[device] = c;
+    }
+    return *g_ctx[device];
+}
+
+void release_all_contexts()
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    for (size_t d = 0; d < g_ctx.size(); ++d) {
+        Context* c = g_ctx[d];
+        if (!c) continue;
+        cudaSetDevice((int)d);
+        cudaStreamSynchronize(c->stream);
+        c->arena.release();
+        c->staging.release();
+        for (auto& e : c->ev) cudaEventDestroy(e);
+        cudaFree(c->dev_status);
+        cudaFreeHost(c->host_pinned);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        g_ctx[d] = nullptr;
+    }
+}
+
+// ------------------------------------------------------------- helpers ---
+static float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+static int64_t round_up(int64_t x, int64_t q) { return (x + q - 1) / q * q; }
+
+static void check_opts(const skl_opts& o)
+{
+    if (!(o.gamma > 0.0) || !std::isfinite(o.gamma)) fail(SKL_ERR_INVALID, "gamma must be > 0");
+    if (o.k < 1) fail(SKL_ERR_INVALID, "k must be >= 1");
+    if (o.max_it < 0) fail(SKL_ERR_INVALID, "max_it must be >= 0");
+    if (o.precision != SKL_PREC_MIXED && o.precision != SKL_PREC_FP64)
+        fail(SKL_ERR_INVALID, "unknown precision");
+}
+
+static unsigned read_status(Context& C)
+{
+    unsigned v = 0;
+    SKL_CUDA(cudaMemcpyAsync(C.host_pinned, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                             C.stream));
+    SKL_CUDA(cudaStreamSynchronize(C.stream));
+    v = *(unsigned*)C.host_pinned;
+    return v;
+}
+
+// Device-resident inputs of a sparse solve after upload/validation.
+struct SparseDev {
+    int64_t n, d, nnz;
+    const int64_t* Ap; const int64_t* Ai; const double* Ax; const double* b;
+};
+
+// ------------------------------------------------------- sparse solve ---
+template <typename T>
+static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, const skl_opts& o,
+                            skl_info& info, const int64_t* host_p, bool timing_upload,
+                            std::thread* hash_thread, std::vector<uint32_t>* host_hidx)
+{
+    cudaStream_t st = C.stream;
+    const int64_t n = in.n, d = in.d, nnz = in.nnz;
+    const int64_t k = o.k;
+    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+    if (k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
+    if (m > 0x7fffffff || nnz > 0x7fffffff || n > 0x7fffffff)
+        fail(SKL_ERR_INVALID, "problem too large for 32-bit device indices");
+    const bool mixed = std::is_same<T, float>::value;
+    const int64_t ld = round_up(m, 32);
+    const int64_t mn = std::min(m, d);
+    info.sketch_rows = m;
+
+    // ---- workspace layout (sized once, then carved) ----
+    const size_t vsz = mixed ? sizeof(float2) : sizeof(double);
+    const size_t qr_ws = cpqr_workspace_bytes<T>(m, d);
+    const size_t inv_ws = trinv_workspace_bytes<T>(d) + (size_t)d * d * sizeof(T);
+    LsqrProblem Pq;
+    Pq.n = n; Pq.d = d; Pq.nnz = nnz; Pq.r = d; Pq.precision = o.precision;
+    const size_t lsqr_ws = lsqr_workspace_bytes(Pq);
+    const size_t csr_scr = build_csr_scratch_ints(n, nnz) * sizeof(int);
+    const size_t bkt_scr = build_buckets_scratch_ints(m, n * k) * sizeof(int);
+    Sizer S;
+    S.add<int>(d + 1); S.add<int>(nnz); S.add<int>(n + 1); S.add<int>(nnz); S.add<double>(nnz);
+    S.add<char>(mixed ? (int64_t)(2 * nnz * sizeof(float2)) : 0);
+    S.add<unsigned>(n * k); S.add<int>(m + 1); S.add<unsigned>(n * k);
+    S.add<T>(ld * d); S.add<double>(d); S.add<double>(d); S.add<double>(m);
+    S.add<int>(d); S.add<T>(mn); S.add<int>(4);
+    S.add<T>(d * d); S.add<T>(d * d); S.add<double>(4);
+    S.add<double>(d); S.add<double>(n); S.add<double>(d); S.add<double>(1024); S.add<double>(8);
+    S.add<char>((int64_t)std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
+    S.add<float2>(d);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    Arena& Ar = C.arena;
+    int* cp = Ar.alloc<int>(d + 1);
+    int* ri = Ar.alloc<int>(nnz);
+    int* rp = Ar.alloc<int>(n + 1);
+    int* ci = Ar.alloc<int>(nnz);
+    double* cx = Ar.alloc<double>(nnz);
+    float2* cx2 = mixed ? (float2*)Ar.take(nnz * sizeof(float2)) : nullptr;
+    float2* rx2 = mixed ? (float2*)Ar.take(nnz * sizeof(float2)) : nullptr;
+    unsigned* hidx = Ar.alloc<unsigned>(n * k);
+    int* bptr = Ar.alloc<int>(m + 1);
+    unsigned* bent = Ar.alloc<unsigned>(n * k);
+    T* SA = Ar.alloc<T>(ld * d);
+    double* colnorm = Ar.alloc<double>(d);
+    double* colscale = Ar.alloc<double>(d);
+    double* cvec = Ar.alloc<double>(m);
+    int* jpvt = Ar.alloc<int>(d);
+    T* tau = Ar.alloc<T>(mn);
+    int* dint = Ar.alloc<int>(4);
+    T* Mc = Ar.alloc<T>(d * d);
+    T* Mr = Ar.alloc<T>(d * d);
+    double* norms = Ar.alloc<double>(4);
+    double* yv = Ar.alloc<double>(d);
+    double* rs = Ar.alloc<double>(n);
+    double* xacc = Ar.alloc<double>(d);
+    double* part = Ar.alloc<double>(1024);
+    double* scal = Ar.alloc<double>(8);
+    void* work = Ar.take(std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
+    float2* ysplit = Ar.alloc<float2>(d);
+    (void)host_p;
+
+    cudaEvent_t* ev = C.ev;
+    SKL_CUDA(cudaEventRecord(ev[1], st));
+    // ---- validate + narrow + CSR ----
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+    csc_narrow(in.Ap, in.Ai, in.Ax, n, d, nnz, cp, ri, C.dev_status, st);
+    build_csr(cp, ri, in.Ax, n, d, nnz, rp, ci, cx, (int*)work, st);
+    if (mixed) {
+        split_values(cx, nnz, cx2, st);
+        split_values(in.Ax, nnz, rx2, st);
+    }
+    // ---- hash stream (host) -> device buckets ----
+    if (hash_thread) {
+        hash_thread->join();
+        SKL_CUDA(cudaMemcpyAsync(hidx, host_hidx->data(), n * k * sizeof(unsigned),
+                                 cudaMemcpyHostToDevice, st));
+    }
+    unsigned bad = read_status(C);
+    if (bad & 1u) fail(SKL_ERR_INVALID, "CSC column pointers are not a valid structure");
+    if (bad & 2u) fail(SKL_ERR_INVALID, "CSC row index out of range");
+    if (bad & 4u) fail(SKL_ERR_NONFINITE, "A contains NaN or Inf");
+    trace_phase(st, "csr+validate");
+    build_buckets(hidx, n, (int)k, m, bptr, bent, (int*)work, st);
+    trace_phase(st, "buckets");
+    SKL_CUDA(cudaEventRecord(ev[2], st));
+    // ---- sketch ----
+    sketch_sparse<T>(cp, ri, in.Ax, n, d, hidx, (int)k, m, SA, ld, 1, colnorm, colscale, st);
+    sketch_rhs(bptr, bent, m, (int)k, in.b, cvec, st);
+    trace_phase(st, "sketch");
+    SKL_CUDA(cudaEventRecord(ev[3], st));
+    // ---- randomized CPQR, c = Q^T S b ----
+    cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1);
+    trace_phase(st, "cpqr");
+    SKL_CUDA(cudaEventRecord(ev[4], st));
+    // ---- rank, inverse, condition ----
+    double rel = o.rank_tol;
+    if (!(rel > 0.0)) rel = mixed ? 1e-5 : 20.0 * (double)(m + d) * 2.220446049250313e-16;
+    int64_t rank = count_rank<T>(SA, ld, mn, 0.0, rel, dint, (int*)C.host_pinned, st);
+    if (rank == 0) fail(SKL_ERR_RANK_ZERO, "SPQR Factorization fails");
+    info.rank = rank;
+    trinv_upper<T>(SA, ld, rank, 0.0, Mc, rank, norms, work, st);
+    SKL_CUDA(cudaMemcpyAsync(C.host_pinned, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    double nr = ((double*)C.host_pinned)[0], nm = ((double*)C.host_pinned)[1];
+    double rcond = (nr > 0 && nm > 0) ? 1.0 / (nr * nm) : 0.0;
+    info.rcond_r11 = rcond;
+    info.success = rcond > o.rcond_threshold ? 1 : 0;
+    if (!info.success && o.perturb != 0.0) {
+        trinv_upper<T>(SA, ld, rank, o.perturb, Mc, rank, norms, work, st);
+    }
+    transpose_upper<T>(Mc, rank, rank, Mr, st);
+    trace_phase(st, "rank+inverse");
+    LsqrProblem P;
+    P.n = n; P.d = d; P.nnz = nnz;
+    P.rp = rp; P.ci = ci; P.cx = mixed ? (const void*)cx2 : (const void*)cx;
+    P.cp = cp; P.ri = ri; P.rx = mixed ? (const void*)rx2 : (const void*)in.Ax;
+    P.cx64 = cx; P.rx64 = in.Ax;
+    P.cols = jpvt; P.colscale = colscale;
+    P.M = Mc; P.Mrow = Mr; P.ldm = rank; P.r = rank; P.precision = o.precision;
+    // ---- explicit sketch solution xs = D P1 M c ----
+    SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
+    precond_apply(P, cvec, x_dev, ysplit, st);
+    residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
+    trace_phase(st, "explicit solution");
+    SKL_CUDA(cudaEventRecord(ev[5], st));
+    SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    double rnorm = ((double*)C.host_pinned)[0];
+    info.explicit_residual = rnorm;
+    info.it = 0;
+    info.flag = 0;
+    // ||A||_F from the column norms
+    double fro = 0.0;
+    {
+        std::vector<double> cn((size_t)d);
+        SKL_CUDA(cudaMemcpyAsync(cn.data(), colnorm, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        for (double v : cn) fro += v * v;
+        fro = std::sqrt(fro);
+    }
+    double be = (rnorm > 0 && fro > 0) ? ((double*)C.host_pinned)[1] / (fro * rnorm) : 0.0;
+    if (!(rnorm < o.abs_tol)) {
+        // ---- LSQR from r_s; x = D P1 M (c + y) ----
+        int64_t total_it = 0;
+        int flag = 1;
+        int64_t restarts = 0;
+        const double btol = o.backward_tol;
+        // first solve
+        LsqrResult R = lsqr_run(P, rs, o.it_tol, o.max_it, yv, work, C.dev_status, C.host_pinned, st);
+        total_it += R.it;
+        flag = R.flag;
+        // y <- y + c (first r entries), x = D P1 M y
+        {
+            auto add_c = [&](double* yy) {
+                std::vector<double> h((size_t)rank), hc((size_t)rank);
+                SKL_CUDA(cudaMemcpyAsync(h.data(), yy, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
+                SKL_CUDA(cudaMemcpyAsync(hc.data(), cvec, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
+                SKL_CUDA(cudaStreamSynchronize(st));
+                for (int64_t i = 0; i < rank; ++i) h[(size_t)i] += hc[(size_t)i];
+                SKL_CUDA(cudaMemcpyAsync(yy, h.data(), rank * sizeof(double), cudaMemcpyHostToDevice, st));
+                SKL_CUDA(cudaStreamSynchronize(st));
+            };
+            add_c(yv);
+        }
+        SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
+        precond_apply(P, yv, x_dev, ysplit, st);
+        residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
+        SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        rnorm = ((double*)C.host_pinned)[0];
+        be = (rnorm > 0 && fro > 0) ? ((double*)C.host_pinned)[1] / (fro * rnorm) : 0.0;
+        // restarts from the FP64 residual while the backward error target is missed
+        while (btol > 0.0 && be > btol && restarts < o.max_refine && total_it < o.max_it) {
+            ++restarts;
+            R = lsqr_run(P, rs, o.it_tol, o.max_it - total_it, yv, work, C.dev_status, C.host_pinned, st);
+            total_it += R.it;
+            flag = R.flag;
+            SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
+            precond_apply(P, yv, xacc, ysplit, st);
+            // x += xacc
+            std::vector<double> hx((size_t)d), ha((size_t)d);
+            SKL_CUDA(cudaMemcpyAsync(hx.data(), x_dev, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaMemcpyAsync(ha.data(), xacc, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            for (int64_t j = 0; j < d; ++j) hx[(size_t)j] += ha[(size_t)j];
+            SKL_CUDA(cudaMemcpyAsync(x_dev, hx.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+            residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
+            SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            rnorm = ((double*)C.host_pinned)[0];
+            be = (rnorm > 0 && fro > 0) ? ((double*)C.host_pinned)[1] / (fro * rnorm) : 0.0;
+        }
+        info.it = total_it;
+        info.flag = flag;
+    }
+    SKL_CUDA(cudaEventRecord(ev[6], st));
+    SKL_CUDA(cudaEventSynchronize(ev[6]));
+    info.residual_norm = rnorm;
+    info.backward_error = be;
+    info.t_setup_ms = elapsed(ev[1], ev[2]);
+    info.t_sketch_ms = elapsed(ev[2], ev[3]);
+    info.t_qr_ms = elapsed(ev[3], ev[4]);
+    info.t_precond_ms = elapsed(ev[4], ev[5]);
+    info.t_lsqr_ms = elapsed(ev[5], ev[6]);
+    info.t_total_ms = elapsed(timing_upload ? ev[0] : ev[1], ev[6]);
+    if (timing_upload) info.t_upload_ms = elapsed(ev[0], ev[1]);
+    unsigned stt = read_status(C);
+    if (stt & 1u) fail(SKL_ERR_TIMEOUT, "a bounded device wait gave up");
+}
+
+static void fill_default(skl_opts* o)
+{
+    std::memset(o, 0, sizeof(*o));
+    o->gamma = 1.1;
+    o->k = 3;
+    o->abs_tol = 1e-8;
+    o->it_tol = 1e-6;
+    o->max_it = 10000;
+    o->rcond_threshold = 1e-10;
+    o->perturb = 1e-10;
+    o->rcond = 1e-10;
+    o->rank_tol = 0.0;
+    o->precision = SKL_PREC_MIXED;
+    o->use_cpqr = 1;
+    o->seed_mode = 0;
+    o->seed = 0;
+    o->wisdom = 0;
+    o->backward_tol = 0.0;
+    o->max_refine = 3;
+    o->device = 0;
+}
+
+static void validate_csc_header(const skl_csc* A)
+{
+    if (!A) fail(SKL_ERR_INVALID, "A is null");
+    if (A->m < 0 || A->n < 0) fail(SKL_ERR_INVALID, "negative dimension");
+    if (A->n > 0 && (!A->p)) fail(SKL_ERR_INVALID, "A->p is null");
+    if (A->m < A->n) fail(SKL_ERR_NOT_OVERDETERMINED, "Matrix is not overdetermined.");
+}
+
+static void sparse_solve_common(const skl_csc* A, const double* b, double* x, const skl_opts* opts,
+                                skl_info* info, bool host)
+{
+    skl_opts o;
+    if (opts) o = *opts;
+    else fill_default(&o);
+    check_opts(o);
+    validate_csc_header(A);
+    if (!b || !x) fail(SKL_ERR_INVALID, "b or x is null");
+    skl_info inf;
+    std::memset(&inf, 0, sizeof inf);
+    const int64_t n = A->m, d = A->n;
+    if (d == 0) {
+        if (info) *info = inf;
+        return;
+    }
+    Context& C = context(o.device);
+    reset_launch_count();
+    cudaStream_t st = C.stream;
+    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+    if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
+    // host hash stream in a worker thread (serial Fisher-Yates)
+    std::vector<uint32_t> hh((size_t)(n * o.k));
+    double hash_ms = 0.0;
+    std::thread th([&]() {
+        auto t0 = std::chrono::steady_clock::now();
+        if (o.seed_mode) rng_srand(o.seed);
+        rng_lock();
+        gen_hash_packed(m, n, o.k, hh.data());
+        rng_unlock();
+        hash_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    });
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() { if (t.joinable()) t.join(); }
+    } joiner{th};
+    SparseDev in;
+    in.n = n;
+    in.d = d;
+    int64_t nnz = 0;
+    SKL_CUDA(cudaEventRecord(C.ev[0], st));
+    if (host) {
+        if (!A->p) fail(SKL_ERR_INVALID, "A->p is null");
+        nnz = A->p[d];
+        if (nnz < 0) fail(SKL_ERR_INVALID, "negative nnz");
+        if (nnz > 0 && (!A->i || !A->x)) fail(SKL_ERR_INVALID, "A->i or A->x is null");
+        Sizer S;
+        S.add<int64_t>(d + 1); S.add<int64_t>(nnz); S.add<double>(nnz); S.add<double>(n);
+        S.add<double>(d);
+        C.staging.reserve(S.bytes());
+        C.staging.reset();
+        int64_t* Ap = C.staging.alloc<int64_t>(d + 1);
+        int64_t* Ai = C.staging.alloc<int64_t>(nnz);
+        double* Ax = C.staging.alloc<double>(nnz);
+        double* bd = C.staging.alloc<double>(n);
+        double* xd = C.staging.alloc<double>(d);
+        SKL_CUDA(cudaMemcpyAsync(Ap, A->p, (d + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        if (nnz > 0) {
+            SKL_CUDA(cudaMemcpyAsync(Ai, A->i, nnz * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            SKL_CUDA(cudaMemcpyAsync(Ax, A->x, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        in.Ap = Ap; in.Ai = Ai; in.Ax = Ax; in.b = bd; in.nnz = nnz;
+        if (o.precision == SKL_PREC_MIXED)
+            sparse_pipeline<float>(C, in, xd, o, inf, A->p, true, &th, &hh);
+        else
+            sparse_pipeline<double>(C, in, xd, o, inf, A->p, true, &th, &hh);
+        SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+    } else {
+        SKL_CUDA(cudaMemcpyAsync(C.host_pinned, A->p + d, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        nnz = *(int64_t*)C.host_pinned;
+        in.Ap = A->p; in.Ai = A->i; in.Ax = A->x; in.b = b; in.nnz = nnz;
+        if (o.precision == SKL_PREC_MIXED)
+            sparse_pipeline<float>(C, in, x, o, inf, nullptr, false, &th, &hh);
+        else
+            sparse_pipeline<double>(C, in, x, o, inf, nullptr, false, &th, &hh);
+    }
+    inf.t_host_hash_ms = hash_ms;
+    inf.kernel_launches = launches_since_reset();
+    if (info) *info = inf;
+}
+
+}  // namespace skl
+
+using namespace skl;
+
+extern "C" {
+
+void skl_default_opts(skl_opts* opts)
+{
+    if (opts) fill_default(opts);
+}
+
+const char* skl_last_error(void) { return t_last_error.c_str(); }
+
+const char* skl_version(void) { return "skills_gb300 0.1 (sm_103a)"; }
+
+skl_status skl_sparse_solve(const skl_csc* A, const double* b, double* x, const skl_opts* opts,
+                            skl_info* info)
+{
+    return guarded([&] { sparse_solve_common(A, b, x, opts, info, true); });
+}
+
+skl_status skl_sparse_solve_device(const skl_csc* A, const double* b, double* x,
+                                   const skl_opts* opts, skl_info* info)
+{
+    return guarded([&] { sparse_solve_common(A, b, x, opts, info, false); });
+}
+
+void skl_finalize(void) { release_all_contexts(); }
+
+}  // extern "C"

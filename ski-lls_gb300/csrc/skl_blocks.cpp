@@ -1,0 +1,184 @@
+// skl_blocks.cpp -- building-block entry points of the C ABI: each runs one
+// stage of the GPU solve path on host data, so the stage can be checked in
+// isolation against the reference's function of the same role.
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <vector>
+
+#include "skl_internal.hpp"
+
+namespace skl {
+
+static skl_status guard(const std::function<void()>& f)
+{
+    struct Box { const std::function<void()>* f; } box{&f};
+    return run_guarded([](void* a) { (*((Box*)a)->f)(); }, &box);
+}
+
+template <typename T>
+static void to_device_as(const double* h, int64_t rows, int64_t cols, int64_t ldh, T* d,
+                         int64_t ldd, cudaStream_t st)
+{
+    std::vector<T> tmp((size_t)(ldd * cols), T(0));
+    for (int64_t j = 0; j < cols; ++j)
+        for (int64_t i = 0; i < rows; ++i) tmp[(size_t)(i + j * ldd)] = (T)h[i + j * ldh];
+    SKL_CUDA(cudaMemcpyAsync(d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
+template <typename T>
+static void from_device_as(const T* d, int64_t rows, int64_t cols, int64_t ldd, double* h,
+                           int64_t ldh, cudaStream_t st)
+{
+    std::vector<T> tmp((size_t)(ldd * cols));
+    SKL_CUDA(cudaMemcpyAsync(tmp.data(), d, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    for (int64_t j = 0; j < cols; ++j)
+        for (int64_t i = 0; i < rows; ++i) h[i + j * ldh] = (double)tmp[(size_t)(i + j * ldd)];
+}
+
+template <typename T>
+static void sketch_sparse_block(const skl_csc* A, const double* b, int64_t m, int64_t k,
+                                const int64_t* rows, const double* vals, int equilibrate,
+                                double* SA, double* Sb)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const int64_t n = A->m, d = A->n, nnz = A->p[d];
+    Sizer S;
+    S.add<int64_t>(d + 1); S.add<int64_t>(nnz); S.add<double>(nnz); S.add<double>(n);
+    S.add<int>(d + 1); S.add<int>(nnz); S.add<unsigned>(n * k); S.add<int>(m + 1);
+    S.add<unsigned>(n * k); S.add<T>(m * d); S.add<double>(d); S.add<double>(d); S.add<double>(m);
+    S.add<int>((int64_t)build_buckets_scratch_ints(m, n * k));
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    Arena& Ar = C.arena;
+    int64_t* Ap = Ar.alloc<int64_t>(d + 1);
+    int64_t* Ai = Ar.alloc<int64_t>(nnz);
+    double* Ax = Ar.alloc<double>(nnz);
+    double* bd = Ar.alloc<double>(n);
+    int* cp = Ar.alloc<int>(d + 1);
+    int* ri = Ar.alloc<int>(nnz);
+    unsigned* hidx = Ar.alloc<unsigned>(n * k);
+    int* bptr = Ar.alloc<int>(m + 1);
+    unsigned* bent = Ar.alloc<unsigned>(n * k);
+    T* SAd = Ar.alloc<T>(m * d);
+    double* cn = Ar.alloc<double>(d);
+    double* cs = Ar.alloc<double>(d);
+    double* Sbd = Ar.alloc<double>(m);
+    int* scr = Ar.alloc<int>((int64_t)build_buckets_scratch_ints(m, n * k));
+    std::vector<uint32_t> h((size_t)(n * k));
+    for (int64_t q = 0; q < n * k; ++q) {
+        if (rows[q] < 0 || rows[q] >= m) fail(SKL_ERR_INVALID, "hash row out of range");
+        h[(size_t)q] = (uint32_t)rows[q] | (vals[q] < 0 ? 0x80000000u : 0u);
+    }
+    SKL_CUDA(cudaMemcpyAsync(Ap, A->p, (d + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    if (nnz) {
+        SKL_CUDA(cudaMemcpyAsync(Ai, A->i, nnz * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        SKL_CUDA(cudaMemcpyAsync(Ax, A->x, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(hidx, h.data(), n * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+    csc_narrow(Ap, Ai, Ax, n, d, nnz, cp, ri, C.dev_status, st);
+    build_buckets(hidx, n, (int)k, m, bptr, bent, scr, st);
+    sketch_sparse<T>(cp, ri, Ax, n, d, hidx, (int)k, m, SAd, m, equilibrate, cn, cs, st);
+    sketch_rhs(bptr, bent, m, (int)k, bd, Sbd, st);
+    from_device_as<T>(SAd, m, d, m, SA, m, st);
+    SKL_CUDA(cudaMemcpyAsync(Sb, Sbd, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
+template <typename T>
+static void cpqr_block(double* A, int64_t m, int64_t d, int64_t* jpvt, double* tau)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const int64_t ld = (m + 31) / 32 * 32, mn = m < d ? m : d;
+    const size_t ws = cpqr_workspace_bytes<T>(m, d);
+    Sizer S;
+    S.add<T>(ld * d); S.add<int>(d); S.add<T>(mn); S.add<char>((int64_t)ws);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    T* Ad = C.arena.alloc<T>(ld * d);
+    int* jp = C.arena.alloc<int>(d);
+    T* td = C.arena.alloc<T>(mn);
+    void* work = C.arena.take(ws);
+    to_device_as<T>(A, m, d, m, Ad, ld, st);
+    cpqr<T>(Ad, m, d, ld, jp, td, work, C.dev_status, st, nullptr, 1);
+    from_device_as<T>(Ad, m, d, ld, A, m, st);
+    std::vector<int> hj((size_t)d);
+    std::vector<T> ht((size_t)mn);
+    SKL_CUDA(cudaMemcpyAsync(hj.data(), jp, d * sizeof(int), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaMemcpyAsync(ht.data(), td, mn * sizeof(T), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    for (int64_t j = 0; j < d; ++j) jpvt[j] = hj[(size_t)j];
+    for (int64_t j = 0; j < mn; ++j) tau[j] = (double)ht[(size_t)j];
+}
+
+template <typename T>
+static void trsv_block(const double* R, int64_t ld, int64_t r, char trans, double* x)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const size_t ws = trinv_workspace_bytes<T>(r);
+    Sizer S;
+    S.add<T>(r * r); S.add<T>(r * r); S.add<double>(4); S.add<double>(r); S.add<double>(r);
+    S.add<char>((int64_t)ws);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    T* Rd = C.arena.alloc<T>(r * r);
+    T* Md = C.arena.alloc<T>(r * r);
+    double* norms = C.arena.alloc<double>(4);
+    double* xd = C.arena.alloc<double>(r);
+    double* yd = C.arena.alloc<double>(r);
+    void* work = C.arena.take(ws);
+    to_device_as<T>(R, r, r, ld, Rd, r, st);
+    SKL_CUDA(cudaMemcpyAsync(xd, x, r * sizeof(double), cudaMemcpyHostToDevice, st));
+    trinv_upper<T>(Rd, r, r, 0.0, Md, r, norms, work, st);
+    trmv_upper<T>(Md, r, r, (trans == 't' || trans == 'T') ? 1 : 0, xd, yd, st);
+    SKL_CUDA(cudaMemcpyAsync(x, yd, r * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace skl
+
+using namespace skl;
+
+extern "C" {
+
+skl_status skl_sketch_sparse(const skl_csc* A, const double* b, int64_t m, int64_t k,
+                             const int64_t* rows, const double* vals, int precision,
+                             int equilibrate, double* SA, double* Sb)
+{
+    return guard([&] {
+        if (!A || !A->p || !b || !rows || !vals || !SA || !Sb || m <= 0 || k < 1)
+            fail(SKL_ERR_INVALID, "skl_sketch_sparse: bad argument");
+        if (precision == SKL_PREC_FP64)
+            sketch_sparse_block<double>(A, b, m, k, rows, vals, equilibrate, SA, Sb);
+        else
+            sketch_sparse_block<float>(A, b, m, k, rows, vals, equilibrate, SA, Sb);
+    });
+}
+
+skl_status skl_cpqr(double* A, int64_t m, int64_t d, int precision, int64_t* jpvt, double* tau)
+{
+    return guard([&] {
+        if (!A || !jpvt || !tau || m <= 0 || d <= 0) fail(SKL_ERR_INVALID, "skl_cpqr: bad argument");
+        if (precision == SKL_PREC_FP64) cpqr_block<double>(A, m, d, jpvt, tau);
+        else cpqr_block<float>(A, m, d, jpvt, tau);
+    });
+}
+
+skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, int precision,
+                          double* x)
+{
+    return guard([&] {
+        if (!R || !x || r <= 0 || ld < r) fail(SKL_ERR_INVALID, "skl_trsv_upper: bad argument");
+        if (precision == SKL_PREC_FP64) trsv_block<double>(R, ld, r, trans, x);
+        else trsv_block<float>(R, ld, r, trans, x);
+    });
+}
+
+}  // extern "C"

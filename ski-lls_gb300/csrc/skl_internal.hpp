@@ -1,0 +1,196 @@
+// skl_internal.hpp -- host-side internals shared by the solver's translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/skills_gb300.h"
+
+namespace skl {
+
+// Internal failures travel as exceptions and are turned into skl_status at
+// the C ABI (no exception crosses the boundary).
+struct Error : std::runtime_error {
+    skl_status status;
+    Error(skl_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+[[noreturn]] void fail(skl_status s, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what, const char* file, int line);
+#define SKL_CUDA(x) ::skl::check_cuda((x), #x, __FILE__, __LINE__)
+
+// Phase tracing (SKILLS_TRACE=1): synchronises the stream after each phase and
+// prints the phase name and the elapsed host time to stderr.
+void trace_phase(cudaStream_t st, const char* name);
+
+// Kernel launch accounting (counted per solve, reported in skl_info).
+void note_launch();
+int64_t launches_since_reset();
+void reset_launch_count();
+#define SKL_LAUNCHED() ::skl::note_launch()
+
+// Grow-only device arena; one per device context, bump-allocated per solve.
+class Arena {
+public:
+    void reserve(size_t bytes);
+    void reset() { used_ = 0; }
+    void* take(size_t bytes);
+    template <typename T>
+    T* alloc(int64_t count) { return static_cast<T*>(take((size_t)(count > 0 ? count : 1) * sizeof(T))); }
+    size_t capacity() const { return cap_; }
+    size_t used() const { return used_; }
+    void release();
+    ~Arena() { release(); }
+
+private:
+    char* base_ = nullptr;
+    size_t cap_ = 0, used_ = 0;
+};
+
+// Computes the arena size of a sequence of allocations before reserving it.
+class Sizer {
+public:
+    template <typename T>
+    void add(int64_t count) { bytes_ += ((size_t)(count > 0 ? count : 1) * sizeof(T) + 255) & ~(size_t)255; }
+    size_t bytes() const { return bytes_ + 4096; }
+
+private:
+    size_t bytes_ = 0;
+};
+
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[16] = {};
+    Arena arena;
+    Arena staging;           // device copies of host inputs
+    unsigned* dev_status = nullptr;  // device error word (kDevErr*)
+    double* dev_scalars = nullptr;   // small pinned-size scalar area (device)
+    void* host_pinned = nullptr;     // pinned host scratch for scalar readback
+    size_t host_pinned_bytes = 0;
+};
+
+Context& context(int device);
+// Runs fn and converts exceptions into an skl_status (C ABI guard).
+skl_status run_guarded(void (*fn)(void*), void* arg);
+void release_all_contexts();
+
+// ---------------------------------------------------------- k_format.cu --
+size_t scan_scratch_ints(int64_t n);
+void scan_exclusive(const int* in, int64_t n, int* out, int* scratch, cudaStream_t st);
+size_t radix_sort_scratch_ints(int64_t n);
+void radix_sort_pairs(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp,
+                      int64_t n, int bits, int* scratch, cudaStream_t st);
+int bits_for(int64_t maxval);
+void csc_narrow(const int64_t* Ap, const int64_t* Ai, const double* Ax, int64_t nrow, int64_t ncol,
+                int64_t nnz, int* cp, int* ri, unsigned* bad, cudaStream_t st);
+size_t build_csr_scratch_ints(int64_t nrow, int64_t nnz);
+void build_csr(const int* cp, const int* ri, const double* Ax, int64_t nrow, int64_t ncol,
+               int64_t nnz, int* rp, int* ci, double* cx, int* scratch, cudaStream_t st);
+size_t build_buckets_scratch_ints(int64_t m, int64_t nk);
+void build_buckets(const unsigned* hidx, int64_t n, int k, int64_t m, int* bptr, unsigned* bent,
+                   int* scratch, cudaStream_t st);
+
+// ---------------------------------------------------------- k_sketch.cu --
+// Sparse sketch: SA (m x d, ld) = S*A with column j scaled by colscale[j]
+// (written by the kernel: 1/||A(:,j)|| if equilibrate else 1); Sb = S*b.
+template <typename T>
+void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, int64_t d,
+                   const unsigned* hidx, int k, int64_t m, T* SA, int64_t ld, int equilibrate,
+                   double* colnorm, double* colscale, cudaStream_t st);
+void sketch_rhs(const int* bptr, const unsigned* bent, int64_t m, int k, const double* b,
+                double* Sb, cudaStream_t st);
+// Dense path: DHT of D*A (n x d, lda) padded to N, hashed into SA (m x d).
+template <typename T>
+void sketch_dense(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
+                  const int* bptr, const unsigned* bent, int k, int64_t m, T* SA, int64_t ld,
+                  double* Y_scratch, double* colnorm, cudaStream_t st);
+void dht_columns(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
+                 double* Y, int64_t ldy, cudaStream_t st);
+void sketch_dense_rhs(const double* b, int64_t n, const double* D, int64_t N, const int* bptr,
+                      const unsigned* bent, int k, int64_t m, double* Sb, double* y_scratch,
+                      cudaStream_t st);
+int64_t dht_length(int64_t n, int wisdom);
+
+// -------------------------------------------------------------- k_qr.cu --
+template <typename T>
+size_t cpqr_workspace_bytes(int64_t m, int64_t d);
+// Randomized CPQR in place on A (m x d, ld); jpvt (int, d) receives the
+// 0-based column permutation, tau (min(m,d)).  If c != nullptr, c (m
+// entries, FP64) is overwritten with Q^T c.  pivoting = 0 gives an unpivoted
+// blocked Householder QR (the _noCPQR path).
+template <typename T>
+void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
+          unsigned* status, cudaStream_t st, double* c, int pivoting);
+
+// ----------------------------------------------------------- k_trinv.cu --
+// M = inv(R11 + perturb*I) for the r x r upper triangle of R (ld); M is r x r
+// (ldm), upper triangular, zeros below.  Also ||R11||_inf and ||M||_inf.
+template <typename T>
+size_t trinv_workspace_bytes(int64_t r);
+template <typename T>
+void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_t ldm,
+                 double* norms /* [2] device */, void* work, cudaStream_t st);
+template <typename T>
+void trmv_upper(const T* M, int64_t ldm, int64_t r, int trans, const double* x, double* y,
+                cudaStream_t st);
+template <typename T>
+int64_t count_rank(const T* R, int64_t ld, int64_t dmin, double abs_thresh, double rel_thresh,
+                   int* dev_out, int* host_pinned, cudaStream_t st);
+
+// ------------------------------------------------------------ k_lsqr.cu --
+struct LsqrProblem {
+    int64_t n = 0, d = 0, nnz = 0;
+    // sparse A: CSR rows (A*z) and CSC columns (A^T*u), values in the LSQR
+    // storage type: (hi, lo) float pairs for the mixed path, double for FP64
+    const int* rp = nullptr; const int* ci = nullptr; const void* cx = nullptr;
+    const int* cp = nullptr; const int* ri = nullptr; const void* rx = nullptr;
+    const double* cx64 = nullptr; const double* rx64 = nullptr;   // FP64 values
+    // dense A: storage-type copy (n x d, lda) and the FP64 original (lda64)
+    const void* Ad = nullptr; int64_t lda = 0;
+    const double* Ad64 = nullptr; int64_t lda64 = 0;
+    // preconditioner: column i of the pivoted set is A(:, cols[i]) scaled by
+    // colscale[cols[i]], times M = R11^{-1} (r x r, column-major M and a
+    // row-major copy Mrow, both ldm)
+    const int* cols = nullptr;
+    const double* colscale = nullptr;
+    const void* M = nullptr; const void* Mrow = nullptr; int64_t ldm = 0; int64_t r = 0;
+    int precision = SKL_PREC_MIXED;
+};
+
+struct LsqrResult {
+    int flag = 1;
+    int64_t it = 0;
+};
+
+size_t lsqr_workspace_bytes(const LsqrProblem& P);
+// Solves min || A P1 D M y - b || from y = 0; y (r entries, device).
+LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t max_it, double* y,
+                    void* work, unsigned* status, void* host_pinned, cudaStream_t st);
+// xfull[cols[i]] = colscale[cols[i]] * (M yv)[i]; scratch holds r float2.
+void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
+                   cudaStream_t st);
+// out[0] = ||b - A x||, out[1] = ||A^T (b - A x)|| in FP64; r (n) and part
+// (512 doubles) are scratch.
+void residual_and_backward(const LsqrProblem& P, const double* x, const double* b, double* r,
+                           double* part, double* out, cudaStream_t st);
+void split_values(const double* x, int64_t n, float2* out, cudaStream_t st);
+void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out, cudaStream_t st);
+template <typename T>
+void transpose_upper(const T* Mc, int64_t ldm, int64_t r, T* Mr, cudaStream_t st);
+
+// ----------------------------------------------------------- hashing.cpp --
+// Host generator compatible with the C library's rand() (glibc TYPE_3).
+void rng_srand(uint32_t seed);
+// Draws the s-hashing matrix of sparse_helpers.cpp:90-116 from the library
+// stream: hidx[i*k+j] = row | (sign < 0 ? 0x80000000 : 0).
+void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx);
+// n random signs (+-1) as in gen_scaled_rand_signs (dense_helpers.cpp:7-16).
+void gen_signs(int64_t n, double* D);
+void rng_lock();
+void rng_unlock();
+
+}  // namespace skl

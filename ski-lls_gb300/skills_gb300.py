@@ -1,0 +1,315 @@
+"""Python host interface of the GB300 Ski-LLS solver (ctypes over the C ABI).
+
+Mirrors the reference's entry points (include/ski-lls.h:15-28):
+
+    ls_sparse_spqr(A, b, gamma, k, abs_tol, ordering, it_tol, max_it,
+                   rcond_threshold, perturb, debug)          -> Result
+    ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol, rcond, it_tol,
+                                max_it, debug, wisdom)       -> Result
+    ls_dense_hashing_blendenpik_noCPQR(A, b, gamma, k, it_tol, max_it,
+                                       debug, wisdom)        -> Result
+
+Result carries x and the reference's output arguments (rank, flag, it) plus
+the solver's diagnostics.  Errors raise RuntimeError with the reference's
+messages ("Matrix is not overdetermined.", "SPQR Factorization fails").
+There is no CPU fallback: if libskills_gb300.so is missing or no GB300 is
+visible, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libskills_gb300.so")
+
+SKL_OK = 0
+SKL_ERR_INVALID = 1
+SKL_ERR_NOT_OVERDETERMINED = 2
+SKL_ERR_RANK_ZERO = 3
+SKL_ERR_CUDA = 4
+SKL_ERR_NO_DEVICE = 5
+SKL_ERR_TIMEOUT = 6
+SKL_ERR_ALLOC = 7
+SKL_ERR_NONFINITE = 8
+
+PREC = {"mixed": 0, "fp64": 1}
+
+# include/bench_config.hpp:7-20
+IT_TOL = 1e-6
+MAX_IT = 10000
+OVER_SAMPLING_RATIO = 1.1
+NNZ_PER_COLUMN = 3
+PERTURB = 1e-10
+RCOND_THRESHOLD = 1e-10
+ABS_TOL = 1e-8
+SPQR_ORDERING = 2
+
+
+class SklCsc(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int64), ("n", ctypes.c_int64), ("nzmax", ctypes.c_int64),
+                ("p", ctypes.c_void_p), ("i", ctypes.c_void_p), ("x", ctypes.c_void_p)]
+
+
+class SklOpts(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("k", ctypes.c_int64), ("abs_tol", ctypes.c_double),
+                ("it_tol", ctypes.c_double), ("max_it", ctypes.c_int64),
+                ("rcond_threshold", ctypes.c_double), ("perturb", ctypes.c_double),
+                ("rcond", ctypes.c_double), ("rank_tol", ctypes.c_double),
+                ("precision", ctypes.c_int), ("use_cpqr", ctypes.c_int),
+                ("seed_mode", ctypes.c_int), ("seed", ctypes.c_uint32), ("wisdom", ctypes.c_int),
+                ("backward_tol", ctypes.c_double), ("max_refine", ctypes.c_int64),
+                ("device", ctypes.c_int)]
+
+
+class SklInfo(ctypes.Structure):
+    _fields_ = [("rank", ctypes.c_int64), ("flag", ctypes.c_int), ("it", ctypes.c_int64),
+                ("success", ctypes.c_int), ("sketch_rows", ctypes.c_int64),
+                ("rcond_r11", ctypes.c_double), ("explicit_residual", ctypes.c_double),
+                ("residual_norm", ctypes.c_double), ("backward_error", ctypes.c_double),
+                ("t_total_ms", ctypes.c_double), ("t_upload_ms", ctypes.c_double),
+                ("t_setup_ms", ctypes.c_double), ("t_sketch_ms", ctypes.c_double),
+                ("t_qr_ms", ctypes.c_double), ("t_precond_ms", ctypes.c_double),
+                ("t_lsqr_ms", ctypes.c_double), ("t_host_hash_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Load libskills_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i64, dbl = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double
+        L.skl_default_opts.argtypes = [ctypes.POINTER(SklOpts)]
+        L.skl_last_error.restype = ctypes.c_char_p
+        L.skl_version.restype = ctypes.c_char_p
+        L.skl_srand.argtypes = [ctypes.c_uint32]
+        for name in ("skl_sparse_solve", "skl_sparse_solve_device"):
+            f = getattr(L, name)
+            f.argtypes = [ctypes.POINTER(SklCsc), vp, vp, ctypes.POINTER(SklOpts),
+                          ctypes.POINTER(SklInfo)]
+            f.restype = ctypes.c_int
+        for name in ("skl_dense_solve", "skl_dense_solve_device"):
+            if not hasattr(L, name):
+                continue
+            f = getattr(L, name)
+            f.argtypes = [vp, i64, i64, i64, vp, vp, ctypes.POINTER(SklOpts),
+                          ctypes.POINTER(SklInfo)]
+            f.restype = ctypes.c_int
+        L.skl_hash_generate.argtypes = [i64, i64, i64, ctypes.c_int, ctypes.c_uint32, vp, vp]
+        L.skl_hash_generate.restype = ctypes.c_int
+        L.skl_sketch_sparse.argtypes = [ctypes.POINTER(SklCsc), vp, i64, i64, vp, vp, ctypes.c_int,
+                                        ctypes.c_int, vp, vp]
+        L.skl_sketch_sparse.restype = ctypes.c_int
+        if hasattr(L, "skl_dht"):
+            L.skl_dht.argtypes = [vp, i64, i64, i64, vp, i64, vp]
+        if hasattr(L, "skl_dht"):
+            L.skl_dht.restype = ctypes.c_int
+        if hasattr(L, "skl_sketch_dense"):
+            L.skl_sketch_dense.argtypes = [vp, i64, i64, i64, vp, vp, i64, i64, i64, vp, vp,
+                                       ctypes.c_int, vp, vp]
+        if hasattr(L, "skl_sketch_dense"):
+            L.skl_sketch_dense.restype = ctypes.c_int
+        L.skl_cpqr.argtypes = [vp, i64, i64, ctypes.c_int, vp, vp]
+        L.skl_cpqr.restype = ctypes.c_int
+        L.skl_trsv_upper.argtypes = [vp, i64, i64, ctypes.c_char, ctypes.c_int, vp]
+        L.skl_trsv_upper.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().skl_last_error().decode()
+
+
+class SklError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+def _check(rc):
+    if rc != SKL_OK:
+        raise SklError(rc, last_error())
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+def default_opts() -> SklOpts:
+    o = SklOpts()
+    lib().skl_default_opts(ctypes.byref(o))
+    return o
+
+
+@dataclass
+class Result:
+    x: np.ndarray
+    rank: int
+    flag: int
+    it: int
+    info: dict = field(default_factory=dict)
+
+
+def _as_csc(A):
+    """(indptr, indices, data, shape) with int64 indices, from a scipy matrix or a tuple."""
+    if hasattr(A, "tocsc"):
+        C = A.tocsc()
+        return (np.ascontiguousarray(C.indptr, dtype=np.int64),
+                np.ascontiguousarray(C.indices, dtype=np.int64),
+                np.ascontiguousarray(C.data, dtype=np.float64), C.shape)
+    indptr, indices, data, shape = A
+    return (np.ascontiguousarray(indptr, dtype=np.int64),
+            np.ascontiguousarray(indices, dtype=np.int64),
+            np.ascontiguousarray(data, dtype=np.float64), tuple(int(s) for s in shape))
+
+
+def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=ABS_TOL,
+                   ordering=SPQR_ORDERING, it_tol=IT_TOL, max_it=MAX_IT,
+                   rcond_threshold=RCOND_THRESHOLD, perturb=PERTURB, debug=0, *,
+                   precision="mixed", seed=None, backward_tol=0.0, max_refine=3,
+                   rank_tol=0.0, device=0) -> Result:
+    """GPU counterpart of ls_sparse_spqr (src/ls_sparse_spqr.cpp:79-214).
+
+    `ordering` and `debug` are accepted for signature parity (the GPU path
+    factorizes the sketch densely; SPQR's fill-reducing ordering has no role).
+    seed=None continues the library's glibc-compatible stream (a fresh process
+    is seed 1, like the reference); an integer reseeds first.
+    """
+    indptr, indices, data, (n, d) = _as_csc(A)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if b.shape != (n,):
+        raise ValueError("b must have A.m entries")
+    x = np.zeros(d, dtype=np.float64)
+    csc = SklCsc(n, d, int(indptr[-1]) if len(indptr) else 0, indptr.ctypes.data,
+                 indices.ctypes.data if indices.size else 0, data.ctypes.data if data.size else 0)
+    o = default_opts()
+    o.gamma, o.k, o.abs_tol, o.it_tol, o.max_it = gamma, k, abs_tol, it_tol, max_it
+    o.rcond_threshold, o.perturb, o.precision = rcond_threshold, perturb, PREC[precision]
+    o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    o.backward_tol, o.max_refine, o.rank_tol, o.device = backward_tol, max_refine, rank_tol, device
+    info = SklInfo()
+    _check(lib().skl_sparse_solve(ctypes.byref(csc), _ptr(b), _ptr(x), ctypes.byref(o),
+                                  ctypes.byref(info)))
+    return Result(x, info.rank, info.flag, info.it, info.as_dict())
+
+
+def ls_dense_hashing_blendenpik(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN,
+                                abs_tol=ABS_TOL, rcond=1e-10, it_tol=IT_TOL, max_it=MAX_IT,
+                                debug=0, wisdom=0, *, precision="mixed", seed=0,
+                                backward_tol=0.0, max_refine=3, use_cpqr=1,
+                                device=0) -> Result:
+    """GPU counterpart of ls_dense_hashing_blendenpik
+    (src/ls_dense_hashing_blendenpik.cpp:23-149).  seed=0 seeds from time(NULL)
+    like the reference (src/dense_helpers.cpp:92); pass a seed to reproduce."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, d = A.shape
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if b.shape != (n,):
+        raise ValueError("b must have A.m entries")
+    x = np.zeros(d, dtype=np.float64)
+    o = default_opts()
+    o.gamma, o.k, o.abs_tol, o.rcond, o.it_tol, o.max_it = gamma, k, abs_tol, rcond, it_tol, max_it
+    o.wisdom, o.precision, o.seed_mode, o.seed = wisdom, PREC[precision], 1, int(seed) & 0xFFFFFFFF
+    o.backward_tol, o.max_refine, o.use_cpqr, o.device = backward_tol, max_refine, use_cpqr, device
+    info = SklInfo()
+    _check(lib().skl_dense_solve(_ptr(A), max(n, 1), n, d, _ptr(b), _ptr(x), ctypes.byref(o),
+                                 ctypes.byref(info)))
+    return Result(x, info.rank, info.flag, info.it, info.as_dict())
+
+
+def ls_dense_hashing_blendenpik_noCPQR(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN,
+                                       it_tol=IT_TOL, max_it=MAX_IT, debug=0, wisdom=0,
+                                       **kw) -> Result:
+    """GPU counterpart of ls_dense_hashing_blendenpik_noCPQR
+    (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-60): unpivoted QR, LSQR from 0."""
+    return ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=0.0, rcond=0.0, it_tol=it_tol,
+                                       max_it=max_it, debug=debug, wisdom=wisdom, use_cpqr=0, **kw)
+
+
+def hash_generate(m, n, k, seed=None):
+    """Rows (int64, n*k) and values (+-1/sqrt(k)) of the s-hashing matrix."""
+    rows = np.empty(n * k, dtype=np.int64)
+    vals = np.empty(n * k, dtype=np.float64)
+    mode, sd = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    _check(lib().skl_hash_generate(m, n, k, mode, sd, _ptr(rows), _ptr(vals)))
+    return rows, vals
+
+
+def srand(seed):
+    lib().skl_srand(int(seed) & 0xFFFFFFFF)
+
+
+def sketch_sparse(A, b, m, k, rows, vals, precision="mixed", equilibrate=False):
+    indptr, indices, data, (n, d) = _as_csc(A)
+    csc = SklCsc(n, d, int(indptr[-1]), indptr.ctypes.data,
+                 indices.ctypes.data if indices.size else 0, data.ctypes.data if data.size else 0)
+    SA = np.zeros((m, d), dtype=np.float64, order="F")
+    Sb = np.zeros(m, dtype=np.float64)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    _check(lib().skl_sketch_sparse(ctypes.byref(csc), _ptr(bb), m, k, _ptr(rows), _ptr(vals),
+                                   PREC[precision], int(equilibrate), _ptr(SA), _ptr(Sb)))
+    return SA, Sb
+
+
+def cpqr(A, precision="mixed"):
+    """Randomized CPQR on the GPU: returns (QR, jpvt 0-based, tau)."""
+    QR = np.array(A, dtype=np.float64, order="F", copy=True)
+    m, d = QR.shape
+    jpvt = np.zeros(d, dtype=np.int64)
+    tau = np.zeros(min(m, d), dtype=np.float64)
+    _check(lib().skl_cpqr(_ptr(QR), m, d, PREC[precision], _ptr(jpvt), _ptr(tau)))
+    return QR, jpvt, tau
+
+
+def trsv_upper(R, x, trans="n", precision="mixed"):
+    R = np.asfortranarray(R, dtype=np.float64)
+    xx = np.array(x, dtype=np.float64, copy=True)
+    r = R.shape[1]
+    _check(lib().skl_trsv_upper(_ptr(R), max(R.shape[0], 1), r, trans.encode(), PREC[precision],
+                                _ptr(xx)))
+    return xx
+
+
+def dht(A, D, N=None):
+    A = np.asfortranarray(A, dtype=np.float64)
+    if A.ndim == 1:
+        A = A[:, None]
+    n, d = A.shape
+    N = n if N is None else N
+    Y = np.zeros((N, d), dtype=np.float64, order="F")
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    _check(lib().skl_dht(_ptr(A), max(n, 1), n, d, _ptr(D), N, _ptr(Y)))
+    return Y
+
+
+def sketch_dense(A, b, D, N, m, k, rows, vals, precision="mixed"):
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, d = A.shape
+    SA = np.zeros((m, d), dtype=np.float64, order="F")
+    Sb = np.zeros(m, dtype=np.float64)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    _check(lib().skl_sketch_dense(_ptr(A), max(n, 1), n, d, _ptr(np.ascontiguousarray(b, dtype=np.float64)),
+                                  _ptr(np.ascontiguousarray(D, dtype=np.float64)), N, m, k,
+                                  _ptr(rows), _ptr(vals), PREC[precision], _ptr(SA), _ptr(Sb)))
+    return SA, Sb
+
+
+def finalize():
+    lib().skl_finalize()

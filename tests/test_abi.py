@@ -1,0 +1,84 @@
+"""C-ABI library: builds, loads, exports every declared symbol; host-side pieces (no GPU)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import skills_gb300 as skl
+import ski_lls_oracle as orc
+from conftest import ROOT, GOLDEN
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", f)).read()
+            names |= set(re.findall(r"\b(skl_[a-z_0-9]+)\s*\(", txt))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def L():
+    if not os.path.exists(skl.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return skl.lib()
+
+
+def test_library_exports_declared_symbols(L):
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, f"declared in include/ but not exported: {missing}"
+
+
+def test_version(L):
+    assert b"sm_103a" in L.skl_version()
+
+
+def test_default_opts_match_reference_macros():
+    o = skl.default_opts()
+    # include/bench_config.hpp:7-20
+    assert (o.it_tol, o.max_it, o.gamma, o.k) == (1e-6, 10000, 1.1, 3)
+    assert (o.perturb, o.rcond_threshold, o.abs_tol) == (1e-10, 1e-10, 1e-8)
+
+
+def test_hash_stream_bit_exact_vs_oracle_and_golden():
+    z = np.load(os.path.join(GOLDEN, "hashing.npz"))
+    from make_golden import CASES
+    for (m, n, k) in CASES:
+        rows, vals = skl.hash_generate(m, n, k, seed=1)
+        np.testing.assert_array_equal(rows, z[f"{m}_{n}_{k}/rows"])
+        np.testing.assert_array_equal((vals > 0).astype(np.uint8), z[f"{m}_{n}_{k}/signs"])
+        r2, v2 = orc.gen_hashing(orc.Rng(1), m, n, k)
+        np.testing.assert_array_equal(rows, r2)
+        np.testing.assert_array_equal(vals, v2)
+
+
+def test_hash_stream_continues_like_global_rand():
+    # two draws without reseeding continue one stream, as the reference's
+    # global rand() does across calls (src/sparse_helpers.cpp:90-116)
+    skl.srand(99)
+    a_rows, _ = skl.hash_generate(50, 30, 2)
+    b_rows, _ = skl.hash_generate(50, 30, 2)
+    g = orc.Rng(99)
+    r1, _ = orc.gen_hashing(g, 50, 30, 2)
+    r2, _ = orc.gen_hashing(g, 50, 30, 2)
+    np.testing.assert_array_equal(a_rows, r1)
+    np.testing.assert_array_equal(b_rows, r2)
+
+
+def test_hash_rejects_bad_sizes():
+    with pytest.raises(skl.SklError):
+        skl.hash_generate(3, 10, 5, seed=1)
+
+
+def test_solve_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    import scipy.sparse as sp
+    A = sp.random(40, 5, density=0.5, random_state=1, format="csc")
+    with pytest.raises(skl.SklError) as e:
+        skl.ls_sparse_spqr(A, np.ones(40), seed=1)
+    assert e.value.status in (skl.SKL_ERR_NO_DEVICE, skl.SKL_ERR_CUDA)
