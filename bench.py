@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Time-to-solve benchmark of the GB300 Ski-LLS solve path.
+
+One step = one full solve (sketch -> randomized CPQR -> preconditioned LSQR)
+of the named workload.  Default workload: the 120,000 x 5,000, 1 %-dense,
+column-scaled (kappa ~ 1e8), rank-deficient sparse problem, s = 2, m = 1.7 d,
+LSQR tolerance 1e-10, mixed precision (FP32 sketch/QR, FP64 LSQR).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--no-cpu-baseline] [--no-fp64]
+
+Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): every rank solves its
+own replica (the single-problem path does not shard); the reported time is
+the max over ranks.  The reference arm (--impl reference) times the CPU
+oracle, a restatement of the reference algorithm, on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for sub in ("ski-lls_gb300", "oracle"):
+    p = os.path.join(ROOT, sub)
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-to-solve @ backward err <=1e-10: mixed vs FP64 path on 1 GB300 (s, %HBM)"
+DEFAULT_WORKLOAD = "sparse_illcond_120000x5000"
+IT_TOL = 1e-10
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), float(pk["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload --
+def make_workload(name):
+    import synthetic
+    w = synthetic.WORKLOADS[name]
+    t0 = time.perf_counter()
+    A, b = w["gen"]()
+    return w, A, b, time.perf_counter() - t0
+
+
+def oracle_solve(kind, A, b, gamma, k):
+    import ski_lls_oracle as orc
+    if kind == "sparse":
+        A = A.tocsc()
+        return orc.ls_sparse_spqr(A.shape[0], A.shape[1], A.indptr, A.indices, A.data, b, gamma,
+                                  k, it_tol=IT_TOL, rng=orc.Rng(1))
+    return orc.ls_dense_hashing_blendenpik(A, b, gamma, k, it_tol=IT_TOL, seed=1)
+
+
+def backward_error(A, x, b):
+    import scipy.sparse as sp
+    r = b - A @ x
+    fro = sp.linalg.norm(A, "fro") if sp.issparse(A) else np.linalg.norm(A)
+    nr = np.linalg.norm(r)
+    return float(np.linalg.norm(A.T @ r) / (fro * nr)) if nr > 0 else 0.0
+
+
+# ---------------------------------------------------------- reference arm --
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    w, A, b, _ = make_workload(args.workload)
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 3))
+    for _ in range(warm):
+        oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
+    times = []
+    out = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
+        times.append(time.perf_counter() - t0)
+    v = statistics.mean(times)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "requested_steps": args.steps,
+        "requested_warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "shape": list(A.shape),
+                   "nnz": int(getattr(A, "nnz", A.size)), "gamma": w["gamma"], "k": w["k"],
+                   "it_tol": IT_TOL},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": "full solve of the workload per step; CPU oracle "
+                                   "(restatement of the reference algorithm: C loops single "
+                                   "thread as the reference's MAX_NUM_THREADS=1, LAPACK dgeqp3/"
+                                   "dormqr/dtrcon via numpy's OpenBLAS on all cores; SPQR "
+                                   "replaced by dense CPQR of the sketch)"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "solve": {"rank": int(out["rank"]), "it": int(out["it"]), "flag": int(out["flag"]),
+                  "backward_error": backward_error(A, out["x"], b)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm --
+def run_ours(args, rank, world):
+    import torch
+    import skills_gb300 as skl
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    w, A, b, gen_s = make_workload(args.workload)
+    if w["kind"] != "sparse":
+        raise SystemExit("dense workloads: use the dense bench mode")
+    A = A.tocsc()
+    n, d = A.shape
+    nnz = int(A.nnz)
+    gamma, k = w["gamma"], w["k"]
+    hbm_peak, _, peak_kind = load_peaks()
+
+    Ap = torch.from_numpy(A.indptr.astype(np.int64)).to(dev)
+    Ai = torch.from_numpy(A.indices.astype(np.int64)).to(dev)
+    Ax = torch.from_numpy(A.data.astype(np.float64)).to(dev)
+    bd = torch.from_numpy(b.astype(np.float64)).to(dev)
+    xd = torch.zeros(d, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    stream = torch.cuda.Stream(device=dev)
+
+    def solve(precision, profile):
+        return skl.sparse_solve_device(n, d, Ap.data_ptr(), Ai.data_ptr(), Ax.data_ptr(),
+                                       bd.data_ptr(), xd.data_ptr(), nnz, gamma, k,
+                                       precision=precision, seed=1, it_tol=IT_TOL,
+                                       stream=stream.cuda_stream, profile=profile, device=local)
+
+    def timed(precision, steps, warmup, profile):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                solve(precision, profile)
+            torch.cuda.synchronize()
+            barrier()
+            torch.cuda.synchronize()
+            evs = []
+            infos = []
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                infos.append(solve(precision, profile))
+                e1.record(stream)
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+            barrier()
+            wall = time.perf_counter() - t0
+        ms = [a.elapsed_time(b_) for a, b_ in evs]
+        return ms, infos, wall
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, infos, wall = timed("mixed", args.steps, max(3, args.warmup), 1)
+    clk = clocks.stop()
+    x_mixed = xd.cpu().numpy()
+    step_s = statistics.mean(ms) / 1e3
+    if dist is not None:
+        t = torch.tensor([step_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s = float(t.item())
+    last = infos[-1]
+
+    fp64 = None
+    if not args.no_fp64:
+        ms64, inf64, _ = timed("fp64", max(1, min(args.steps, 3)), 1, 0)
+        x64 = xd.cpu().numpy()
+        fp64 = {"value": statistics.mean(ms64) / 1e3, "unit": "s",
+                "mixed_speedup": statistics.mean(ms64) / statistics.mean(ms),
+                "backward_error": backward_error(A, x64, b), "it": int(inf64[-1].it),
+                "rank": int(inf64[-1].rank),
+                "phases_ms": {"setup": inf64[-1].t_setup_ms, "sketch": inf64[-1].t_sketch_ms,
+                              "qr": inf64[-1].t_qr_ms, "precond": inf64[-1].t_precond_ms,
+                              "lsqr": inf64[-1].t_lsqr_ms}}
+
+    # ---- roofline of the LSQR products from the live events of the timed steps
+    r = int(last.rank)
+    prof_ms = np.sum([np.array(list(i.prof_ms)) for i in infos], axis=0)
+    prof_n = np.sum([np.array(list(i.prof_launches)) for i in infos], axis=0)
+    nnz_sel = nnz   # all columns are read by A*z (dropped columns carry z = 0)
+    alg_bytes = {
+        # CSR: col idx 4 B + (hi,lo) value 8 B per nnz, row ptr, z gather (d pairs),
+        # u read + u write + split write
+        "lsqr_spmv_csr_Az": 12 * nnz + 4 * (n + 1) + 8 * d + 24 * n,
+        # CSC over the r kept columns: row idx + value, u split reads counted once
+        "lsqr_spmv_csc_ATu": 12 * nnz_sel + 4 * (d + 1) + 8 * n + 8 * r,
+        "lsqr_trmv_Mv": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+        "lsqr_trmv_MTt": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+    }
+    kernels = {}
+    for q, name in enumerate(alg_bytes):
+        if prof_n[q] > 0:
+            per = prof_ms[q] / prof_n[q]
+            ach = alg_bytes[name] / (per * 1e-3) / 1e9
+            kernels[name] = {"launches": int(prof_n[q]), "ms_per_launch": per,
+                             "total_ms": float(prof_ms[q]), "alg_bytes": int(alg_bytes[name]),
+                             "achieved_gbs": ach, "frac": ach / hbm_peak}
+    dom = max(kernels, key=lambda kk: kernels[kk]["total_ms"]) if kernels else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath) and dom:
+        with open(tpath) as f:
+            traffic = json.load(f).get(args.workload, {}).get(dom)
+    roofline = None
+    if dom:
+        kk = kernels[dom]
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": kk["achieved_gbs"],
+                    "peak": hbm_peak, "unit": "GB/s", "frac": kk["frac"], "traffic": traffic,
+                    "peak_kind": peak_kind, "alg_bytes_per_launch": kk["alg_bytes"]}
+
+    # ---- e2e through the host-pointer C ABI (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.from_numpy(A.indptr.astype(np.int64)).pin_memory()
+        hi = torch.from_numpy(A.indices.astype(np.int64)).pin_memory()
+        hx = torch.from_numpy(A.data.astype(np.float64)).pin_memory()
+        hb = torch.from_numpy(b.astype(np.float64)).pin_memory()
+        hxo = torch.zeros(d, dtype=torch.float64).pin_memory()
+        import ctypes
+        csc = skl.SklCsc(n, d, nnz, hp.data_ptr(), hi.data_ptr(), hx.data_ptr())
+        o = skl.default_opts()
+        o.gamma, o.k, o.it_tol, o.seed_mode, o.seed, o.device = gamma, k, IT_TOL, 1, 1, local
+        o.stream = stream.cuda_stream
+        times = []
+        for q in range(max(3, args.warmup) + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            info = skl.SklInfo()
+            rc = skl.lib().skl_sparse_solve(ctypes.byref(csc), ctypes.c_void_p(hb.data_ptr()),
+                                            ctypes.c_void_p(hxo.data_ptr()), ctypes.byref(o),
+                                            ctypes.byref(info))
+            if rc != 0:
+                raise RuntimeError(skl.last_error())
+            t = time.perf_counter() - t0
+            if q >= max(3, args.warmup):
+                times.append(t)
+        e2e = {"value": statistics.mean(times), "unit": "s",
+               "h2d_bytes_per_step": int(8 * (d + 1) + 16 * nnz + 8 * n),
+               "d2h_bytes_per_step": int(8 * d),
+               "x_matches_device_path": bool(np.array_equal(hxo.numpy(), x_mixed))}
+
+    cpu = None
+    be_oracle = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        out = oracle_solve("sparse", A, b, gamma, k)
+        tcpu = time.perf_counter() - t0
+        be_oracle = backward_error(A, out["x"], b)
+        cpu = {"value": tcpu, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full solve of the workload by the CPU oracle (C loops single "
+                         "thread, LAPACK via numpy OpenBLAS on all cores)",
+               "backward_error": be_oracle, "it": int(out["it"]), "rank": int(out["rank"]),
+               "x_rel_diff_gpu_vs_oracle": float(np.linalg.norm(x_mixed - out["x"]) /
+                                                 np.linalg.norm(out["x"]))}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": step_s * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": args.workload, "n": n, "d": d, "nnz": nnz, "gamma": gamma, "k": k,
+                   "sketch_rows": int(last.sketch_rows), "it_tol": IT_TOL,
+                   "precision": "mixed (FP32 sketch/QR/R^-1, float-float LSQR products, FP64 "
+                                "recurrences)",
+                   "l2": "inputs larger than L2 (CSC+CSR 145 MB, sketch 170 MB) and a 256 MB "
+                         "buffer written between steps", "parallelism": "replicas"},
+        "e2e": e2e,
+        "gpu_launches": int(sum(i.kernel_launches for i in infos)),
+        "roofline": roofline,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "fp64_path": fp64,
+        "solve": {"rank": int(last.rank), "it": int(last.it), "flag": int(last.flag),
+                  "success": int(last.success), "rcond_r11": last.rcond_r11,
+                  "backward_error": backward_error(A, x_mixed, b),
+                  "backward_error_oracle": be_oracle,
+                  "explicit_residual": last.explicit_residual,
+                  "phases_ms": {"setup": last.t_setup_ms, "sketch": last.t_sketch_ms,
+                                "qr": last.t_qr_ms, "precond": last.t_precond_ms,
+                                "lsqr": last.t_lsqr_ms, "host_hash": last.t_host_hash_ms},
+                  "step_ms": ms, "wall_s": wall, "workload_gen_s": gen_s},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,6 +81,8 @@ typedef struct {
                                 <= backward_tol (checked in FP64)                 */
     int64_t max_refine;      /* restarts allowed to meet backward_tol            */
     int device;              /* CUDA device ordinal                               */
+    void* stream;            /* cudaStream_t to run on; NULL = the library's own  */
+    int profile;             /* 1: time the LSQR products with CUDA events        */
 } skl_opts;
 
 typedef struct {
@@ -102,6 +104,10 @@ typedef struct {
     double t_lsqr_ms;        /* LSQR iterations                                   */
     double t_host_hash_ms;   /* host wall time generating the hash stream         */
     int64_t kernel_launches; /* kernels launched by this solve                    */
+    /* opts.profile = 1: summed CUDA-event time and launch count of the LSQR
+       products (0: A*z CSR/dense, 1: A^T*u CSC/dense, 2: M*v, 3: M^T*t) */
+    double prof_ms[4];
+    int64_t prof_launches[4];
 } skl_info;
 
 /* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,

@@ -589,20 +589,33 @@ static unsigned tri_blocks(int64_t r)
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * 8));
 }
 
+// ev (optional): 8 events, begin/end around M*v, A*z, A^T*u, M^T*t
 template <bool MIXED>
-static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
+static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
+                             cudaEvent_t* ev = nullptr)
 {
     using V = ValT<MIXED>;
     using MT = MatT<MIXED>;
+    auto mark = [&](int q) {
+        if (ev) SKL_CUDA(cudaEventRecordWithFlags(ev[q], st, cudaEventRecordExternal));
+    };
     const unsigned gt = tri_blocks(P.r);
+    mark(4);
     k_tri_n<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
                                               P.cols, P.colscale, (V*)B.z, B.S, 0, nullptr);
     SKL_LAUNCHED();
+    mark(5);
+    mark(0);
     launch_spmv_n<MIXED>(P, B, st);
+    mark(1);
+    mark(2);
     launch_spmv_t<MIXED>(P, B, st);
+    mark(3);
+    mark(6);
     k_tri_t<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
                                               B.S, 0, B.partials);
     SKL_LAUNCHED();
+    mark(7);
     unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
     k_lsqr_update<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
     SKL_LAUNCHED();
@@ -610,7 +623,8 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
 
 template <bool MIXED>
 static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, int64_t max_it,
-                           double* y_out, void* work, void* host_pinned, cudaStream_t st)
+                           double* y_out, void* work, void* host_pinned, cudaStream_t st,
+                           int profile, cudaStream_t capture_stream)
 {
     using V = ValT<MIXED>;
     using MT = MatT<MIXED>;
@@ -637,9 +651,17 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     const int kIterPerGraph = 4;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaStream_t cap = st;
+    // capture on a non-default stream (capture is not allowed on the legacy
+    // default stream); the graph is then launched on the caller's stream
+    cudaStream_t cap = capture_stream ? capture_stream : st;
+    std::vector<cudaEvent_t> pev;
+    if (profile) {
+        pev.resize(8 * kIterPerGraph);
+        for (auto& e : pev) SKL_CUDA(cudaEventCreate(&e));
+    }
     SKL_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int q = 0; q < kIterPerGraph; ++q) launch_iteration<MIXED>(P, B, cap);
+    for (int q = 0; q < kIterPerGraph; ++q)
+        launch_iteration<MIXED>(P, B, cap, profile ? &pev[8 * q] : nullptr);
     SKL_CUDA(cudaStreamEndCapture(cap, &graph));
     SKL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
     struct Flags { int done; int flag; long long it; };
@@ -648,6 +670,8 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     cudaEvent_t ev;
     SKL_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     bool done = false;
+    LsqrResult res;
+    long long it_prev = 0;
     trace_phase(st, "lsqr: init");
     const auto t_start = std::chrono::steady_clock::now();
     while (!done) {
@@ -664,10 +688,22 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
         SKL_CUDA(cudaMemcpyAsync((void*)hs, B.S, sizeof(LsqrState), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaEventRecord(ev, st));
         SKL_CUDA(cudaEventSynchronize(ev));
+        if (profile) {
+            // iterations that ran in this replay (later ones returned at entry)
+            long long ran = hs->it - it_prev;
+            for (long long q = 0; q < ran && q < kIterPerGraph; ++q)
+                for (int kk = 0; kk < 4; ++kk) {
+                    float ms = 0.f;
+                    SKL_CUDA(cudaEventElapsedTime(&ms, pev[8 * q + 2 * kk], pev[8 * q + 2 * kk + 1]));
+                    res.prof_ms[kk] += ms;
+                    res.prof_launches[kk] += 1;
+                }
+        }
+        it_prev = hs->it;
         done = hs->done != 0 || launched >= max_it + kIterPerGraph;
     }
+    for (auto& e : pev) cudaEventDestroy(e);
     trace_phase(st, "lsqr: done");
-    LsqrResult res;
     res.flag = hs->flag;
     res.it = hs->it;
     SKL_CUDA(cudaEventDestroy(ev));
@@ -678,11 +714,13 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
 }
 
 LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t max_it, double* y,
-                    void* work, unsigned* status, void* host_pinned, cudaStream_t st)
+                    void* work, unsigned* status, void* host_pinned, cudaStream_t st, int profile,
+                    cudaStream_t capture_stream)
 {
     (void)status;
-    if (P.precision == SKL_PREC_MIXED) return run_impl<true>(P, b, tol, max_it, y, work, host_pinned, st);
-    return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st);
+    if (P.precision == SKL_PREC_MIXED)
+        return run_impl<true>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
+    return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
 }
 
 // x_full[cols[i]] = colscale[cols[i]] * (M yv)[i] (FP64 output), other entries untouched.

@@ -194,12 +194,12 @@ static void check_opts(const skl_opts& o)
         fail(SKL_ERR_INVALID, "unknown precision");
 }
 
-static unsigned read_status(Context& C)
+static unsigned read_status(Context& C, cudaStream_t st)
 {
     unsigned v = 0;
     SKL_CUDA(cudaMemcpyAsync(C.host_pinned, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                             C.stream));
-    SKL_CUDA(cudaStreamSynchronize(C.stream));
+                             st));
+    SKL_CUDA(cudaStreamSynchronize(st));
     v = *(unsigned*)C.host_pinned;
     return v;
 }
@@ -212,11 +212,10 @@ struct SparseDev {
 
 // ------------------------------------------------------- sparse solve ---
 template <typename T>
-static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, const skl_opts& o,
-                            skl_info& info, const int64_t* host_p, bool timing_upload,
+static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, double* x_dev,
+                            const skl_opts& o, skl_info& info, bool timing_upload,
                             std::thread* hash_thread, std::vector<uint32_t>* host_hidx)
 {
-    cudaStream_t st = C.stream;
     const int64_t n = in.n, d = in.d, nnz = in.nnz;
     const int64_t k = o.k;
     const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
@@ -277,7 +276,6 @@ static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, cons
     double* scal = Ar.alloc<double>(8);
     void* work = Ar.take(std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
     float2* ysplit = Ar.alloc<float2>(d);
-    (void)host_p;
 
     cudaEvent_t* ev = C.ev;
     SKL_CUDA(cudaEventRecord(ev[1], st));
@@ -295,7 +293,7 @@ static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, cons
         SKL_CUDA(cudaMemcpyAsync(hidx, host_hidx->data(), n * k * sizeof(unsigned),
                                  cudaMemcpyHostToDevice, st));
     }
-    unsigned bad = read_status(C);
+    unsigned bad = read_status(C, st);
     if (bad & 1u) fail(SKL_ERR_INVALID, "CSC column pointers are not a valid structure");
     if (bad & 2u) fail(SKL_ERR_INVALID, "CSC row index out of range");
     if (bad & 4u) fail(SKL_ERR_NONFINITE, "A contains NaN or Inf");
@@ -366,7 +364,15 @@ static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, cons
         int64_t restarts = 0;
         const double btol = o.backward_tol;
         // first solve
-        LsqrResult R = lsqr_run(P, rs, o.it_tol, o.max_it, yv, work, C.dev_status, C.host_pinned, st);
+        auto add_prof = [&](const LsqrResult& Rr) {
+            for (int q = 0; q < 4; ++q) {
+                info.prof_ms[q] += Rr.prof_ms[q];
+                info.prof_launches[q] += Rr.prof_launches[q];
+            }
+        };
+        LsqrResult R = lsqr_run(P, rs, o.it_tol, o.max_it, yv, work, C.dev_status, C.host_pinned,
+                                st, o.profile, C.stream);
+        add_prof(R);
         total_it += R.it;
         flag = R.flag;
         // y <- y + c (first r entries), x = D P1 M y
@@ -392,7 +398,9 @@ static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, cons
         // restarts from the FP64 residual while the backward error target is missed
         while (btol > 0.0 && be > btol && restarts < o.max_refine && total_it < o.max_it) {
             ++restarts;
-            R = lsqr_run(P, rs, o.it_tol, o.max_it - total_it, yv, work, C.dev_status, C.host_pinned, st);
+            R = lsqr_run(P, rs, o.it_tol, o.max_it - total_it, yv, work, C.dev_status, C.host_pinned,
+                         st, o.profile, C.stream);
+            add_prof(R);
             total_it += R.it;
             flag = R.flag;
             SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
@@ -424,7 +432,7 @@ static void sparse_pipeline(Context& C, const SparseDev& in, double* x_dev, cons
     info.t_lsqr_ms = elapsed(ev[5], ev[6]);
     info.t_total_ms = elapsed(timing_upload ? ev[0] : ev[1], ev[6]);
     if (timing_upload) info.t_upload_ms = elapsed(ev[0], ev[1]);
-    unsigned stt = read_status(C);
+    unsigned stt = read_status(C, st);
     if (stt & 1u) fail(SKL_ERR_TIMEOUT, "a bounded device wait gave up");
 }
 
@@ -476,7 +484,7 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
     }
     Context& C = context(o.device);
     reset_launch_count();
-    cudaStream_t st = C.stream;
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : C.stream;
     const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
     if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
     // host hash stream in a worker thread (serial Fisher-Yates)
@@ -522,9 +530,9 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
         SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
         in.Ap = Ap; in.Ai = Ai; in.Ax = Ax; in.b = bd; in.nnz = nnz;
         if (o.precision == SKL_PREC_MIXED)
-            sparse_pipeline<float>(C, in, xd, o, inf, A->p, true, &th, &hh);
+            sparse_pipeline<float>(C, st, in, xd, o, inf, true, &th, &hh);
         else
-            sparse_pipeline<double>(C, in, xd, o, inf, A->p, true, &th, &hh);
+            sparse_pipeline<double>(C, st, in, xd, o, inf, true, &th, &hh);
         SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
     } else {
@@ -533,9 +541,9 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
         nnz = *(int64_t*)C.host_pinned;
         in.Ap = A->p; in.Ai = A->i; in.Ax = A->x; in.b = b; in.nnz = nnz;
         if (o.precision == SKL_PREC_MIXED)
-            sparse_pipeline<float>(C, in, x, o, inf, nullptr, false, &th, &hh);
+            sparse_pipeline<float>(C, st, in, x, o, inf, false, &th, &hh);
         else
-            sparse_pipeline<double>(C, in, x, o, inf, nullptr, false, &th, &hh);
+            sparse_pipeline<double>(C, st, in, x, o, inf, false, &th, &hh);
     }
     inf.t_host_hash_ms = hash_ms;
     inf.kernel_launches = launches_since_reset();

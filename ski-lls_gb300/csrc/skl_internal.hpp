@@ -164,12 +164,15 @@ struct LsqrProblem {
 struct LsqrResult {
     int flag = 1;
     int64_t it = 0;
+    double prof_ms[4] = {0, 0, 0, 0};      // A*z, A^T*u, M*v, M^T*t (profile = 1)
+    int64_t prof_launches[4] = {0, 0, 0, 0};
 };
 
 size_t lsqr_workspace_bytes(const LsqrProblem& P);
 // Solves min || A P1 D M y - b || from y = 0; y (r entries, device).
 LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t max_it, double* y,
-                    void* work, unsigned* status, void* host_pinned, cudaStream_t st);
+                    void* work, unsigned* status, void* host_pinned, cudaStream_t st,
+                    int profile = 0, cudaStream_t capture_stream = nullptr);
 // xfull[cols[i]] = colscale[cols[i]] * (M yv)[i]; scratch holds r float2.
 void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
                    cudaStream_t st);

@@ -63,7 +63,7 @@ class SklOpts(ctypes.Structure):
                 ("precision", ctypes.c_int), ("use_cpqr", ctypes.c_int),
                 ("seed_mode", ctypes.c_int), ("seed", ctypes.c_uint32), ("wisdom", ctypes.c_int),
                 ("backward_tol", ctypes.c_double), ("max_refine", ctypes.c_int64),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("stream", ctypes.c_void_p), ("profile", ctypes.c_int)]
 
 
 class SklInfo(ctypes.Structure):
@@ -75,10 +75,15 @@ class SklInfo(ctypes.Structure):
                 ("t_setup_ms", ctypes.c_double), ("t_sketch_ms", ctypes.c_double),
                 ("t_qr_ms", ctypes.c_double), ("t_precond_ms", ctypes.c_double),
                 ("t_lsqr_ms", ctypes.c_double), ("t_host_hash_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("prof_ms", ctypes.c_double * 4),
+                ("prof_launches", ctypes.c_int64 * 4)]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if name.startswith("prof_") else v
+        return out
 
 
 _lib = None
@@ -181,7 +186,7 @@ def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=AB
                    ordering=SPQR_ORDERING, it_tol=IT_TOL, max_it=MAX_IT,
                    rcond_threshold=RCOND_THRESHOLD, perturb=PERTURB, debug=0, *,
                    precision="mixed", seed=None, backward_tol=0.0, max_refine=3,
-                   rank_tol=0.0, device=0) -> Result:
+                   rank_tol=0.0, device=0, stream=None, profile=0) -> Result:
     """GPU counterpart of ls_sparse_spqr (src/ls_sparse_spqr.cpp:79-214).
 
     `ordering` and `debug` are accepted for signature parity (the GPU path
@@ -201,17 +206,36 @@ def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=AB
     o.rcond_threshold, o.perturb, o.precision = rcond_threshold, perturb, PREC[precision]
     o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
     o.backward_tol, o.max_refine, o.rank_tol, o.device = backward_tol, max_refine, rank_tol, device
+    o.stream, o.profile = stream, profile
     info = SklInfo()
     _check(lib().skl_sparse_solve(ctypes.byref(csc), _ptr(b), _ptr(x), ctypes.byref(o),
                                   ctypes.byref(info)))
     return Result(x, info.rank, info.flag, info.it, info.as_dict())
 
 
+def sparse_solve_device(n, d, p_ptr, i_ptr, x_ptr, b_ptr, xout_ptr, nnz, gamma, k, *,
+                        precision="mixed", seed=None, it_tol=IT_TOL, max_it=MAX_IT,
+                        abs_tol=ABS_TOL, backward_tol=0.0, stream=None, profile=0,
+                        device=0) -> SklInfo:
+    """skl_sparse_solve_device on device pointers (CSC with int64 indices)."""
+    csc = SklCsc(n, d, nnz, p_ptr, i_ptr, x_ptr)
+    o = default_opts()
+    o.gamma, o.k, o.abs_tol, o.it_tol, o.max_it = gamma, k, abs_tol, it_tol, max_it
+    o.precision = PREC[precision]
+    o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    o.backward_tol, o.device, o.stream, o.profile = backward_tol, device, stream, profile
+    info = SklInfo()
+    _check(lib().skl_sparse_solve_device(ctypes.byref(csc), ctypes.c_void_p(b_ptr),
+                                         ctypes.c_void_p(xout_ptr), ctypes.byref(o),
+                                         ctypes.byref(info)))
+    return info
+
+
 def ls_dense_hashing_blendenpik(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN,
                                 abs_tol=ABS_TOL, rcond=1e-10, it_tol=IT_TOL, max_it=MAX_IT,
                                 debug=0, wisdom=0, *, precision="mixed", seed=0,
                                 backward_tol=0.0, max_refine=3, use_cpqr=1,
-                                device=0) -> Result:
+                                device=0, stream=None, profile=0) -> Result:
     """GPU counterpart of ls_dense_hashing_blendenpik
     (src/ls_dense_hashing_blendenpik.cpp:23-149).  seed=0 seeds from time(NULL)
     like the reference (src/dense_helpers.cpp:92); pass a seed to reproduce."""
@@ -225,6 +249,7 @@ def ls_dense_hashing_blendenpik(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUM
     o.gamma, o.k, o.abs_tol, o.rcond, o.it_tol, o.max_it = gamma, k, abs_tol, rcond, it_tol, max_it
     o.wisdom, o.precision, o.seed_mode, o.seed = wisdom, PREC[precision], 1, int(seed) & 0xFFFFFFFF
     o.backward_tol, o.max_refine, o.use_cpqr, o.device = backward_tol, max_refine, use_cpqr, device
+    o.stream, o.profile = stream, profile
     info = SklInfo()
     _check(lib().skl_dense_solve(_ptr(A), max(n, 1), n, d, _ptr(b), _ptr(x), ctypes.byref(o),
                                  ctypes.byref(info)))
