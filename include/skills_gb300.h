@@ -108,6 +108,10 @@ typedef struct {
        products (0: A*z CSR/dense, 1: A^T*u CSC/dense, 2: M*v, 3: M^T*t) */
     double prof_ms[4];
     int64_t prof_launches[4];
+    /* opts.profile = 1: CUDA-event ms of the QR sub-steps: 0 sample QRP,
+       1 column moves, 2 panel, 3 Q^T c, 4 W = V^T A, 5 Z = T^T W,
+       6 A -= V Z, 7 sample downdate, 8 initial sample Y = G A */
+    double qr_prof_ms[9];
 } skl_info;
 
 /* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,
@@ -161,9 +165,13 @@ skl_status skl_sketch_sparse(const skl_csc* A, const double* b, int64_t m, int64
                              int equilibrate, double* SA, double* Sb);
 
 /* Orthonormal DHT of the columns of D*A (n x d host, column-major), padded
- * to N rows (N >= n; zeros below n): Y = H_N [D A; 0] / sqrt(N). */
+ * to N rows (N >= n, N even, N/2 a product of 2, 3, 5, 7; zeros below n):
+ * Y = H_N [D A; 0] / sqrt(N), computed in FP32 or FP64 per `precision`. */
 skl_status skl_dht(const double* A, int64_t lda, int64_t n, int64_t d, const double* D,
-                   int64_t N, double* Y);
+                   int64_t N, int precision, double* Y);
+
+/* Transform length the dense solver uses for n rows (wisdom as in skl_opts). */
+int64_t skl_dht_length(int64_t n, int wisdom);
 
 /* alpha*S*(H D A) for the dense path (alpha = 1/sqrt(k), as sketch() applies
  * on top of S's +-1/sqrt(k) values): SA is m x d, Sb is m. */

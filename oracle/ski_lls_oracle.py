@@ -157,13 +157,17 @@ def dense_sketch(Y, m, k, rows, vals):
     return SA
 
 
-def unitary_dht(A, D):
-    """y = DHT_N( D * A / sqrt(N) ) column-wise, N = rows(A) (wisdom = 0)."""
+def unitary_dht(A, D, N=None):
+    """y = DHT_N( [D * A; 0] / sqrt(N) ) column-wise; N = rows(A) unless a
+    padded length is given (the reference pads in its wisdom mode,
+    src/fast_unitary_transform.cpp:63-64, :98-99)."""
     A = np.asarray(A, dtype=np.float64)
     if A.ndim == 1:
         A = A[:, None]
-    N = A.shape[0]
-    y = (1.0 / math.sqrt(N)) * D[:, None] * A
+    n = A.shape[0]
+    N = n if N is None else N
+    y = np.zeros((N, A.shape[1]))
+    y[:n] = (1.0 / math.sqrt(N)) * D[:, None] * A
     F = np.fft.fft(y, axis=0)
     return np.asfortranarray(F.real - F.imag)
 
@@ -290,7 +294,7 @@ def ls_sparse_spqr(n, d, indptr, indices, data, b, gamma, k, abs_tol=1e-8, it_to
 
 
 def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_tol=1e-6,
-                                max_it=10000, seed=1):
+                                max_it=10000, seed=1, N=None):
     """Restates ls_dense_hashing_blendenpik (src/ls_dense_hashing_blendenpik.cpp:23-149).
 
     The reference seeds with srand(time(NULL)) (src/dense_helpers.cpp:92, :12);
@@ -301,11 +305,12 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     if n < d:
         raise RuntimeError("Matrix is not overdetermined.")
     m = int(math.ceil(d * gamma))
+    N = n if N is None else N
     rng = Rng(seed)
     D = rand_signs(rng, n)
-    Y = unitary_dht(A, D)
-    yb = unitary_dht(np.asarray(b, dtype=np.float64), D)[:, 0]
-    rows, vals = gen_hashing(rng, m, n, k)
+    Y = unitary_dht(A, D, N)
+    yb = unitary_dht(np.asarray(b, dtype=np.float64), D, N)[:, 0]
+    rows, vals = gen_hashing(rng, m, N, k)
     SA = dense_sketch(Y, m, k, rows, vals)
     Sb = dense_sketch(yb[:, None], m, k, rows, vals)[:, 0]
     qr, E, tau = _cpqr(SA.copy(order="F"))
@@ -332,6 +337,29 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     x = xs + x
     out.update(x=x, flag=flag, it=it)
     return out
+
+
+def ls_dense_hashing_blendenpik_noCPQR(A, b, gamma, k, it_tol=1e-6, max_it=10000, seed=1,
+                                       N=None):
+    """Restates ls_dense_hashing_blendenpik_noCPQR
+    (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-59): sketch A only, unpivoted
+    QR (dense_qr, src/dense_qr.cpp:8-32), LSQR on (A, b) from zero, x = R^{-1} y."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, d = A.shape
+    if n < d:
+        raise RuntimeError("Matrix is not overdetermined.")
+    m = int(math.ceil(d * gamma))
+    N = n if N is None else N
+    rng = Rng(seed)
+    D = rand_signs(rng, n)
+    Y = unitary_dht(A, D, N)
+    rows, vals = gen_hashing(rng, m, N, k)
+    SA = dense_sketch(Y, m, k, rows, vals)
+    R = np.asfortranarray(np.linalg.qr(SA, mode="r")[:d, :d])
+    y, flag, it = lsqr(n, d, np.asarray(b, dtype=np.float64), np.arange(d), R, it_tol, max_it,
+                       dense=A)
+    x = usolve(R, y, 1, 0.0)
+    return dict(m=m, rank=d, x=x, flag=flag, it=it, SA=SA)
 
 
 def backward_error(A_mv, A_rmv, fro, x, b):

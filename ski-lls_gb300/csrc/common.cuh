@@ -196,28 +196,32 @@ SKL_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_sh
 SKL_DEV uint32_t dsmem_addr(const void* local, unsigned rank)
 {
     uint32_t a = smem_u32(local), r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
     return r;
 }
 
+// The loads are volatile (never merged, hoisted or dropped, and kept in order
+// relative to the cluster barriers, which carry the memory clobber) but carry
+// no clobber themselves, so independent loads issue back to back and their
+// latencies overlap.
 SKL_DEV float dsmem_ld_f32(const float* local, unsigned rank)
 {
     float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(dsmem_addr(local, rank)) : "memory");
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(dsmem_addr(local, rank)));
     return v;
 }
 
 SKL_DEV double dsmem_ld_f64(const double* local, unsigned rank)
 {
     double v;
-    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(dsmem_addr(local, rank)) : "memory");
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(dsmem_addr(local, rank)));
     return v;
 }
 
 SKL_DEV int dsmem_ld_s32(const int* local, unsigned rank)
 {
     int v;
-    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(dsmem_addr(local, rank)) : "memory");
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(dsmem_addr(local, rank)));
     return v;
 }
 

@@ -124,6 +124,29 @@ void gen_signs(int64_t n, double* D)
     for (int64_t i = 0; i < n; ++i) D[i] = (g_rng.next() & 1u) ? 1.0 : -1.0;
 }
 
+// NoFLA_Normal_random_matrix / NoFLA_Normal_random_number
+// (hqrrp/lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4_skint.c:584-624):
+// pairs (c1, c2) uniform in (-1,1)^2 are drawn until 0 < c1^2+c2^2 < 1; each
+// accepted pair yields two normals.  Only the number of rand() calls matters.
+void rng_hqrrp_advance(int64_t rows, int64_t cols)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_rng.seed(12);
+    g_seeded = true;
+    const int64_t count = rows * cols;
+    const double rmax = 2147483647.0;
+    for (int64_t q = 0; q < count; q += 2) {
+        double a;
+        do {
+            const double c1 = -1.0 + 2.0 * ((double)g_rng.next() / rmax);
+            const double c2 = -1.0 + 2.0 * ((double)g_rng.next() / rmax);
+            const double p1 = c1 * c1;
+            const double p2 = c2 * c2;
+            a = p1 + p2;
+        } while (a == 0 || a >= 1);
+    }
+}
+
 }  // namespace skl
 
 extern "C" void skl_srand(uint32_t seed) { skl::rng_srand(seed); }

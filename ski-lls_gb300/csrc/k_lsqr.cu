@@ -23,6 +23,7 @@
 // The all-FP64 path uses plain double values and DFMA.
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -39,6 +40,7 @@ struct LsqrState {
 };
 
 constexpr int kLThreads = 256;
+constexpr int kTriThreads = 128;   // threads per row pair of the triangular products
 
 // Fixed-order reduction of partials[0..np) by one block; result to *out.
 SKL_DEV double block_reduce_partials(const double* partials, int np)
@@ -107,80 +109,142 @@ using MatT = typename std::conditional<MIXED, float, double>::type;
 template <bool MIXED>
 using ValT = typename VecT<MIXED>::type;   // stored A values: float2 (hi,lo) or double
 
+// ------------------------------------------------------- triangular dots --
+// Partial dot of M[j0:j1] (contiguous) with v[j0:j1] for one thread of a block
+// that strides 4-element chunks by `nthr`: 16-byte loads, two independent
+// accumulators.  Head/tail elements (before the first 4-element boundary and
+// after the last whole chunk) are taken by the first threads.  The row start
+// must be 4-element aligned in memory (ldm is a multiple of 4).
+template <bool MIXED>
+SKL_DEV Acc<MIXED> thread_dot_seg(const MatT<MIXED>* __restrict__ M, const ValT<MIXED>* __restrict__ v,
+                                  int j0, int j1, int t, int nthr)
+{
+    Acc<MIXED> a0, a1;
+    const int jb = min(j1, (j0 + 3) & ~3);
+    if (t < jb - j0) a0.fma_f(M[j0 + t], v[j0 + t]);
+    const int nch = (j1 - jb) >> 2;
+    const int je = jb + (nch << 2);
+    if constexpr (MIXED) {
+        const float4* M4 = reinterpret_cast<const float4*>(M + jb);
+        const float4* v4 = reinterpret_cast<const float4*>(v + jb);   // 2 elements per float4
+        for (int c = t; c < nch; c += nthr) {
+            const float4 m0 = M4[c];
+            const float4 x0 = v4[2 * c], x1 = v4[2 * c + 1];
+            a0.fma_f(m0.x, make_float2(x0.x, x0.y));
+            a1.fma_f(m0.y, make_float2(x0.z, x0.w));
+            a0.fma_f(m0.z, make_float2(x1.x, x1.y));
+            a1.fma_f(m0.w, make_float2(x1.z, x1.w));
+        }
+    } else {
+        const double2* M2 = reinterpret_cast<const double2*>(M + jb);
+        const double2* v2 = reinterpret_cast<const double2*>(v + jb);
+        for (int c = t; c < nch; c += nthr) {
+            const double2 m0 = M2[2 * c], m1 = M2[2 * c + 1];
+            const double2 x0 = v2[2 * c], x1 = v2[2 * c + 1];
+            a0.fma_f(m0.x, x0.x);
+            a1.fma_f(m0.y, x0.y);
+            a0.fma_f(m1.x, x1.x);
+            a1.fma_f(m1.y, x1.y);
+        }
+    }
+    if (t < j1 - je) a1.fma_f(M[je + t], v[je + t]);
+    a0.add(a1);
+    return a0;
+}
+
+// Fixed-order block reduction of two accumulators (all threads call it).
+template <bool MIXED>
+SKL_DEV void block_reduce2(Acc<MIXED>& a, Acc<MIXED>& b, Acc<MIXED>* sm)
+{
+    constexpr int NW = kTriThreads / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a.add(a.shfl_xor(o));
+        b.add(b.shfl_xor(o));
+    }
+    if (lane == 0) {
+        sm[wid] = a;
+        sm[NW + wid] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < NW; ++q) {
+            sm[0].add(sm[q]);
+            sm[NW].add(sm[NW + q]);
+        }
+    }
+    __syncthreads();
+    a = sm[0];
+    b = sm[NW];
+}
+
 // ------------------------------------------------------------- tri_n -----
 // z[cols[i]] = colscale[cols[i]] * sum_{j>=i} M[i][j] v[j]   (Mr row-major)
-// Warp w handles rows w and r-1-w so every warp sees ~r+1 entries.
+// One block per row pair (i, r-1-i): every block reads ~r+1 entries.
 template <bool MIXED>
-__global__ void __launch_bounds__(kLThreads)
+__global__ void __launch_bounds__(kTriThreads)
 k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED>* __restrict__ v,
         const int* __restrict__ cols, const double* __restrict__ colscale,
         ValT<MIXED>* __restrict__ z, const LsqrState* __restrict__ S, int plain_out,
         double* __restrict__ zplain)
 {
     if (S && S->done) return;
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ Acc<MIXED> sm[2 * kTriThreads / 32];
     const int npairs = (r + 1) / 2;
-    for (int pidx = gw; pidx < npairs; pidx += nw) {
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            int i = h == 0 ? pidx : r - 1 - pidx;
-            if (h == 1 && i == pidx) break;
-            const MatT<MIXED>* row = Mr + (int64_t)i * ldm;
-            Acc<MIXED> acc;
-            for (int j = i + lane; j < r; j += 32) acc.fma_f(row[j], v[j]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
-            if (lane == 0) {
-                int c = cols[i];
-                double val = colscale[c] * acc.value();
+    for (int pidx = blockIdx.x; pidx < npairs; pidx += gridDim.x) {
+        const int i1 = pidx, i2 = r - 1 - pidx;
+        Acc<MIXED> a = thread_dot_seg<MIXED>(Mr + (int64_t)i1 * ldm, v, i1, r, threadIdx.x, kTriThreads);
+        Acc<MIXED> b;
+        if (i2 != i1) b = thread_dot_seg<MIXED>(Mr + (int64_t)i2 * ldm, v, i2, r, threadIdx.x, kTriThreads);
+        block_reduce2<MIXED>(a, b, sm);
+        if (threadIdx.x == 0) {
+            int c = cols[i1];
+            double val = colscale[c] * a.value();
+            if (plain_out) zplain[c] = val;
+            else z[c] = store_val<MIXED>(val);
+            if (i2 != i1) {
+                c = cols[i2];
+                val = colscale[c] * b.value();
                 if (plain_out) zplain[c] = val;
                 else z[c] = store_val<MIXED>(val);
             }
         }
+        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------- tri_t -----
 // vh[j] = sum_{i<=j} M[i][j] t[i] - coef * vh[j], coef = beta'/alpha (0 at init)
 template <bool MIXED>
-__global__ void __launch_bounds__(kLThreads)
+__global__ void __launch_bounds__(kTriThreads)
 k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED>* __restrict__ t,
         double* __restrict__ vh, LsqrState* __restrict__ S, int init, double* __restrict__ partials)
 {
     if (S->done) return;
-    __shared__ double wsum[kLThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ Acc<MIXED> sm[2 * kTriThreads / 32];
     const double coef = init ? 0.0 : (S->alpha > 0.0 ? S->beta / S->alpha : 0.0);
     const int npairs = (r + 1) / 2;
     double ss = 0.0;
-    for (int pidx = gw; pidx < npairs; pidx += nw) {
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            int j = h == 0 ? pidx : r - 1 - pidx;
-            if (h == 1 && j == pidx) break;
-            const MatT<MIXED>* col = Mc + (int64_t)j * ldm;
-            Acc<MIXED> acc;
-            for (int i = lane; i <= j; i += 32) acc.fma_f(col[i], t[i]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
-            if (lane == 0) {
-                double nv = acc.value() - coef * vh[j];
-                vh[j] = nv;
+    for (int pidx = blockIdx.x; pidx < npairs; pidx += gridDim.x) {
+        const int j1 = pidx, j2 = r - 1 - pidx;
+        Acc<MIXED> a = thread_dot_seg<MIXED>(Mc + (int64_t)j1 * ldm, t, 0, j1 + 1, threadIdx.x, kTriThreads);
+        Acc<MIXED> b;
+        if (j2 != j1) b = thread_dot_seg<MIXED>(Mc + (int64_t)j2 * ldm, t, 0, j2 + 1, threadIdx.x, kTriThreads);
+        block_reduce2<MIXED>(a, b, sm);
+        if (threadIdx.x == 0) {
+            double nv = a.value() - coef * vh[j1];
+            vh[j1] = nv;
+            ss += nv * nv;
+            if (j2 != j1) {
+                nv = b.value() - coef * vh[j2];
+                vh[j2] = nv;
                 ss += nv * nv;
             }
         }
+        __syncthreads();
     }
-    if (lane == 0) wsum[wid] = ss;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += wsum[q];
-        partials[blockIdx.x] = s;
-    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = ss;
     if (arrive_last(&S->cnt[1])) {
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
@@ -196,11 +260,21 @@ k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED
 template <bool MIXED, int L>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<MIXED>* __restrict__ cv,
-             int n, int rows_per_block, const ValT<MIXED>* __restrict__ z, double* __restrict__ uh,
-             ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S, double* __restrict__ partials)
+             int n, int rows_per_block, const ValT<MIXED>* __restrict__ zg, int d_stage,
+             double* __restrict__ uh, ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S,
+             double* __restrict__ partials)
 {
     if (S->done) return;
     __shared__ double wsum[kLThreads / 32];
+    // z is gathered at random columns: stage it in shared memory when it fits
+    extern __shared__ __align__(16) unsigned char zsm_raw[];
+    const ValT<MIXED>* z = zg;
+    if (d_stage > 0) {
+        ValT<MIXED>* zs = reinterpret_cast<ValT<MIXED>*>(zsm_raw);
+        for (int j = threadIdx.x; j < d_stage; j += blockDim.x) zs[j] = zg[j];
+        __syncthreads();
+        z = zs;
+    }
     // Each warp owns 32/L consecutive row slots per pass; the pass count is
     // uniform across the warp so the full-mask shuffles below always see all
     // 32 lanes (groups past the last row contribute zero).
@@ -215,11 +289,31 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
     for (int base = r0 + warp_grp0; base < r1; base += ngrp) {
         const int i = base + (grp - warp_grp0);
         const bool active = i < r1;
-        Acc<MIXED> acc;
+        Acc<MIXED> acc, acc2;
         if (active) {
             const int p1 = rp[i + 1];
-            for (int p = rp[i] + lane; p < p1; p += L) acc.fma_mv(cv[p], z[ci[p]]);
+            // predicated groups of four: every lane issues its (index, value)
+            // loads and gathers before any arithmetic, also on short rows
+            for (int pb = rp[i] + lane; pb < p1; pb += 4 * L) {
+                int cc[4];
+                ValT<MIXED> aa[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int p = pb + k * L;
+                    const bool ok = p < p1;
+                    cc[k] = ok ? ci[p] : 0;
+                    aa[k] = ok ? cv[p] : ValT<MIXED>{};
+                }
+                ValT<MIXED> zz[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) zz[k] = z[cc[k]];
+                acc.fma_mv(aa[0], zz[0]);
+                acc2.fma_mv(aa[1], zz[1]);
+                acc.fma_mv(aa[2], zz[2]);
+                acc2.fma_mv(aa[3], zz[3]);
+            }
         }
+        acc.add(acc2);
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
         if (active && lane == 0) {
@@ -265,13 +359,31 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
     for (int base = gw0; base < r; base += ng) {
         const int i = base + (g - gw0);
         const bool active = i < r;
-        Acc<MIXED> acc;
+        Acc<MIXED> acc, acc2;
         int c = 0;
         if (active) {
             c = cols[i];
             const int p1 = cp[c + 1];
-            for (int p = cp[c] + lane; p < p1; p += L) acc.fma_mv(cv[p], us[ri[p]]);
+            for (int pb = cp[c] + lane; pb < p1; pb += 4 * L) {
+                int rr[4];
+                ValT<MIXED> aa[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int p = pb + k * L;
+                    const bool ok = p < p1;
+                    rr[k] = ok ? ri[p] : 0;
+                    aa[k] = ok ? cv[p] : ValT<MIXED>{};
+                }
+                ValT<MIXED> uu[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) uu[k] = us[rr[k]];
+                acc.fma_mv(aa[0], uu[0]);
+                acc2.fma_mv(aa[1], uu[1]);
+                acc.fma_mv(aa[2], uu[2]);
+                acc2.fma_mv(aa[3], uu[3]);
+            }
         }
+        acc.add(acc2);
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
         if (active && lane == 0) t[i] = store_val<MIXED>(colscale[c] * acc.value() * ib);
@@ -468,21 +580,22 @@ struct LsqrBufs {
     int nparts;
 };
 
+// lanes per row/column so that each lane handles about four nonzeros
 static int lanes_for(double avg)
 {
-    if (avg >= 24) return 32;
-    if (avg >= 10) return 16;
-    if (avg >= 5) return 8;
+    if (avg >= 96) return 32;
+    if (avg >= 40) return 16;
+    if (avg >= 16) return 8;
     return 4;
 }
 
-static const int kRowsPerBlock = 256;
+static const int kRowsPerBlock = 64;
 static const int kDenseChunk = 128;
 
 static int64_t spmv_n_blocks(const LsqrProblem& P)
 {
     if (P.Ad) return (P.n + kLThreads - 1) / kLThreads;
-    return (P.n + kRowsPerBlock - 1) / kRowsPerBlock;
+    return (P.n + kRowsPerBlock - 1) / kRowsPerBlock;   // upper bound on the grid
 }
 
 size_t lsqr_workspace_bytes(const LsqrProblem& P)
@@ -545,10 +658,19 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
         SKL_LAUNCHED();
         return;
     }
-    const unsigned g = (unsigned)spmv_n_blocks(P);
     const double avg = P.n ? (double)P.nnz / P.n : 0.0;
     const int L = lanes_for(avg);
-#define SPMV_N(LL) k_spmv_n_csr<MIXED, LL><<<g, kLThreads, 0, st>>>(P.rp, P.ci, (const V*)P.cx, (int)P.n, kRowsPerBlock, (const V*)B.z, B.uh, (V*)B.us, B.S, B.partials)
+    // z staged in shared memory (<= 96 KB); blocks sized to ~4 per SM
+    const size_t zbytes = (size_t)P.d * sizeof(V);
+    const int stage = zbytes <= 96 * 1024 ? (int)P.d : 0;
+    const size_t smem = stage ? zbytes : 0;
+    int rpb = kRowsPerBlock;
+    if (stage) rpb = (int)std::max<int64_t>(kRowsPerBlock, (P.n + 152 * 4 - 1) / (152 * 4));
+    const unsigned g = (unsigned)((P.n + rpb - 1) / rpb);
+#define SPMV_N(LL) do { \
+        if (smem > 48 * 1024) SKL_CUDA(cudaFuncSetAttribute(k_spmv_n_csr<MIXED, LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        k_spmv_n_csr<MIXED, LL><<<g, kLThreads, smem, st>>>(P.rp, P.ci, (const V*)P.cx, (int)P.n, rpb, (const V*)B.z, stage, B.uh, (V*)B.us, B.S, B.partials); \
+    } while (0)
     if (L == 32) SPMV_N(32);
     else if (L == 16) SPMV_N(16);
     else if (L == 8) SPMV_N(8);
@@ -584,9 +706,8 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
 
 static unsigned tri_blocks(int64_t r)
 {
-    int64_t warps = (r + 1) / 2;
-    int64_t blocks = (warps + (kLThreads / 32) - 1) / (kLThreads / 32);
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * 8));
+    int64_t pairs = (r + 1) / 2;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(pairs, 152 * 32));
 }
 
 // ev (optional): 8 events, begin/end around M*v, A*z, A^T*u, M^T*t
@@ -601,7 +722,7 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     };
     const unsigned gt = tri_blocks(P.r);
     mark(4);
-    k_tri_n<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
+    k_tri_n<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
                                               P.cols, P.colscale, (V*)B.z, B.S, 0, nullptr);
     SKL_LAUNCHED();
     mark(5);
@@ -612,7 +733,7 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     launch_spmv_t<MIXED>(P, B, st);
     mark(3);
     mark(6);
-    k_tri_t<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+    k_tri_t<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
                                               B.S, 0, B.partials);
     SKL_LAUNCHED();
     mark(7);
@@ -640,7 +761,7 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     SKL_LAUNCHED();
     launch_spmv_t<MIXED>(P, B, st);
     const unsigned gt = tri_blocks(P.r);
-    k_tri_t<MIXED><<<gt, kLThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+    k_tri_t<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
                                               B.S, 1, B.partials);
     SKL_LAUNCHED();
     unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
@@ -674,13 +795,17 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     long long it_prev = 0;
     trace_phase(st, "lsqr: init");
     const auto t_start = std::chrono::steady_clock::now();
+    static const double limit_s = [] {
+        const char* e = getenv("SKILLS_LSQR_TIMEOUT_S");
+        return e ? atof(e) : 60.0;
+    }();
     while (!done) {
-        // host-side bound: a replay loop that runs past a minute reports a timeout
-        if (std::chrono::steady_clock::now() - t_start > std::chrono::seconds(60)) {
+        // host-side bound: a replay loop that runs past the limit reports a timeout
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() > limit_s) {
             cudaEventDestroy(ev);
             cudaGraphExecDestroy(exec);
             cudaGraphDestroy(graph);
-            fail(SKL_ERR_TIMEOUT, "LSQR replay loop exceeded 60 s");
+            fail(SKL_ERR_TIMEOUT, "LSQR replay loop exceeded its time limit (SKILLS_LSQR_TIMEOUT_S)");
         }
         SKL_CUDA(cudaGraphLaunch(exec, st));
         launched += kIterPerGraph;
@@ -740,11 +865,11 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
     if (P.precision == SKL_PREC_MIXED) {
         float2* ys = (float2*)scratch;
         k_split_vec<<<(unsigned)((P.r + 255) / 256), 256, 0, st>>>(yv, (int)P.r, ys);
-        k_tri_n<true><<<gt, kLThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, ys, P.cols,
+        k_tri_n<true><<<gt, kTriThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, ys, P.cols,
                                                  P.colscale, nullptr, nullptr, 1, xfull);
         SKL_LAUNCHED();
     } else {
-        k_tri_n<false><<<gt, kLThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv, P.cols,
+        k_tri_n<false><<<gt, kTriThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv, P.cols,
                                                   P.colscale, nullptr, nullptr, 1, xfull);
     }
     SKL_LAUNCHED();

@@ -29,6 +29,8 @@
 // src/ls_dense_hashing_blendenpik.cpp:70-76).
 #include <cmath>
 #include <cstdio>
+#include <utility>
+#include <vector>
 
 #include "skl_internal.hpp"
 #include "common.cuh"
@@ -86,18 +88,24 @@ SKL_DEV void householder(T alpha, T sigma2, T& beta, T& tau, T& scale)
 // ------------------------------------------------------------ Y-QRP -----
 // QR with column pivoting of Y(:, j0:j0+N) (nbp x N) for b steps; writes the
 // selected columns (relative indices) in selection order to sel[0..b).
+// CTA c of the cluster holds columns [c*cn, c*cn+cn) in shared memory with an
+// odd column stride (conflict-free thread-per-column access).  One step:
+//   local argmax -> publish candidate (norm, index, column) -> cluster barrier
+//   -> every CTA reads all 16 candidates in one batched DSMEM round trip ->
+//   same winner and Householder vector everywhere -> thread-per-column update.
 template <typename T>
 struct YqrpSmem {
-    // layout offsets in the dynamic shared buffer
+    __host__ __device__ static int ldp(int nbp) { return nbp | 1; }
     static size_t bytes(int nbp, int cn)
     {
-        size_t s = (size_t)nbp * cn * sizeof(T);          // Ys
-        s += (size_t)cn * sizeof(T);                       // nrm
-        s += (size_t)cn;                                   // taken
+        size_t s = (size_t)ldp(nbp) * cn * sizeof(T);      // Ys
+        s += (size_t)cn * sizeof(T);                        // nrm
+        s += (size_t)cn + 16;                               // taken
         s = (s + 15) & ~(size_t)15;
-        s += 2 * (size_t)nbp * sizeof(T);                  // cand_col[2]
-        s += (size_t)nbp * sizeof(T);                      // v
-        s += 2 * sizeof(T) + 2 * sizeof(int) + 64;         // cand val/idx
+        s += 2 * (size_t)nbp * sizeof(T);                   // cand_col[2][nbp]
+        s += (size_t)kCluster * nbp * sizeof(T);            // all candidates' columns
+        s += (size_t)nbp * sizeof(T);                       // v
+        s += 2 * sizeof(T) + 2 * sizeof(int) + 64;          // cand val/idx
         return s + 256;
     }
 };
@@ -111,30 +119,35 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     const int cn = (N + kCluster - 1) / kCluster;
     const int c0 = (int)crank * cn;
     const int ncols = max(0, min(cn, N - c0));
+    const int ldp = YqrpSmem<T>::ldp(nbp);
     T* Ys = (T*)smem_raw;
-    T* nrm = Ys + (size_t)nbp * cn;
+    T* nrm = Ys + (size_t)ldp * cn;
     unsigned char* taken = (unsigned char*)(nrm + cn);
-    size_t off = ((size_t)nbp * cn * sizeof(T) + cn * sizeof(T) + cn + 15) & ~(size_t)15;
+    size_t off = ((size_t)ldp * cn * sizeof(T) + cn * sizeof(T) + cn + 16 + 15) & ~(size_t)15;
     T* cand_col = (T*)(smem_raw + off);          // [2][nbp]
-    T* v = cand_col + 2 * nbp;                    // [nbp]
+    T* allc = cand_col + 2 * nbp;                 // [16][nbp]
+    T* v = allc + kCluster * nbp;                 // [nbp]
     T* cand_val = v + nbp;                        // [2]
     int* cand_idx = (int*)(cand_val + 2);         // [2]
     __shared__ T s_red_v[kQrWarps];
     __shared__ int s_red_i[kQrWarps];
+    __shared__ T s_cv[kCluster];
+    __shared__ int s_ci[kCluster];
     __shared__ T s_tau;
+    __shared__ int s_win_idx, s_local;
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int e = tid; e < nbp * ncols; e += kQrThreads) {
         int r = e % nbp, c = e / nbp;
-        Ys[r + (size_t)c * nbp] = Y[r + (int64_t)(j0 + c0 + c) * ldy];
+        Ys[r + (size_t)c * ldp] = Y[r + (int64_t)(j0 + c0 + c) * ldy];
     }
     for (int c = tid; c < cn; c += kQrThreads) taken[c] = (c < ncols) ? 0 : 1;
     __syncthreads();
-    for (int c = wid; c < ncols; c += kQrWarps) {
-        T s = T(0);
-        for (int r = lane; r < nbp; r += 32) { T y = Ys[r + (size_t)c * nbp]; s += y * y; }
-        s = warp_sum(s);
-        if (lane == 0) nrm[c] = s;
+    for (int c = tid; c < ncols; c += kQrThreads) {
+        const T* col = Ys + (size_t)c * ldp;
+        T ss = T(0);
+        for (int r = 0; r < nbp; ++r) ss += col[r] * col[r];
+        nrm[c] = ss;
     }
     __syncthreads();
 
@@ -143,9 +156,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         // (a) local argmax (largest norm; ties -> smallest index)
         T bv = T(-1);
         int bi = -1;
-        for (int c = tid; c < ncols; c += kQrThreads) {
+        for (int c = tid; c < ncols; c += kQrThreads)
             if (!taken[c] && nrm[c] > bv) { bv = nrm[c]; bi = c; }
-        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             T ov = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -154,34 +166,43 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         }
         if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
         __syncthreads();
-        if (tid == 0) {
-            T v0 = T(-1);
-            int i0 = -1;
-            for (int w = 0; w < kQrWarps; ++w) {
-                T ov = s_red_v[w];
-                int oi = s_red_i[w];
-                if (ov > v0 || (ov == v0 && oi >= 0 && (i0 < 0 || oi < i0))) { v0 = ov; i0 = oi; }
+        if (wid == 0) {
+            T ov = lane < kQrWarps ? s_red_v[lane] : T(-1);
+            int oi = lane < kQrWarps ? s_red_i[lane] : -1;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                T xv = __shfl_xor_sync(0xffffffffu, ov, o);
+                int xi = __shfl_xor_sync(0xffffffffu, oi, o);
+                if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; }
             }
-            cand_val[p] = v0;
-            cand_idx[p] = (i0 >= 0) ? c0 + i0 : -1;
-            s_red_i[0] = i0;
+            if (lane == 0) {
+                cand_val[p] = ov;
+                cand_idx[p] = (oi >= 0) ? c0 + oi : -1;
+                s_local = oi;
+            }
         }
         __syncthreads();
         {
-            int li = s_red_i[0];
-            for (int r = tid; r < nbp; r += kQrThreads)
-                cand_col[p * nbp + r] = (li >= 0) ? Ys[r + (size_t)li * nbp] : T(0);
+            const int li = s_local;
+            for (int r = s + tid; r < nbp; r += kQrThreads)
+                cand_col[p * nbp + r] = (li >= 0) ? Ys[r + (size_t)li * ldp] : T(0);
         }
         cluster_sync();
-        // (c) global winner
+        // (b) one batched DSMEM round trip: all candidates and their columns
+        if (tid < kCluster) {
+            s_cv[tid] = dsmem_ld(&cand_val[p], tid);
+            s_ci[tid] = dsmem_ld_s32(&cand_idx[p], tid);
+        }
+        const int rows_left = nbp - s;
+        for (int e = tid; e < kCluster * rows_left; e += kQrThreads) {
+            int q = e / rows_left, r = s + e % rows_left;
+            allc[q * nbp + r] = dsmem_ld(&cand_col[p * nbp + r], q);
+        }
+        __syncthreads();
         if (wid == 0) {
-            T ov = T(-1);
-            int oi = -1, orank = 0;
-            if (lane < kCluster) {
-                ov = dsmem_ld(&cand_val[p], lane);
-                oi = dsmem_ld_s32(&cand_idx[p], lane);
-                orank = lane;
-            }
+            T ov = lane < kCluster ? s_cv[lane] : T(-1);
+            int oi = lane < kCluster ? s_ci[lane] : -1;
+            int orank = lane;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 T xv = __shfl_xor_sync(0xffffffffu, ov, o);
@@ -189,40 +210,51 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 int xr = __shfl_xor_sync(0xffffffffu, orank, o);
                 if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; orank = xr; }
             }
-            // winner column into v (rows s..nbp-1)
-            for (int r = s + lane; r < nbp; r += 32) v[r] = dsmem_ld(&cand_col[p * nbp + r], orank);
-            __syncwarp();
+            const T* wc = allc + orank * nbp;
             T sg = T(0);
-            for (int r = s + 1 + lane; r < nbp; r += 32) sg += v[r] * v[r];
+            for (int r = s + 1 + lane; r < nbp; r += 32) sg += wc[r] * wc[r];
             sg = warp_sum(sg);
             T beta, tau, scale;
-            householder(v[s], sg, beta, tau, scale);
-            __syncwarp();
-            for (int r = s + 1 + lane; r < nbp; r += 32) v[r] *= scale;
+            householder(wc[s], sg, beta, tau, scale);
+            for (int r = s + 1 + lane; r < nbp; r += 32) v[r] = wc[r] * scale;
             if (lane == 0) {
                 v[s] = T(1);
                 s_tau = tau;
+                s_win_idx = oi;
                 if (crank == 0) sel[s] = oi;
                 if (oi >= c0 && oi < c0 + ncols) taken[oi - c0] = 1;
             }
         }
         __syncthreads();
         const T tau = s_tau;
-        // (d) apply H = I - tau v v^T to the untaken local columns, new norms
-        for (int c = wid; c < ncols; c += kQrWarps) {
-            if (taken[c]) continue;
-            T* col = Ys + (size_t)c * nbp;
-            T w = T(0);
-            for (int r = s + lane; r < nbp; r += 32) w += v[r] * col[r];
-            w = warp_sum(w) * tau;
-            T ss = T(0);
-            for (int r = s + lane; r < nbp; r += 32) {
-                T y = col[r] - w * v[r];
-                col[r] = y;
-                if (r > s) ss += y * y;
+        // (c) H = I - tau v v^T on the untaken local columns, new norms (rows > s):
+        // 4 lanes per column, passes uniform across the CTA (quad shuffles)
+        {
+            const int q4 = tid & 3;
+            const int gcol = tid >> 2;
+            const int per_pass = kQrThreads / 4;
+            for (int base = 0; base < ncols; base += per_pass) {
+                const int c = base + gcol;
+                const bool act = c < ncols && !taken[c];
+                T* col = Ys + (size_t)(act ? c : 0) * ldp;
+                T w = T(0);
+                if (act)
+                    for (int r = s + q4; r < nbp; r += 4) w += v[r] * col[r];
+                w += __shfl_xor_sync(0xffffffffu, w, 1);
+                w += __shfl_xor_sync(0xffffffffu, w, 2);
+                w *= tau;
+                T ss = T(0);
+                if (act) {
+                    for (int r = s + q4; r < nbp; r += 4) {
+                        T y = col[r] - w * v[r];
+                        col[r] = y;
+                        if (r > s) ss += y * y;
+                    }
+                }
+                ss += __shfl_xor_sync(0xffffffffu, ss, 1);
+                ss += __shfl_xor_sync(0xffffffffu, ss, 2);
+                if (act && q4 == 0) nrm[c] = ss;
             }
-            ss = warp_sum(ss);
-            if (lane == 0) nrm[c] = ss;
         }
         __syncthreads();
     }
@@ -317,17 +349,55 @@ __global__ void k_perm_ints(int* __restrict__ jpvt, int j0, const int* __restric
 
 // ------------------------------------------------------------- panel ----
 // Pivoted Householder QR of the panel P = A(j0:m, j0:j0+b) held in the
-// cluster's shared memory (CTA c owns panel rows [c*R, c*R+R)).
+// cluster's shared memory: CTA c owns panel rows [c*R, c*R+R) (R a multiple
+// of 4, rows past the panel end are zero).  Per column step s:
+//   (A) cluster barrier, one batched DSMEM round trip gathers the column
+//       norms below row s and the owner's row s  ->  pivot, Householder v;
+//   local swap + scaling of column s;
+//   dots d_c = sum_{r>=s} v_r P[r][c] for every column c != s: for c > s this
+//       is w = V^T P (the rank-1 update), for c < s it is V(:,c)^T v_s, the
+//       column of V^T V that the T factor needs (dlarft recurrence), so T is
+//       built step by step without a separate Gram pass;
+//   (B) cluster barrier, one DSMEM round trip gathers the dots;
+//   update of the columns c > s and their next norms.
+// Row loops use float4 (double2) vectors along the rows of a column.
 template <typename T>
 size_t panel_smem_bytes(int R, int b)
 {
     size_t s = (size_t)R * b * sizeof(T);       // Ps
-    s += 4 * (size_t)kMaxNb * sizeof(T);        // red1, red2, rowS, nrm2
-    s += (size_t)kMaxNb * kMaxNb * sizeof(T);   // gram partial
-    s += (size_t)kMaxNb * kMaxNb * sizeof(T);   // T (rank 0 only)
-    s += 2 * (size_t)kMaxNb * sizeof(int);      // piv history
+    s += 6 * (size_t)kMaxNb * sizeof(T);        // red1, red2, rowS, nrm2, rowL, dots
+    s += (size_t)kMaxNb * kMaxNb * sizeof(T);   // T factor
+    s += 2 * (size_t)kMaxNb * sizeof(int);      // piv history, permutation
     return s + 512;
 }
+
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec4T<double> { using type = double2; static constexpr int n = 2; };
+
+template <typename T>
+SKL_DEV void v_fma(typename Vec4T<T>::type& x, T a, typename Vec4T<T>::type y);
+template <>
+SKL_DEV void v_fma<float>(float4& x, float a, float4 y)
+{ x.x = fmaf(a, y.x, x.x); x.y = fmaf(a, y.y, x.y); x.z = fmaf(a, y.z, x.z); x.w = fmaf(a, y.w, x.w); }
+template <>
+SKL_DEV void v_fma<double>(double2& x, double a, double2 y)
+{ x.x = fma(a, y.x, x.x); x.y = fma(a, y.y, x.y); }
+
+template <typename T>
+SKL_DEV T v_dot(typename Vec4T<T>::type a, typename Vec4T<T>::type b);
+template <>
+SKL_DEV float v_dot<float>(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+template <>
+SKL_DEV double v_dot<double>(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+
+// element e of a vector
+template <typename T>
+SKL_DEV T v_get(const typename Vec4T<T>::type& a, int e);
+template <>
+SKL_DEV float v_get<float>(const float4& a, int e) { return e == 0 ? a.x : e == 1 ? a.y : e == 2 ? a.z : a.w; }
+template <>
+SKL_DEV double v_get<double>(const double2& a, int e) { return e == 0 ? a.x : a.y; }
 
 template <typename T>
 __global__ void __launch_bounds__(kQrThreads)
@@ -335,35 +405,39 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
         T* __restrict__ Tout, int ldt, T* __restrict__ V, int64_t ldv, int* __restrict__ jpvt,
         T* __restrict__ Y, int ldy, int nbp, int pivot_panel)
 {
+    using V4 = typename Vec4T<T>::type;
+    constexpr int VN = Vec4T<T>::n;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned crank = cluster_ctarank();
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int r0 = (int)crank * R;                      // first panel row owned
-    const int nr = max(0, min(R, M - r0));              // rows owned
+    const int nr = max(0, min(R, M - r0));              // real rows owned (rest are zero)
     T* Ps = (T*)smem_raw;                               // [b][R] column-major
     T* red1 = Ps + (size_t)R * b;
     T* red2 = red1 + kMaxNb;
     T* rowS = red2 + kMaxNb;
     T* nrm2 = rowS + kMaxNb;
-    T* gram = nrm2 + kMaxNb;
-    T* Tl = gram + kMaxNb * kMaxNb;
+    T* rowL = nrm2 + kMaxNb;
+    T* dots = rowL + kMaxNb;
+    T* Tl = dots + kMaxNb;                              // [b][kMaxNb], column i at Tl[i*kMaxNb]
     int* pivh = (int*)(Tl + kMaxNb * kMaxNb);
+    int* perm = pivh + kMaxNb;
     __shared__ T s_beta, s_tau, s_scale;
     __shared__ int s_piv;
+    const int nv = R / VN;                              // vectors per column
 
-    // load the panel rows
-    for (int e = tid; e < nr * b; e += kQrThreads) {
-        int lr = e % nr, c = e / nr;
-        Ps[lr + (size_t)c * R] = A[(int64_t)(j0 + r0 + lr) + (int64_t)(j0 + c) * ld];
+    // load the panel rows (zero padding past the panel end)
+    for (int e = tid; e < R * b; e += kQrThreads) {
+        int lr = e % R, c = e / R;
+        Ps[lr + (size_t)c * R] = (lr < nr) ? A[(int64_t)(j0 + r0 + lr) + (int64_t)(j0 + c) * ld] : T(0);
     }
     __syncthreads();
     // initial partial norms over rows > 0 and row 0 values
     for (int c = wid; c < b; c += kQrWarps) {
         T ss = T(0);
         for (int lr = lane; lr < nr; lr += 32) {
-            int g = r0 + lr;
             T x = Ps[lr + (size_t)c * R];
-            if (g > 0) ss += x * x;
+            if (r0 + lr > 0) ss += x * x;
             else rowS[c] = x;
         }
         ss = warp_sum(ss);
@@ -371,138 +445,178 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
     }
     const int steps = min(b, M);
     for (int s = 0; s < steps; ++s) {
-        const unsigned own = (unsigned)(s / R);          // CTA holding panel row s
+        const unsigned own = (unsigned)(s / R);
         cluster_sync();                                  // (A) red1, rowS published
-        // full column norms for columns s..b-1
-        for (int c = s + wid; c < b; c += kQrWarps) {
-            T x = T(0);
-            if (lane < kCluster) x = dsmem_ld(&red1[c], lane);
-            x = warp_sum(x);
-            if (lane == 0) {
-                T a = dsmem_ld(&rowS[c], own);
-                nrm2[c] = x + a * a;
-                red2[c] = x;   // below-row-s part kept for sigma^2 (local copy)
+        {
+            const int q = tid & 15;
+#pragma unroll
+            for (int pass = 0; pass < 2; ++pass) {
+                const int c = s + pass * (kQrThreads / 16) + (tid >> 4);
+                T x = T(0);
+                if (c < b) x = dsmem_ld(&red1[c], q);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (q == 0 && c < b) nrm2[c] = x;
             }
+            if (tid < b - s) rowL[s + tid] = dsmem_ld(&rowS[s + tid], own);
         }
         __syncthreads();
-        if (tid == 0) {
+        if (wid == 0) {
             int piv = s;
-            T best = nrm2[s];
-            if (pivot_panel)
-                for (int c = s + 1; c < b; ++c)
-                    if (nrm2[c] > best) { best = nrm2[c]; piv = c; }
-            T alpha = dsmem_ld(&rowS[piv], own);
-            T beta, tau, scale;
-            householder(alpha, red2[piv], beta, tau, scale);
-            s_piv = piv;
-            s_beta = beta;
-            s_tau = tau;
-            s_scale = scale;
-            pivh[s] = piv;
+            T best = T(-1);
+            for (int c = s + lane; c < b; c += 32) {
+                T v2 = nrm2[c] + rowL[c] * rowL[c];
+                if (v2 > best) { best = v2; piv = c; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int op = __shfl_xor_sync(0xffffffffu, piv, o);
+                if (ob > best || (ob == best && op < piv)) { best = ob; piv = op; }
+            }
+            if (!pivot_panel) piv = s;
+            if (lane == 0) {
+                T beta, tau, scale;
+                householder(rowL[piv], nrm2[piv], beta, tau, scale);
+                s_piv = piv;
+                s_beta = beta;
+                s_tau = tau;
+                s_scale = scale;
+                pivh[s] = piv;
+            }
         }
         __syncthreads();
         const int piv = s_piv;
-        const T tau = s_tau, scale = s_scale;
-        if (piv != s) {
-            for (int lr = tid; lr < nr; lr += kQrThreads) {
-                T a = Ps[lr + (size_t)s * R], c = Ps[lr + (size_t)piv * R];
-                Ps[lr + (size_t)s * R] = c;
+        const T tau = s_tau, scale = s_scale, beta = s_beta;
+        for (int lr = tid; lr < R; lr += kQrThreads) {
+            T a = Ps[lr + (size_t)s * R];
+            if (piv != s) {
+                T c = Ps[lr + (size_t)piv * R];
                 Ps[lr + (size_t)piv * R] = a;
+                a = c;
             }
+            const int g = r0 + lr;
+            if (g > s) a *= scale;
+            else if (g == s) a = beta;
+            Ps[lr + (size_t)s * R] = a;
         }
         __syncthreads();
-        // v: scale rows > s of column s; row s keeps beta (R_ss), v_s = 1
-        for (int lr = tid; lr < nr; lr += kQrThreads) {
-            int g = r0 + lr;
-            if (g > s) Ps[lr + (size_t)s * R] *= scale;
-            else if (g == s) Ps[lr + (size_t)s * R] = s_beta;
-        }
-        __syncthreads();
-        // partial w_c = sum_{rows >= s} v_r P[r][c], c > s
-        const int lr_s = max(0, s - r0);   // first local row with g >= s
-        for (int c = s + 1 + wid; c < b; c += kQrWarps) {
-            T acc = T(0);
-            for (int lr = lr_s + lane; lr < nr; lr += 32) {
-                int g = r0 + lr;
-                T vv = (g == s) ? T(1) : Ps[lr + (size_t)s * R];
-                acc += vv * Ps[lr + (size_t)c * R];
+        // v restricted to rows >= s: vectors of VN rows; the vector holding
+        // row s gets v_s = 1 and zeros above
+        const int lr_s = max(0, s - r0);
+        const int q0 = lr_s / VN;
+        auto vload = [&](int qv) -> V4 {
+            V4 vv = reinterpret_cast<const V4*>(Ps + (size_t)s * R)[qv];
+            const int base = r0 + qv * VN;
+            if (base + VN - 1 >= s && base <= s) {
+                T* pv = reinterpret_cast<T*>(&vv);
+#pragma unroll
+                for (int e = 0; e < VN; ++e) {
+                    int g = base + e;
+                    pv[e] = (g < s) ? T(0) : (g == s ? T(1) : pv[e]);
+                }
             }
-            acc = warp_sum(acc);
-            if (lane == 0) red2[c] = acc;
+            return vv;
+        };
+        // dots for all columns c != s (4 per warp, covering 64 columns)
+        {
+            T acc[4] = {T(0), T(0), T(0), T(0)};
+            for (int qv = q0 + lane; qv < nv; qv += 32) {
+                const V4 vv = vload(qv);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = wid + q * kQrWarps;
+                    if (c < b && c != s) acc[q] += v_dot<T>(vv, reinterpret_cast<const V4*>(Ps + (size_t)c * R)[qv]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = wid + q * kQrWarps;
+                T x = warp_sum(acc[q]);
+                if (lane == 0 && c < b) red2[c] = x;
+            }
         }
         cluster_sync();                                  // (B) red2 published
-        for (int c = s + 1 + wid; c < b; c += kQrWarps) {
-            T w = T(0);
-            if (lane < kCluster) w = dsmem_ld(&red2[c], lane);
-            w = warp_sum(w) * tau;
-            T ss = T(0);
-            for (int lr = lr_s + lane; lr < nr; lr += 32) {
-                int g = r0 + lr;
-                T vv = (g == s) ? T(1) : Ps[lr + (size_t)s * R];
-                T x = Ps[lr + (size_t)c * R] - w * vv;
-                Ps[lr + (size_t)c * R] = x;
-                if (g > s + 1) ss += x * x;
-                else if (g == s + 1) rowS[c] = x;
+        {
+            const int q = tid & 15;
+#pragma unroll
+            for (int pass = 0; pass < 2; ++pass) {
+                const int c = pass * (kQrThreads / 16) + (tid >> 4);
+                T x = T(0);
+                if (c < b) x = dsmem_ld(&red2[c], q);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (q == 0 && c < b) dots[c] = x;
             }
-            ss = warp_sum(ss);
-            if (lane == 0) red1[c] = ss;
+        }
+        __syncthreads();
+        // T(0:s, s) = -tau * T(0:s, 0:s) * (V(:,0:s)^T v_s), T(s,s) = tau
+        if (wid == 1) {
+            for (int i = lane; i < s; i += 32) {
+                T acc = T(0);
+                for (int c = i; c < s; ++c) acc += Tl[i + c * kMaxNb] * dots[c];
+                Tl[i + s * kMaxNb] = -tau * acc;
+            }
+            if (lane == 0) Tl[s + s * kMaxNb] = tau;
+        }
+        // update columns c > s, next partial norms (rows > s+1) and row s+1
+        {
+            T ss[4] = {T(0), T(0), T(0), T(0)};
+            T wq[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = wid + q * kQrWarps;
+                wq[q] = (c < b && c > s) ? dots[c] * tau : T(0);
+            }
+            for (int qv = q0 + lane; qv < nv; qv += 32) {
+                const V4 vv = vload(qv);
+                const int base = r0 + qv * VN;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = wid + q * kQrWarps;
+                    if (c < b && c > s) {
+                        V4* pc = reinterpret_cast<V4*>(Ps + (size_t)c * R) + qv;
+                        V4 x = *pc;
+                        v_fma<T>(x, -wq[q], vv);
+                        *pc = x;
+                        const T* px = reinterpret_cast<const T*>(&x);
+#pragma unroll
+                        for (int e = 0; e < VN; ++e) {
+                            const int g = base + e;
+                            if (g > s + 1) ss[q] += px[e] * px[e];
+                            else if (g == s + 1) rowS[c] = px[e];
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = wid + q * kQrWarps;
+                T x = warp_sum(ss[q]);
+                if (lane == 0 && c < b && c > s) red1[c] = x;
+            }
         }
         if (tid == 0 && crank == 0) tau_out[j0 + s] = tau;
         __syncthreads();
     }
-    // Gram matrix of V (unit lower trapezoid) for the T factor: one warp per
-    // (a, c) pair, lanes over rows.
-    for (int e = wid; e < b * b; e += kQrWarps) {
-        int a = e % b, c = e / b;
-        T acc = T(0);
-        if (a < c) {
-            int lr0 = max(0, c - r0);          // V[:,c] is zero above row c
-            for (int lr = lr0 + lane; lr < nr; lr += 32) {
-                int g = r0 + lr;
-                T vc = (g == c) ? T(1) : Ps[lr + (size_t)c * R];
-                T va = Ps[lr + (size_t)a * R];  // g >= c > a
-                acc += va * vc;
-            }
-            acc = warp_sum(acc);
+    // final permutation of the panel's columns (composition of the swaps)
+    if (tid == 0) {
+        for (int t = 0; t < b; ++t) perm[t] = t;
+        for (int s2 = 0; s2 < steps; ++s2) {
+            int p2 = pivh[s2];
+            int x = perm[s2];
+            perm[s2] = perm[p2];
+            perm[p2] = x;
         }
-        if (lane == 0) gram[a + c * kMaxNb] = acc;
     }
-    cluster_sync();
     if (crank == 0) {
-        // sum the partial Gram matrices
         for (int e = tid; e < b * b; e += kQrThreads) {
             int a = e % b, c = e / b;
-            if (a >= c) continue;
-            T acc = T(0);
-            for (int q = 0; q < kCluster; ++q) acc += dsmem_ld(&gram[a + c * kMaxNb], q);
-            Tl[a + c * kMaxNb] = acc;     // holds V_a^T V_c for a < c (temporarily)
-        }
-        __syncthreads();
-        // T (dlarft forward/columnwise): T_ii = tau_i,
-        // T(0:i, i) = -tau_i * T(0:i, 0:i) * (V(:,0:i)^T v_i)
-        __shared__ T col[kMaxNb];
-        for (int i = 0; i < b; ++i) {
-            T ti = tau_out[j0 + i];
-            if (tid < i) col[tid] = Tl[tid + i * kMaxNb];
-            __syncthreads();
-            if (tid < i) {
-                T acc = T(0);
-                for (int c = tid; c < i; ++c) acc += gram[tid + c * kMaxNb] * col[c];
-                // gram[] now used as the T storage (upper part), see below
-                Tl[tid + i * kMaxNb] = -ti * acc;
-            }
-            __syncthreads();
-            if (tid == 0) gram[i + i * kMaxNb] = ti;
-            if (tid < i) gram[tid + i * kMaxNb] = Tl[tid + i * kMaxNb];
-            __syncthreads();
-        }
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            int a = e % b, c = e / b;
-            Tout[a + (int64_t)c * ldt] = (a <= c) ? gram[a + c * kMaxNb] : T(0);
+            Tout[a + (int64_t)c * ldt] = (a <= c) ? Tl[a + c * kMaxNb] : T(0);
         }
     }
-    cluster_sync();   // other CTAs' Gram partials must stay alive until read
-    // write back panel: R (upper) + V (below) into A; explicit V into V buffer
+    cluster_sync();   // no CTA leaves while others may still read its shared memory
+    // write back panel: R (upper) + V (below) into A; explicit V into the V buffer
     for (int e = tid; e < nr * b; e += kQrThreads) {
         int lr = e % nr, c = e / nr;
         int g = r0 + lr;
@@ -510,41 +624,23 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
         A[(int64_t)(j0 + g) + (int64_t)(j0 + c) * ld] = x;
         V[(int64_t)g + (int64_t)c * ldv] = (g > c) ? x : (g == c ? T(1) : T(0));
     }
-    // apply the panel's column swaps to rows above the panel, to Y and jpvt
+    // permute the columns j0..j0+b of the rows above the panel, of Y and of
+    // jpvt: each row gathers its b values once (independent loads), then stores
     const int nabove = j0;
     for (int row = (int)crank * kQrThreads + tid; row < nabove + nbp + 1;
          row += kCluster * kQrThreads) {
-        if (row < nabove) {
-            T* base = A + row;
-            for (int s = 0; s < steps; ++s) {
-                int p = pivh[s];
-                if (p != s) {
-                    T a = base[(int64_t)(j0 + s) * ld];
-                    base[(int64_t)(j0 + s) * ld] = base[(int64_t)(j0 + p) * ld];
-                    base[(int64_t)(j0 + p) * ld] = a;
-                }
-            }
-        } else if (row < nabove + nbp) {
-            if (Y) {
-                T* base = Y + (row - nabove);
-                for (int s = 0; s < steps; ++s) {
-                    int p = pivh[s];
-                    if (p != s) {
-                        T a = base[(int64_t)(j0 + s) * ldy];
-                        base[(int64_t)(j0 + s) * ldy] = base[(int64_t)(j0 + p) * ldy];
-                        base[(int64_t)(j0 + p) * ldy] = a;
-                    }
-                }
-            }
-        } else {
-            for (int s = 0; s < steps; ++s) {
-                int p = pivh[s];
-                if (p != s) {
-                    int a = jpvt[j0 + s];
-                    jpvt[j0 + s] = jpvt[j0 + p];
-                    jpvt[j0 + p] = a;
-                }
-            }
+        if (row < nabove || (row < nabove + nbp && Y)) {
+            T* base = row < nabove ? A + row : Y + (row - nabove);
+            const int64_t stride = row < nabove ? ld : (int64_t)ldy;
+            T vals[kMaxNb];
+#pragma unroll 8
+            for (int t = 0; t < b; ++t) vals[t] = base[(int64_t)(j0 + perm[t]) * stride];
+#pragma unroll 8
+            for (int t = 0; t < b; ++t) base[(int64_t)(j0 + t) * stride] = vals[t];
+        } else if (row == nabove + nbp) {
+            int vals[kMaxNb];
+            for (int t = 0; t < b; ++t) vals[t] = jpvt[j0 + perm[t]];
+            for (int t = 0; t < b; ++t) jpvt[j0 + t] = vals[t];
         }
     }
 }
@@ -609,6 +705,7 @@ static QrPlan qr_plan(int64_t m, int64_t d)
 {
     QrPlan p;
     p.R = (int)((m + kCluster - 1) / kCluster);
+    p.R = (p.R + 3) / 4 * 4;   // whole float4 / double2 row vectors
     int nb = kMaxNb;
     size_t budget = 200 * 1024;
     while (nb > 8 && panel_smem_bytes<T>(p.R, nb) > budget) nb -= 8;
@@ -697,10 +794,54 @@ static void launch_cluster(const void* fn, dim3 block, size_t smem, cudaStream_t
     SKL_LAUNCHED();
 }
 
+// Event pairs around QR sub-steps (profiling only).
+struct QrTimer {
+    double* acc;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    cudaStream_t st;
+    cudaEvent_t get()
+    {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            SKL_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    cudaEvent_t begin()
+    {
+        if (!acc) return nullptr;
+        cudaEvent_t e = get();
+        SKL_CUDA(cudaEventRecord(e, st));
+        return e;
+    }
+    void end(int slot, cudaEvent_t b)
+    {
+        if (!acc) return;
+        cudaEvent_t e = get();
+        SKL_CUDA(cudaEventRecord(e, st));
+        marks.push_back({slot, {b, e}});
+    }
+    void finish()
+    {
+        if (!acc) return;
+        SKL_CUDA(cudaStreamSynchronize(st));
+        for (auto& mk : marks) {
+            float ms = 0.f;
+            SKL_CUDA(cudaEventElapsedTime(&ms, mk.second.first, mk.second.second));
+            acc[mk.first] += ms;
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
 template <typename T>
 static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
-                    cudaStream_t st, double* c, bool pivoting)
+                    cudaStream_t st, double* c, bool pivoting, double* qr_prof)
 {
+    QrTimer tm{qr_prof, {}, {}, 0, st};
     QrPlan p = qr_plan<T>(m, d);
     QrBuffers<T> B = qr_carve<T>(work, m, d, p, nullptr);
     const int nb = p.nb, nbp = p.nbp;
@@ -712,8 +853,10 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         k_gaussian<T><<<(unsigned)((cnt + 255) / 256 < 2048 ? (cnt + 255) / 256 : 2048), 256, 0, st>>>(
             B.G, cnt, 0x5eed000000000012ull);
         SKL_LAUNCHED();
+        cudaEvent_t t0 = tm.begin();
         gemm<T>(false, false, nbp, (int)d, (int)m, T(1), B.G, nbp, A, ld, T(0), B.Y, nbp, B.part,
                 B.part_cap, st);
+        tm.end(8, t0);
     }
     const size_t ysm_max = YqrpSmem<T>::bytes(nbp, (int)((d + kCluster - 1) / kCluster));
     const size_t psm = panel_smem_bytes<T>(p.R, nb);
@@ -729,8 +872,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             const T* Yc = B.Y;
             int* sel = B.sel;
             void* args[] = {(void*)&Yc, &ldy, (void*)&nbp, &jj, (void*)&N, (void*)&b, &sel};
+            cudaEvent_t t0 = tm.begin();
             launch_cluster<T>((const void*)k_yqrp<T>, dim3(kQrThreads), ysm_max, st, args);
+            tm.end(0, t0);
             trace_phase(st, "qr: yqrp");
+            t0 = tm.begin();
             k_perm_plan<<<1, kMaxNb, 0, st>>>(B.sel, b, B.plan_src, B.plan_dst, B.plan_n);
             SKL_LAUNCHED();
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
@@ -741,6 +887,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             k_perm_scatter<T><<<gY, 128, 0, st>>>(B.Y, nbp, nbp, jj, B.plan_dst, B.plan_n, B.tmp);
             k_perm_ints<<<1, 128, 0, st>>>(jpvt, jj, B.plan_src, B.plan_dst, B.plan_n);
             for (int q = 0; q < 5; ++q) SKL_LAUNCHED();
+            tm.end(1, t0);
         }
         {
             // panel: with pivoting=false the panel keeps its column order
@@ -754,26 +901,37 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             int pp = pivoting ? 1 : 0;
             void* args[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
                             &ldv, &jpvt, &Yp, &ldy, &nbpp, &pp};
+            cudaEvent_t t0 = tm.begin();
             launch_cluster<T>((const void*)k_panel<T>, dim3(kQrThreads), psm, st, args);
+            tm.end(2, t0);
             trace_phase(st, "qr: panel");
         }
         if (c) {
+            cudaEvent_t t0 = tm.begin();
             k_qt_w<T><<<b, 256, 0, st>>>(B.V, m, M, b, c + j, B.qw);
             k_qt_update<T><<<(unsigned)std::min<int64_t>((M + 255) / 256, 256), 256, 0, st>>>(
                 B.V, m, M, b, B.Tm, nb, B.qw, c + j);
             SKL_LAUNCHED();
             SKL_LAUNCHED();
+            tm.end(3, t0);
         }
         const int N2 = N - b;
         if (N2 > 0) {
             T* Atr = A + j + (j + b) * ld;
             // W = V^T A_trail ; Z = T^T W ; A_trail -= V Z
+            cudaEvent_t t0 = tm.begin();
             gemm<T>(true, false, b, N2, M, T(1), B.V, m, Atr, ld, T(0), B.W, b, B.part,
                     B.part_cap, st);
+            tm.end(4, t0);
+            t0 = tm.begin();
             gemm<T>(true, false, b, N2, b, T(1), B.Tm, nb, B.W, b, T(0), B.Z, b, nullptr, 0, st);
+            tm.end(5, t0);
+            t0 = tm.begin();
             gemm<T>(false, false, M, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
+            tm.end(6, t0);
         }
         if (pivoting && !last) {
+            cudaEvent_t t0 = tm.begin();
             T* Gj = B.G + j * nbp;
             // GU = G(:, j:m) V ; GUT = GU T ; B = G1 - GUT U11^T ; Y2 -= B R12 ; G(:, j:m) -= GUT V^T
             gemm<T>(false, false, nbp, b, M, T(1), Gj, nbp, B.V, m, T(0), B.GU, nbp, B.part,
@@ -789,22 +947,24 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
                         B.Y + (j + b) * nbp, nbp, nullptr, 0, st);
             gemm<T>(false, true, nbp, M, b, T(-1), B.GUT, nbp, B.V, m, T(1), Gj, nbp, nullptr, 0,
                     st);
+            tm.end(7, t0);
         }
     }
+    tm.finish();
 }
 
 template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work, unsigned* status,
-          cudaStream_t st, double* c, int pivoting)
+          cudaStream_t st, double* c, int pivoting, double* qr_prof)
 {
     (void)status;
-    qr_core<T>(A, m, d, ld, jpvt, tau, work, st, c, pivoting != 0);
+    qr_core<T>(A, m, d, ld, jpvt, tau, work, st, c, pivoting != 0, qr_prof);
 }
 
 template void cpqr<float>(float*, int64_t, int64_t, int64_t, int*, float*, void*, unsigned*,
-                          cudaStream_t, double*, int);
+                          cudaStream_t, double*, int, double*);
 template void cpqr<double>(double*, int64_t, int64_t, int64_t, int*, double*, void*, unsigned*,
-                           cudaStream_t, double*, int);
+                           cudaStream_t, double*, int, double*);
 template size_t cpqr_workspace_bytes<float>(int64_t, int64_t);
 template size_t cpqr_workspace_bytes<double>(int64_t, int64_t);
 

@@ -242,7 +242,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     S.add<unsigned>(n * k); S.add<int>(m + 1); S.add<unsigned>(n * k);
     S.add<T>(ld * d); S.add<double>(d); S.add<double>(d); S.add<double>(m);
     S.add<int>(d); S.add<T>(mn); S.add<int>(4);
-    S.add<T>(d * d); S.add<T>(d * d); S.add<double>(4);
+    S.add<T>(round_up(d, 4) * d); S.add<T>(round_up(d, 4) * d); S.add<double>(4);
     S.add<double>(d); S.add<double>(n); S.add<double>(d); S.add<double>(1024); S.add<double>(8);
     S.add<char>((int64_t)std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
     S.add<float2>(d);
@@ -266,8 +266,8 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     int* jpvt = Ar.alloc<int>(d);
     T* tau = Ar.alloc<T>(mn);
     int* dint = Ar.alloc<int>(4);
-    T* Mc = Ar.alloc<T>(d * d);
-    T* Mr = Ar.alloc<T>(d * d);
+    T* Mc = Ar.alloc<T>(round_up(d, 4) * d);
+    T* Mr = Ar.alloc<T>(round_up(d, 4) * d);
     double* norms = Ar.alloc<double>(4);
     double* yv = Ar.alloc<double>(d);
     double* rs = Ar.alloc<double>(n);
@@ -307,7 +307,8 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     trace_phase(st, "sketch");
     SKL_CUDA(cudaEventRecord(ev[3], st));
     // ---- randomized CPQR, c = Q^T S b ----
-    cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1);
+    cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1,
+            o.profile ? info.qr_prof_ms : nullptr);
     trace_phase(st, "cpqr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank, inverse, condition ----
@@ -316,7 +317,8 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     int64_t rank = count_rank<T>(SA, ld, mn, 0.0, rel, dint, (int*)C.host_pinned, st);
     if (rank == 0) fail(SKL_ERR_RANK_ZERO, "SPQR Factorization fails");
     info.rank = rank;
-    trinv_upper<T>(SA, ld, rank, 0.0, Mc, rank, norms, work, st);
+    const int64_t ldm = round_up(rank, 4);   // 16-byte aligned rows/columns of M
+    trinv_upper<T>(SA, ld, rank, 0.0, Mc, ldm, norms, work, st);
     SKL_CUDA(cudaMemcpyAsync(C.host_pinned, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     SKL_CUDA(cudaStreamSynchronize(st));
     double nr = ((double*)C.host_pinned)[0], nm = ((double*)C.host_pinned)[1];
@@ -324,9 +326,9 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     info.rcond_r11 = rcond;
     info.success = rcond > o.rcond_threshold ? 1 : 0;
     if (!info.success && o.perturb != 0.0) {
-        trinv_upper<T>(SA, ld, rank, o.perturb, Mc, rank, norms, work, st);
+        trinv_upper<T>(SA, ld, rank, o.perturb, Mc, ldm, norms, work, st);
     }
-    transpose_upper<T>(Mc, rank, rank, Mr, st);
+    transpose_upper<T>(Mc, ldm, rank, Mr, st);
     trace_phase(st, "rank+inverse");
     LsqrProblem P;
     P.n = n; P.d = d; P.nnz = nnz;
@@ -334,7 +336,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     P.cp = cp; P.ri = ri; P.rx = mixed ? (const void*)rx2 : (const void*)in.Ax;
     P.cx64 = cx; P.rx64 = in.Ax;
     P.cols = jpvt; P.colscale = colscale;
-    P.M = Mc; P.Mrow = Mr; P.ldm = rank; P.r = rank; P.precision = o.precision;
+    P.M = Mc; P.Mrow = Mr; P.ldm = ldm; P.r = rank; P.precision = o.precision;
     // ---- explicit sketch solution xs = D P1 M c ----
     SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
     precond_apply(P, cvec, x_dev, ysplit, st);
@@ -550,6 +552,283 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
     if (info) *info = inf;
 }
 
+
+// --------------------------------------------------------- dense solve ---
+// ls_dense_hashing_blendenpik (src/ls_dense_hashing_blendenpik.cpp:23-149) and,
+// with use_cpqr = 0, ls_dense_hashing_blendenpik_noCPQR
+// (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-59).
+
+template <typename T>
+static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t lda, int64_t n,
+                           int64_t d, const double* b, double* x_dev, const skl_opts& o,
+                           skl_info& info, bool timing_upload, std::thread* host_thread,
+                           const std::vector<double>* hD, const std::vector<uint32_t>* hh,
+                           int64_t N)
+{
+    const bool mixed = std::is_same<T, float>::value;
+    const bool cpqr_on = o.use_cpqr != 0;
+    const int64_t k = o.k;
+    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+    if (m < d) fail(SKL_ERR_INVALID, "sketch has fewer rows than A has columns (gamma*d < d)");
+    const int64_t ld = round_up(m, 32);
+    const int64_t mn = std::min(m, d);
+    info.sketch_rows = m;
+    const size_t qr_ws = cpqr_workspace_bytes<T>(m, d);
+    const size_t inv_ws = trinv_workspace_bytes<T>(d);
+    LsqrProblem Pq;
+    Pq.n = n; Pq.d = d; Pq.r = d; Pq.precision = o.precision; Pq.Ad = A; Pq.lda = n;
+    const size_t lsqr_ws = lsqr_workspace_bytes(Pq);
+    const size_t bkt_scr = build_buckets_scratch_ints(m, N * k) * sizeof(int);
+    const size_t dht_ws = dht_scratch_bytes(N, o.precision);
+    const size_t work_bytes = std::max({qr_ws, inv_ws, lsqr_ws, bkt_scr, dht_ws});
+    const int64_t ldm_max = round_up(d, 4);
+    Sizer S;
+    S.add<double>(n); S.add<unsigned>(N * k); S.add<int>(m + 1); S.add<unsigned>(N * k);
+    S.add<char>(mixed ? (int64_t)(n * d * sizeof(float2)) : 0);
+    S.add<T>(ld * d); S.add<double>(d); S.add<double>(m); S.add<int>(d); S.add<T>(mn); S.add<int>(4);
+    S.add<T>(ldm_max * d); S.add<T>(ldm_max * d); S.add<double>(4); S.add<double>(d);
+    S.add<double>(n); S.add<double>(d); S.add<double>(1024); S.add<double>(8);
+    S.add<char>((int64_t)work_bytes); S.add<float2>(d);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    Arena& Ar = C.arena;
+    double* Dd = Ar.alloc<double>(n);
+    unsigned* hidx = Ar.alloc<unsigned>(N * k);
+    int* bptr = Ar.alloc<int>(m + 1);
+    unsigned* bent = Ar.alloc<unsigned>(N * k);
+    float2* A2 = mixed ? (float2*)Ar.take(n * d * sizeof(float2)) : nullptr;
+    T* SA = Ar.alloc<T>(ld * d);
+    double* colscale = Ar.alloc<double>(d);
+    double* cvec = Ar.alloc<double>(m);
+    int* jpvt = Ar.alloc<int>(d);
+    T* tau = Ar.alloc<T>(mn);
+    int* dint = Ar.alloc<int>(4);
+    T* Mc = Ar.alloc<T>(ldm_max * d);
+    T* Mr = Ar.alloc<T>(ldm_max * d);
+    double* norms = Ar.alloc<double>(4);
+    double* yv = Ar.alloc<double>(d);
+    double* rs = Ar.alloc<double>(n);
+    double* xacc = Ar.alloc<double>(d);
+    double* part = Ar.alloc<double>(1024);
+    double* scal = Ar.alloc<double>(8);
+    void* work = Ar.take(work_bytes);
+    float2* ysplit = Ar.alloc<float2>(d);
+    cudaEvent_t* ev = C.ev;
+    SKL_CUDA(cudaEventRecord(ev[1], st));
+    if (mixed) split_dense(A, lda, n, d, A2, st);
+    {
+        std::vector<double> ones((size_t)d, 1.0);
+        SKL_CUDA(cudaMemcpyAsync(colscale, ones.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+    }
+    host_thread->join();
+    SKL_CUDA(cudaMemcpyAsync(Dd, hD->data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(hidx, hh->data(), N * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    build_buckets(hidx, N, (int)k, m, bptr, bent, (int*)work, st);
+    SKL_CUDA(cudaEventRecord(ev[2], st));
+    // ---- sketch: DHT + hash of A (and b) ----
+    dht_hash<T>(A, lda, n, d, Dd, N, bptr, bent, (int)k, m, SA, ld, nullptr, 0, work, work_bytes, st);
+    if (cpqr_on) dht_hash_rhs(b, n, Dd, N, bptr, bent, (int)k, m, cvec, work, work_bytes, st);
+    trace_phase(st, "dense sketch");
+    SKL_CUDA(cudaEventRecord(ev[3], st));
+    // ---- QR (pivoted for the CPQR path) ----
+    cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cpqr_on ? cvec : nullptr,
+            cpqr_on ? 1 : 0, o.profile ? info.qr_prof_ms : nullptr);
+    trace_phase(st, "dense qr");
+    SKL_CUDA(cudaEventRecord(ev[4], st));
+    // ---- rank: leading |R_ii| > rcond (absolute, :79-89); noCPQR keeps all ----
+    int64_t rank = d;
+    if (cpqr_on) {
+        // the reference's absolute rule, floored at the working precision's
+        // resolution of the sketch (FP32 cannot resolve |R_ii| below eps*|R_00|)
+        const double floor_rel = mixed ? 5.960464477539063e-08 : 0.0;
+        rank = count_rank<T>(SA, ld, mn, o.rcond, floor_rel, dint, (int*)C.host_pinned, st);
+        if (rank == 0) fail(SKL_ERR_RANK_ZERO, "sketch has no diagonal entry above rcond");
+    }
+    info.rank = rank;
+    info.success = 1;
+    const int64_t ldm = round_up(rank, 4);
+    trinv_upper<T>(SA, ld, rank, 0.0, Mc, ldm, norms, work, st);
+    transpose_upper<T>(Mc, ldm, rank, Mr, st);
+    SKL_CUDA(cudaMemcpyAsync(C.host_pinned, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    {
+        double nr = ((double*)C.host_pinned)[0], nm = ((double*)C.host_pinned)[1];
+        info.rcond_r11 = (nr > 0 && nm > 0) ? 1.0 / (nr * nm) : 0.0;
+    }
+    LsqrProblem P;
+    P.n = n; P.d = d; P.nnz = n * d;
+    P.Ad = mixed ? (const void*)A2 : (const void*)A;
+    P.lda = mixed ? n : lda;
+    P.Ad64 = A; P.lda64 = lda;
+    P.cols = jpvt; P.colscale = colscale;
+    P.M = Mc; P.Mrow = Mr; P.ldm = ldm; P.r = rank; P.precision = o.precision;
+    // ||A||_F
+    fro_partials(A, lda, n, d, part, st);
+    std::vector<double> fp(512);
+    SKL_CUDA(cudaMemcpyAsync(fp.data(), part, 512 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    double fro = 0.0;
+    for (double v : fp) fro += v;
+    fro = std::sqrt(fro);
+    double rnorm = 0.0, be = 0.0;
+    auto residual = [&]() {
+        residual_and_backward(P, x_dev, b, rs, part, scal, st);
+        SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        rnorm = ((double*)C.host_pinned)[0];
+        be = (rnorm > 0 && fro > 0) ? ((double*)C.host_pinned)[1] / (fro * rnorm) : 0.0;
+    };
+    auto add_prof = [&](const LsqrResult& Rr) {
+        for (int q = 0; q < 4; ++q) {
+            info.prof_ms[q] += Rr.prof_ms[q];
+            info.prof_launches[q] += Rr.prof_launches[q];
+        }
+    };
+    SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
+    info.it = 0;
+    info.flag = 0;
+    bool solved = false;
+    if (cpqr_on) {
+        // explicit sketch solution xs = P1 M c, early exit (:93-117)
+        precond_apply(P, cvec, x_dev, ysplit, st);
+        residual();
+        info.explicit_residual = rnorm;
+        solved = rnorm < o.abs_tol;
+    }
+    SKL_CUDA(cudaEventRecord(ev[5], st));
+    if (!solved) {
+        // LSQR on A P1 M from r_s (CPQR path) or from b with y = 0 (noCPQR path)
+        const double* rhs = b;
+        if (cpqr_on) rhs = rs;
+        LsqrResult R = lsqr_run(P, rhs, o.it_tol, o.max_it, yv, work, C.dev_status, C.host_pinned,
+                                st, o.profile, C.stream);
+        add_prof(R);
+        int64_t total_it = R.it;
+        int flag = R.flag;
+        if (cpqr_on) {
+            std::vector<double> h((size_t)rank), hc((size_t)rank);
+            SKL_CUDA(cudaMemcpyAsync(h.data(), yv, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaMemcpyAsync(hc.data(), cvec, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            for (int64_t i = 0; i < rank; ++i) h[(size_t)i] += hc[(size_t)i];
+            SKL_CUDA(cudaMemcpyAsync(yv, h.data(), rank * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
+        precond_apply(P, yv, x_dev, ysplit, st);
+        residual();
+        int64_t restarts = 0;
+        while (o.backward_tol > 0.0 && be > o.backward_tol && restarts < o.max_refine &&
+               total_it < o.max_it) {
+            ++restarts;
+            R = lsqr_run(P, rs, o.it_tol, o.max_it - total_it, yv, work, C.dev_status,
+                         C.host_pinned, st, o.profile, C.stream);
+            add_prof(R);
+            total_it += R.it;
+            flag = R.flag;
+            SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
+            precond_apply(P, yv, xacc, ysplit, st);
+            std::vector<double> hx((size_t)d), ha((size_t)d);
+            SKL_CUDA(cudaMemcpyAsync(hx.data(), x_dev, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaMemcpyAsync(ha.data(), xacc, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            for (int64_t j = 0; j < d; ++j) hx[(size_t)j] += ha[(size_t)j];
+            SKL_CUDA(cudaMemcpyAsync(x_dev, hx.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+            residual();
+        }
+        info.it = total_it;
+        info.flag = flag;
+    }
+    SKL_CUDA(cudaEventRecord(ev[6], st));
+    SKL_CUDA(cudaEventSynchronize(ev[6]));
+    info.residual_norm = rnorm;
+    info.backward_error = be;
+    info.t_setup_ms = elapsed(ev[1], ev[2]);
+    info.t_sketch_ms = elapsed(ev[2], ev[3]);
+    info.t_qr_ms = elapsed(ev[3], ev[4]);
+    info.t_precond_ms = elapsed(ev[4], ev[5]);
+    info.t_lsqr_ms = elapsed(ev[5], ev[6]);
+    info.t_total_ms = elapsed(timing_upload ? ev[0] : ev[1], ev[6]);
+    if (timing_upload) info.t_upload_ms = elapsed(ev[0], ev[1]);
+}
+
+static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
+                               double* x, const skl_opts* opts, skl_info* info, bool host)
+{
+    skl_opts o;
+    if (opts) o = *opts;
+    else fill_default(&o);
+    check_opts(o);
+    if (n < 0 || d < 0) fail(SKL_ERR_INVALID, "negative dimension");
+    if (n < d) fail(SKL_ERR_NOT_OVERDETERMINED, "Matrix is not overdetermined.");
+    if (!A || !b || !x) fail(SKL_ERR_INVALID, "A, b or x is null");
+    if (lda < std::max<int64_t>(1, n)) fail(SKL_ERR_INVALID, "lda < n");
+    skl_info inf;
+    std::memset(&inf, 0, sizeof inf);
+    if (d == 0) {
+        if (info) *info = inf;
+        return;
+    }
+    Context& C = context(o.device);
+    reset_launch_count();
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : C.stream;
+    const int64_t N = dht_length(n, o.wisdom);
+    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+    if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
+    if (N > 0x7fffffff || m > 0x7fffffff) fail(SKL_ERR_INVALID, "problem too large");
+    // signs then hash from one reseeded stream (srand(time(NULL)) in the
+    // reference, src/dense_helpers.cpp:92 and :12; seed 0 selects time)
+    const uint32_t seed = o.seed ? o.seed : (uint32_t)time(nullptr);
+    std::vector<double> hD((size_t)n);
+    std::vector<uint32_t> hh((size_t)(N * o.k));
+    double hash_ms = 0.0;
+    const bool hqrrp_stream = o.use_cpqr && std::min(m, d) >= 1000;
+    std::thread th([&]() {
+        auto t0 = std::chrono::steady_clock::now();
+        rng_srand(seed);
+        rng_lock();
+        gen_signs(n, hD.data());
+        gen_hash_packed(m, N, o.k, hh.data());
+        rng_unlock();
+        hash_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    });
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() { if (t.joinable()) t.join(); }
+    } joiner{th};
+    SKL_CUDA(cudaEventRecord(C.ev[0], st));
+    if (host) {
+        Sizer S;
+        S.add<double>(n * d); S.add<double>(n); S.add<double>(d);
+        C.staging.reserve(S.bytes());
+        C.staging.reset();
+        double* Ad = C.staging.alloc<double>(n * d);
+        double* bd = C.staging.alloc<double>(n);
+        double* xd = C.staging.alloc<double>(d);
+        SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double),
+                                   d, cudaMemcpyHostToDevice, st));
+        SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (o.precision == SKL_PREC_MIXED)
+            dense_pipeline<float>(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
+        else
+            dense_pipeline<double>(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
+        SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+    } else {
+        if (o.precision == SKL_PREC_MIXED)
+            dense_pipeline<float>(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
+        else
+            dense_pipeline<double>(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
+    }
+    // HQRRP reseeds the C library stream with srand(12) and draws its Gaussian
+    // sample (hqrrp/.../NoFLA_HQRRP_WY_blk_var4_skint.c:390,414) when
+    // min(m,d) >= 1000; leave the library stream where the reference leaves it.
+    if (hqrrp_stream) rng_hqrrp_advance(64 + 10, m);
+    inf.t_host_hash_ms = hash_ms;
+    inf.kernel_launches = launches_since_reset();
+    if (info) *info = inf;
+}
+
 }  // namespace skl
 
 using namespace skl;
@@ -575,6 +854,18 @@ skl_status skl_sparse_solve_device(const skl_csc* A, const double* b, double* x,
                                    const skl_opts* opts, skl_info* info)
 {
     return guarded([&] { sparse_solve_common(A, b, x, opts, info, false); });
+}
+
+skl_status skl_dense_solve(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
+                           double* x, const skl_opts* opts, skl_info* info)
+{
+    return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, true); });
+}
+
+skl_status skl_dense_solve_device(const double* A, int64_t lda, int64_t n, int64_t d,
+                                  const double* b, double* x, const skl_opts* opts, skl_info* info)
+{
+    return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, false); });
 }
 
 void skl_finalize(void) { release_all_contexts(); }

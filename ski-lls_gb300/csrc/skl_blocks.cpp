@@ -3,7 +3,9 @@
 // isolation against the reference's function of the same role.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <functional>
+#include <type_traits>
 #include <vector>
 
 #include "skl_internal.hpp"
@@ -142,6 +144,71 @@ static void trsv_block(const double* R, int64_t ld, int64_t r, char trans, doubl
     SKL_CUDA(cudaStreamSynchronize(st));
 }
 
+template <typename T>
+static void dht_block(const double* A, int64_t lda, int64_t n, int64_t d, const double* D,
+                      int64_t N, double* Y)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const size_t scr = dht_scratch_bytes(N, std::is_same<T, float>::value ? SKL_PREC_MIXED : SKL_PREC_FP64);
+    Sizer S;
+    S.add<double>(n * d); S.add<double>(n); S.add<double>(N * d); S.add<char>((int64_t)scr);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    double* Ad = C.arena.alloc<double>(n * d);
+    double* Dd = C.arena.alloc<double>(n);
+    double* Yd = C.arena.alloc<double>(N * d);
+    void* work = C.arena.take(scr);
+    SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), d,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(Dd, D, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    dht_hash<T>(Ad, n, n, d, Dd, N, nullptr, nullptr, 1, 0, (T*)nullptr, 0, Yd, N, work, scr, st);
+    SKL_CUDA(cudaMemcpyAsync(Y, Yd, N * d * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
+template <typename T>
+static void sketch_dense_block(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
+                               const double* D, int64_t N, int64_t m, int64_t k,
+                               const int64_t* rows, const double* vals, double* SA, double* Sb)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const size_t scr = std::max(dht_scratch_bytes(N, SKL_PREC_FP64),
+                                build_buckets_scratch_ints(m, N * k) * sizeof(int));
+    Sizer S;
+    S.add<double>(n * d); S.add<double>(n); S.add<double>(n); S.add<unsigned>(N * k);
+    S.add<int>(m + 1); S.add<unsigned>(N * k); S.add<T>(m * d); S.add<double>(m);
+    S.add<char>((int64_t)scr);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    double* Ad = C.arena.alloc<double>(n * d);
+    double* bd = C.arena.alloc<double>(n);
+    double* Dd = C.arena.alloc<double>(n);
+    unsigned* hidx = C.arena.alloc<unsigned>(N * k);
+    int* bptr = C.arena.alloc<int>(m + 1);
+    unsigned* bent = C.arena.alloc<unsigned>(N * k);
+    T* SAd = C.arena.alloc<T>(m * d);
+    double* Sbd = C.arena.alloc<double>(m);
+    void* work = C.arena.take(scr);
+    std::vector<uint32_t> h((size_t)(N * k));
+    for (int64_t q = 0; q < N * k; ++q) {
+        if (rows[q] < 0 || rows[q] >= m) fail(SKL_ERR_INVALID, "hash row out of range");
+        h[(size_t)q] = (uint32_t)rows[q] | (vals[q] < 0 ? 0x80000000u : 0u);
+    }
+    SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), d,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(Dd, D, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(hidx, h.data(), N * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    build_buckets(hidx, N, (int)k, m, bptr, bent, (int*)work, st);
+    dht_hash<T>(Ad, n, n, d, Dd, N, bptr, bent, (int)k, m, SAd, m, nullptr, 0, work, scr, st);
+    dht_hash_rhs(bd, n, Dd, N, bptr, bent, (int)k, m, Sbd, work, scr, st);
+    from_device_as<T>(SAd, m, d, m, SA, m, st);
+    SKL_CUDA(cudaMemcpyAsync(Sb, Sbd, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
 }  // namespace skl
 
 using namespace skl;
@@ -178,6 +245,34 @@ skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, in
         if (!R || !x || r <= 0 || ld < r) fail(SKL_ERR_INVALID, "skl_trsv_upper: bad argument");
         if (precision == SKL_PREC_FP64) trsv_block<double>(R, ld, r, trans, x);
         else trsv_block<float>(R, ld, r, trans, x);
+    });
+}
+
+skl_status skl_dht(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
+                   int precision, double* Y)
+{
+    return guard([&] {
+        if (!A || !D || !Y || n <= 0 || d <= 0 || lda < n || N < n)
+            fail(SKL_ERR_INVALID, "skl_dht: bad argument");
+        if (precision == SKL_PREC_FP64) dht_block<double>(A, lda, n, d, D, N, Y);
+        else dht_block<float>(A, lda, n, d, D, N, Y);
+    });
+}
+
+int64_t skl_dht_length(int64_t n, int wisdom) { return dht_length(n, wisdom); }
+
+skl_status skl_sketch_dense(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
+                            const double* D, int64_t N, int64_t m, int64_t k, const int64_t* rows,
+                            const double* vals, int precision, double* SA, double* Sb)
+{
+    return guard([&] {
+        if (!A || !b || !D || !rows || !vals || !SA || !Sb || n <= 0 || d <= 0 || lda < n ||
+            N < n || m <= 0 || k < 1)
+            fail(SKL_ERR_INVALID, "skl_sketch_dense: bad argument");
+        if (precision == SKL_PREC_FP64)
+            sketch_dense_block<double>(A, lda, n, d, b, D, N, m, k, rows, vals, SA, Sb);
+        else
+            sketch_dense_block<float>(A, lda, n, d, b, D, N, m, k, rows, vals, SA, Sb);
     });
 }
 

@@ -103,17 +103,22 @@ void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, in
                    double* colnorm, double* colscale, cudaStream_t st);
 void sketch_rhs(const int* bptr, const unsigned* bent, int64_t m, int k, const double* b,
                 double* Sb, cudaStream_t st);
-// Dense path: DHT of D*A (n x d, lda) padded to N, hashed into SA (m x d).
-template <typename T>
-void sketch_dense(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
-                  const int* bptr, const unsigned* bent, int k, int64_t m, T* SA, int64_t ld,
-                  double* Y_scratch, double* colnorm, cudaStream_t st);
-void dht_columns(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
-                 double* Y, int64_t ldy, cudaStream_t st);
-void sketch_dense_rhs(const double* b, int64_t n, const double* D, int64_t N, const int* bptr,
-                      const unsigned* bent, int k, int64_t m, double* Sb, double* y_scratch,
-                      cudaStream_t st);
+// ----------------------------------------------------------- k_dense.cu --
+// Dense path: Y = DHT_N(D*A/sqrt(N)) column by column (n x d, lda; zero padded
+// to N), hashed into SA (m x d, ld) through S's buckets with the net factor
+// (1/sqrt(k))^2; optionally Y itself to Yout (N x d, ldy).  FP64 columns use
+// `scratch` (dht_scratch_bytes).
 int64_t dht_length(int64_t n, int wisdom);
+size_t dht_scratch_bytes(int64_t N, int precision);
+template <typename T>
+void dht_hash(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
+              const int* bptr, const unsigned* bent, int k, int64_t m, T* SA, int64_t ld,
+              double* Yout, int64_t ldy, void* scratch, size_t scratch_bytes, cudaStream_t st);
+void dht_hash_rhs(const double* b, int64_t n, const double* D, int64_t N, const int* bptr,
+                  const unsigned* bent, int k, int64_t m, double* Sb, void* scratch,
+                  size_t scratch_bytes, cudaStream_t st);
+void fro_partials(const double* A, int64_t lda, int64_t n, int64_t d, double* out512,
+                  cudaStream_t st);
 
 // -------------------------------------------------------------- k_qr.cu --
 template <typename T>
@@ -122,9 +127,13 @@ size_t cpqr_workspace_bytes(int64_t m, int64_t d);
 // 0-based column permutation, tau (min(m,d)).  If c != nullptr, c (m
 // entries, FP64) is overwritten with Q^T c.  pivoting = 0 gives an unpivoted
 // blocked Householder QR (the _noCPQR path).
+// qr_prof (optional, host array of kQrProfSlots): summed CUDA-event ms of the
+// QR sub-steps: 0 sample QRP, 1 column moves, 2 panel, 3 Q^T c, 4 W = V^T A,
+// 5 Z = T^T W, 6 A -= V Z, 7 Y/G downdate, 8 initial sample Y = G A.
+constexpr int kQrProfSlots = 9;
 template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
-          unsigned* status, cudaStream_t st, double* c, int pivoting);
+          unsigned* status, cudaStream_t st, double* c, int pivoting, double* qr_prof = nullptr);
 
 // ----------------------------------------------------------- k_trinv.cu --
 // M = inv(R11 + perturb*I) for the r x r upper triangle of R (ld); M is r x r
@@ -193,6 +202,9 @@ void rng_srand(uint32_t seed);
 void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx);
 // n random signs (+-1) as in gen_scaled_rand_signs (dense_helpers.cpp:7-16).
 void gen_signs(int64_t n, double* D);
+// Leaves the library stream where HQRRP leaves the C library's: srand(12),
+// then the rand() calls of Marsaglia's polar method for rows*cols normals.
+void rng_hqrrp_advance(int64_t rows, int64_t cols);
 void rng_lock();
 void rng_unlock();
 

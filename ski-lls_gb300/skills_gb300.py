@@ -25,7 +25,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "lib", "libskills_gb300.so")
+LIB_PATH = os.environ.get("SKILLS_LIB", os.path.join(_HERE, "lib", "libskills_gb300.so"))
 
 SKL_OK = 0
 SKL_ERR_INVALID = 1
@@ -76,13 +76,13 @@ class SklInfo(ctypes.Structure):
                 ("t_qr_ms", ctypes.c_double), ("t_precond_ms", ctypes.c_double),
                 ("t_lsqr_ms", ctypes.c_double), ("t_host_hash_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("prof_ms", ctypes.c_double * 4),
-                ("prof_launches", ctypes.c_int64 * 4)]
+                ("prof_launches", ctypes.c_int64 * 4), ("qr_prof_ms", ctypes.c_double * 9)]
 
     def as_dict(self):
         out = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            out[name] = list(v) if name.startswith("prof_") else v
+            out[name] = list(v) if isinstance(v, ctypes.Array) else v
         return out
 
 
@@ -107,8 +107,6 @@ def lib():
                           ctypes.POINTER(SklInfo)]
             f.restype = ctypes.c_int
         for name in ("skl_dense_solve", "skl_dense_solve_device"):
-            if not hasattr(L, name):
-                continue
             f = getattr(L, name)
             f.argtypes = [vp, i64, i64, i64, vp, vp, ctypes.POINTER(SklOpts),
                           ctypes.POINTER(SklInfo)]
@@ -118,15 +116,13 @@ def lib():
         L.skl_sketch_sparse.argtypes = [ctypes.POINTER(SklCsc), vp, i64, i64, vp, vp, ctypes.c_int,
                                         ctypes.c_int, vp, vp]
         L.skl_sketch_sparse.restype = ctypes.c_int
-        if hasattr(L, "skl_dht"):
-            L.skl_dht.argtypes = [vp, i64, i64, i64, vp, i64, vp]
-        if hasattr(L, "skl_dht"):
-            L.skl_dht.restype = ctypes.c_int
-        if hasattr(L, "skl_sketch_dense"):
-            L.skl_sketch_dense.argtypes = [vp, i64, i64, i64, vp, vp, i64, i64, i64, vp, vp,
+        L.skl_dht.argtypes = [vp, i64, i64, i64, vp, i64, ctypes.c_int, vp]
+        L.skl_dht.restype = ctypes.c_int
+        L.skl_dht_length.argtypes = [i64, ctypes.c_int]
+        L.skl_dht_length.restype = i64
+        L.skl_sketch_dense.argtypes = [vp, i64, i64, i64, vp, vp, i64, i64, i64, vp, vp,
                                        ctypes.c_int, vp, vp]
-        if hasattr(L, "skl_sketch_dense"):
-            L.skl_sketch_dense.restype = ctypes.c_int
+        L.skl_sketch_dense.restype = ctypes.c_int
         L.skl_cpqr.argtypes = [vp, i64, i64, ctypes.c_int, vp, vp]
         L.skl_cpqr.restype = ctypes.c_int
         L.skl_trsv_upper.argtypes = [vp, i64, i64, ctypes.c_char, ctypes.c_int, vp]
@@ -311,15 +307,20 @@ def trsv_upper(R, x, trans="n", precision="mixed"):
     return xx
 
 
-def dht(A, D, N=None):
+def dht_length(n, wisdom=0):
+    return int(lib().skl_dht_length(n, wisdom))
+
+
+def dht(A, D, N=None, precision="mixed"):
+    """Y = DHT_N(D*A/sqrt(N)) column-wise (zero padded to N rows) on the GPU."""
     A = np.asfortranarray(A, dtype=np.float64)
     if A.ndim == 1:
         A = A[:, None]
     n, d = A.shape
-    N = n if N is None else N
+    N = dht_length(n) if N is None else N
     Y = np.zeros((N, d), dtype=np.float64, order="F")
     D = np.ascontiguousarray(D, dtype=np.float64)
-    _check(lib().skl_dht(_ptr(A), max(n, 1), n, d, _ptr(D), N, _ptr(Y)))
+    _check(lib().skl_dht(_ptr(A), max(n, 1), n, d, _ptr(D), N, PREC[precision], _ptr(Y)))
     return Y
 
 
