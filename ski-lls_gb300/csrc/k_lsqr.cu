@@ -848,6 +848,28 @@ LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t m
     return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
 }
 
+// Final assembly x_full[cols[i]] = colscale[cols[i]] * (M y)[i] with FP64
+// accumulation (M upcast exactly): one product per solve, so the solution is
+// formed at FP64 accuracy even on the mixed path.
+template <typename MT>
+__global__ void __launch_bounds__(kTriThreads)
+k_tri_n_f64acc(const MT* __restrict__ Mr, int64_t ldm, int r, const double* __restrict__ y,
+               const int* __restrict__ cols, const double* __restrict__ colscale,
+               double* __restrict__ xfull)
+{
+    __shared__ double red[kTriThreads / 32];
+    for (int i = blockIdx.x; i < r; i += gridDim.x) {
+        const MT* row = Mr + (int64_t)i * ldm;
+        double acc = 0.0;
+        for (int j = i + threadIdx.x; j < r; j += blockDim.x) acc = fma((double)row[j], y[j], acc);
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) {
+            const int c = cols[i];
+            xfull[c] = colscale[c] * acc;
+        }
+    }
+}
+
 // x_full[cols[i]] = colscale[cols[i]] * (M yv)[i] (FP64 output), other entries untouched.
 __global__ void k_split_vec(const double* __restrict__ x, int n, float2* __restrict__ out)
 {
@@ -861,17 +883,14 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
                    cudaStream_t st)
 {
     if (P.r <= 0) return;
-    const unsigned gt = tri_blocks(P.r);
-    if (P.precision == SKL_PREC_MIXED) {
-        float2* ys = (float2*)scratch;
-        k_split_vec<<<(unsigned)((P.r + 255) / 256), 256, 0, st>>>(yv, (int)P.r, ys);
-        k_tri_n<true><<<gt, kTriThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, ys, P.cols,
-                                                 P.colscale, nullptr, nullptr, 1, xfull);
-        SKL_LAUNCHED();
-    } else {
-        k_tri_n<false><<<gt, kTriThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv, P.cols,
-                                                  P.colscale, nullptr, nullptr, 1, xfull);
-    }
+    (void)scratch;
+    const unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
+    if (P.precision == SKL_PREC_MIXED)
+        k_tri_n_f64acc<float><<<g, kTriThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, yv,
+                                                         P.cols, P.colscale, xfull);
+    else
+        k_tri_n_f64acc<double><<<g, kTriThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv,
+                                                          P.cols, P.colscale, xfull);
     SKL_LAUNCHED();
 }
 
