@@ -29,6 +29,9 @@
 // src/ls_dense_hashing_blendenpik.cpp:70-76).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -268,45 +271,45 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
 __global__ void k_perm_plan(const int* __restrict__ sel, int b, int* __restrict__ plan_src,
                             int* __restrict__ plan_dst, int* __restrict__ plan_n)
 {
+    // one warp: lanes own positions t and t+32 (b <= 64)
+    __shared__ int s_sel[kMaxNb];
     __shared__ int in_low[kMaxNb];
-    __shared__ int high_sel[kMaxNb];
-    __shared__ int nhigh;
-    const int t = threadIdx.x;
-    if (t < kMaxNb) in_low[t] = 0;
-    if (t == 0) nhigh = 0;
-    __syncthreads();
-    if (t < b) {
-        int s = sel[t];
-        if (s < b) in_low[s] = 1;
+    const int lane = threadIdx.x;
+    for (int t = lane; t < kMaxNb; t += 32) {
+        s_sel[t] = t < b ? sel[t] : -1;
+        in_low[t] = 0;
     }
-    __syncthreads();
-    if (t == 0) {
-        // deterministic serial pass over <= 64 entries
-        int nh = 0;
-        for (int q = 0; q < b; ++q) if (sel[q] >= b) high_sel[nh++] = sel[q];
-        // sort vacated positions ascending (insertion sort, <= 64)
-        for (int a = 1; a < nh; ++a) {
-            int x = high_sel[a], c = a - 1;
-            while (c >= 0 && high_sel[c] > x) { high_sel[c + 1] = high_sel[c]; --c; }
-            high_sel[c + 1] = x;
-        }
-        nhigh = nh;
-        int n = 0;
-        for (int q = 0; q < b; ++q) {           // selected -> front
-            plan_src[n] = sel[q];
-            plan_dst[n] = q;
-            ++n;
-        }
-        int h = 0;
-        for (int pos = 0; pos < b; ++pos) {      // displaced -> vacated
-            if (!in_low[pos]) {
-                plan_src[n] = pos;
-                plan_dst[n] = high_sel[h++];
-                ++n;
+    __syncwarp();
+    for (int t = lane; t < b; t += 32)
+        if (s_sel[t] < b) in_low[s_sel[t]] = 1;
+    __syncwarp();
+    // selected columns go to the front in selection order
+    for (int t = lane; t < b; t += 32) {
+        plan_src[t] = s_sel[t];
+        plan_dst[t] = t;
+    }
+    // displaced low positions (not selected), in increasing order, fill the
+    // vacated high positions (selected with index >= b) in increasing order
+    int n_extra = 0;
+    for (int t = lane; t < b; t += 32) {
+        const int hs = s_sel[t];
+        if (hs >= b) {
+            // rank of hs among the high selections
+            int rk = 0;
+            for (int u = 0; u < b; ++u) rk += (s_sel[u] >= b && s_sel[u] < hs) ? 1 : 0;
+            // the rk-th displaced low position
+            int cnt = -1, pos = 0;
+            for (pos = 0; pos < b; ++pos) {
+                if (!in_low[pos]) ++cnt;
+                if (cnt == rk) break;
             }
+            plan_src[b + rk] = pos;
+            plan_dst[b + rk] = hs;
         }
-        *plan_n = n;
+        n_extra += (hs >= b) ? 1 : 0;
     }
+    for (int o = 16; o > 0; o >>= 1) n_extra += __shfl_xor_sync(0xffffffffu, n_extra, o);
+    if (lane == 0) *plan_n = b + n_extra;
 }
 
 // Copy the planned source columns of X (rows x cols, ld) into tmp, then
@@ -403,8 +406,10 @@ template <typename T>
 __global__ void __launch_bounds__(kQrThreads)
 k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restrict__ tau_out,
         T* __restrict__ Tout, int ldt, T* __restrict__ V, int64_t ldv, int* __restrict__ jpvt,
-        T* __restrict__ Y, int ldy, int nbp, int pivot_panel)
+        T* __restrict__ Y, int ldy, int nbp, int pivot_panel, const int* __restrict__ chol_fail)
 {
+    // runs only when the CholeskyQR2 panel (if any) declined this panel
+    if (chol_fail && *chol_fail == 0) return;
     using V4 = typename Vec4T<T>::type;
     constexpr int VN = Vec4T<T>::n;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -645,16 +650,270 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
     }
 }
 
+
+// --------------------------------------------------- CholeskyQR2 panel ----
+// Unpivoted QR of the panel P = A(j0:m, j0:j0+b) (column order from the
+// sample QRP) in the cluster's shared memory by CholeskyQR2, then Householder
+// reconstruction by the modified LU of Ballard, Demmel, Grigori, Jacquelin,
+// Knight and Nguyen ("Reconstructing Householder vectors from TSQR", 2015):
+//   Q1 - S = L U (no pivoting, S_kk = -sign of the k-th pivot),
+//   V = [L; Q2 U^{-1}],  T = -U S L^{-T},  R_H = S R,
+// so I - V T V^T has Q S as its first b columns and the trailing update and
+// the sample downdate use (V, T) exactly as with the column-by-column panel.
+// A Cholesky pivot below 32 eps of its column's mass (kappa(P) too large for
+// CholeskyQR2, e.g. dependent columns) sets *fail = 1 and leaves A untouched;
+// the pivoted panel kernel launched next then factors the panel instead.
+template <typename T>
+size_t chol_panel_smem_bytes(int R, int b)
+{
+    const size_t ldg = (size_t)b + 1;
+    const int npairs = b * (b + 1) / 2;
+    size_t s = (size_t)R * b * sizeof(T);                  // Ps
+    s += 4 * (size_t)b * ldg * sizeof(T);                  // G/LU, Racc, Rinv/T, Tmp
+    s += (size_t)npairs * sizeof(T);                       // flat Gram pairs
+    s += (size_t)4 * b * sizeof(T);                        // signs, masses
+    s += (size_t)((npairs + kCluster - 1) / kCluster + 8) * sizeof(T);   // slice
+    return s + 512;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kQrThreads)
+k_panel_chol(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restrict__ tau_out,
+             T* __restrict__ Tout, int ldt, T* __restrict__ V, int64_t ldv, int* __restrict__ fail)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int LDG = b + 1;
+    const unsigned crank = cluster_ctarank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int r0 = (int)crank * R;
+    const int nr = max(0, min(R, M - r0));
+    const int npairs = b * (b + 1) / 2;
+    const int per = (npairs + kCluster - 1) / kCluster;
+    T* Ps = (T*)smem_raw;                        // [b][R]
+    T* G = Ps + (size_t)R * b;                   // Gram -> Cholesky factor; later the LU (L below, U above)
+    T* Racc = G + b * LDG;                       // accumulated R (upper)
+    T* Rinv = Racc + b * LDG;                    // Rc^{-1}; staging; later T
+    T* Tmp = Rinv + b * LDG;                     // L^{-1}, then U^{-1}
+    T* flat = Tmp + b * LDG;                     // Gram pairs (a <= c), this CTA's partial
+    T* Sg = flat + npairs;                       // signs S (CTA 0) and the copy of S (all)
+    T* mass = Sg + 2 * b;                        // ||P(:,k)||^2 before each pass
+    T* slice = mass + 2 * b;                     // this CTA's reduced slice of the Gram
+    __shared__ int s_bad;
+    const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
+
+    for (int e = tid; e < R * b; e += kQrThreads) {
+        int lr = e % R, c = e / R;
+        Ps[lr + (size_t)c * R] = (lr < nr) ? A[(int64_t)(j0 + r0 + lr) + (int64_t)(j0 + c) * ld] : T(0);
+    }
+    if (tid == 0) s_bad = 0;
+    for (int e = tid; e < b * LDG; e += kQrThreads) Racc[e] = T(0);
+    __syncthreads();
+    for (int a = tid; a < b; a += kQrThreads) Racc[a * LDG + a] = T(1);
+
+    for (int pass = 0; pass < 2; ++pass) {
+        // ---- local Gram, pairs (a <= c) in row order of the upper triangle ----
+        for (int q = wid; q < npairs; q += kQrWarps) {
+            int a = 0, rem = q;
+            while (rem >= b - a) { rem -= b - a; ++a; }
+            const int c = a + rem;
+            const T* pa = Ps + (size_t)a * R;
+            const T* pc = Ps + (size_t)c * R;
+            T acc = T(0);
+            for (int lr = lane; lr < nr; lr += 32) acc += pa[lr] * pc[lr];
+            acc = warp_sum(acc);
+            if (lane == 0) flat[q] = acc;
+        }
+        cluster_sync();
+        // reduce-scatter: CTA crank sums pairs [crank*per, crank*per + per)
+        for (int q = (int)crank * per + tid; q < min(npairs, ((int)crank + 1) * per); q += kQrThreads) {
+            T v[kCluster];
+#pragma unroll
+            for (int w = 0; w < kCluster; ++w) v[w] = dsmem_ld(&flat[q], w);
+            T acc = T(0);
+#pragma unroll
+            for (int w = 0; w < kCluster; ++w) acc += v[w];
+            slice[q - (int)crank * per] = acc;
+        }
+        cluster_sync();
+        // all-gather straight into the symmetric G
+        for (int q = tid; q < npairs; q += kQrThreads) {
+            const int owner = q / per;
+            const T g = dsmem_ld(&slice[q - owner * per], owner);
+            int a = 0, rem = q;
+            while (rem >= b - a) { rem -= b - a; ++a; }
+            const int c = a + rem;
+            G[a * LDG + c] = g;
+            G[c * LDG + a] = g;
+            if (a == c) mass[a] = g;
+        }
+        cluster_sync();   // all slices read before they are reused
+        // ---- Cholesky G = Rc^T Rc (upper Rc in G's upper triangle) ----
+        for (int k = 0; k < b; ++k) {
+            if (tid == 0) {
+                const T gk = G[k * LDG + k];
+                if (!(gk > T(32) * eps * mass[k]) || !(mass[k] > T(0))) s_bad = 1;
+                G[k * LDG + k] = gk > T(0) ? t_sqrt(gk) : T(1);
+            }
+            __syncthreads();
+            const T idk = T(1) / G[k * LDG + k];
+            for (int c = k + 1 + tid; c < b; c += kQrThreads) G[k * LDG + c] *= idk;
+            __syncthreads();
+            const int rem_n = b - k - 1;
+            for (int e = tid; e < rem_n * rem_n; e += kQrThreads) {
+                const int i = k + 1 + e / rem_n, c = k + 1 + e % rem_n;
+                if (c >= i) G[i * LDG + c] -= G[k * LDG + i] * G[k * LDG + c];
+            }
+            __syncthreads();
+        }
+        if (s_bad) break;   // uniform: every CTA computed the same G
+        // ---- Rinv = Rc^{-1} (upper), column per thread ----
+        for (int c = tid; c < b; c += kQrThreads) {
+            Rinv[c * LDG + c] = T(1) / G[c * LDG + c];
+            for (int i = c - 1; i >= 0; --i) {
+                T acc = T(0);
+                for (int kk = i + 1; kk <= c; ++kk) acc += G[i * LDG + kk] * Rinv[kk * LDG + c];
+                Rinv[i * LDG + c] = -acc / G[i * LDG + i];
+            }
+            for (int i = c + 1; i < b; ++i) Rinv[i * LDG + c] = T(0);
+        }
+        __syncthreads();
+        // ---- P <- P Rc^{-1}: thread per local row ----
+        for (int lr = tid; lr < nr; lr += kQrThreads) {
+            T row[kMaxNb];
+            for (int a = 0; a < b; ++a) row[a] = Ps[lr + (size_t)a * R];
+            for (int c = b - 1; c >= 0; --c) {
+                T acc = T(0);
+                for (int a = 0; a <= c; ++a) acc += row[a] * Rinv[a * LDG + c];
+                Ps[lr + (size_t)c * R] = acc;
+            }
+        }
+        __syncthreads();
+        // ---- Racc <- Rc * Racc (staged in Rinv, now free) ----
+        for (int e = tid; e < b * b; e += kQrThreads) {
+            const int i = e / b, c = e % b;
+            T acc = T(0);
+            if (i <= c)
+                for (int kk = i; kk <= c; ++kk) acc += G[i * LDG + kk] * Racc[kk * LDG + c];
+            Rinv[i * LDG + c] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < b * b; e += kQrThreads) {
+            const int i = e / b, c = e % b;
+            Racc[i * LDG + c] = Rinv[i * LDG + c];
+        }
+        __syncthreads();
+    }
+    if (s_bad) {
+        // every CTA reached the same verdict from the same data: A untouched
+        if (crank == 0 && tid == 0) *fail = 1;
+        cluster_sync();
+        return;
+    }
+    // ---- modified LU of Q1 - S on CTA 0 (global panel rows 0..b-1, R >= b) ----
+    if (crank == 0) {
+        for (int e = tid; e < b * b; e += kQrThreads) {
+            const int i = e % b, c = e / b;
+            G[i * LDG + c] = Ps[i + (size_t)c * R];
+        }
+        __syncthreads();
+        for (int k = 0; k < b; ++k) {
+            if (tid == 0) {
+                const T pv = G[k * LDG + k];
+                const T sk = pv >= T(0) ? T(-1) : T(1);   // S_kk = -sign(pivot)
+                Sg[k] = sk;
+                G[k * LDG + k] = pv - sk;
+            }
+            __syncthreads();
+            const T ukk = G[k * LDG + k];
+            for (int i = k + 1 + tid; i < b; i += kQrThreads) G[i * LDG + k] /= ukk;
+            __syncthreads();
+            const int rem_n = b - k - 1;
+            for (int e = tid; e < rem_n * rem_n; e += kQrThreads) {
+                const int i = k + 1 + e / rem_n, c = k + 1 + e % rem_n;
+                G[i * LDG + c] -= G[i * LDG + k] * G[k * LDG + c];
+            }
+            __syncthreads();
+        }
+        // Tmp = L^{-1} (unit lower), column per thread
+        for (int c = tid; c < b; c += kQrThreads) {
+            for (int i = 0; i < b; ++i) {
+                T acc = (i == c) ? T(1) : T(0);
+                for (int kk = c; kk < i; ++kk) acc -= G[i * LDG + kk] * Tmp[kk * LDG + c];
+                Tmp[i * LDG + c] = (i < c) ? T(0) : acc;
+            }
+        }
+        __syncthreads();
+        // T = -U S L^{-T} into Rinv:  T[i][c] = -sum_{k=i..c} U[i][k] S_k L^{-1}[c][k]
+        for (int e = tid; e < b * b; e += kQrThreads) {
+            const int i = e / b, c = e % b;
+            T acc = T(0);
+            if (i <= c)
+                for (int kk = i; kk <= c; ++kk) acc += G[i * LDG + kk] * Sg[kk] * Tmp[c * LDG + kk];
+            Rinv[i * LDG + c] = -acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < b * b; e += kQrThreads) {
+            const int i = e % b, c = e / b;
+            Tout[i + (int64_t)c * ldt] = (i <= c) ? Rinv[i * LDG + c] : T(0);
+            if (i == c) tau_out[j0 + i] = Rinv[i * LDG + i];
+        }
+        __syncthreads();
+        // Tmp = U^{-1} (upper), column per thread
+        for (int c = tid; c < b; c += kQrThreads) {
+            Tmp[c * LDG + c] = T(1) / G[c * LDG + c];
+            for (int i = c - 1; i >= 0; --i) {
+                T acc = T(0);
+                for (int kk = i + 1; kk <= c; ++kk) acc += G[i * LDG + kk] * Tmp[kk * LDG + c];
+                Tmp[i * LDG + c] = -acc / G[i * LDG + i];
+            }
+            for (int i = c + 1; i < b; ++i) Tmp[i * LDG + c] = T(0);
+        }
+    }
+    cluster_sync();   // CTA 0's S, L (in G) and U^{-1} (in Tmp) published
+    // every CTA fetches U^{-1} into Rinv and S into Sg[b..2b)
+    for (int e = tid; e < b * b; e += kQrThreads) {
+        const int i = e / b, c = e % b;
+        Rinv[i * LDG + c] = (i <= c) ? dsmem_ld(&Tmp[i * LDG + c], 0) : T(0);
+    }
+    for (int k = tid; k < b; k += kQrThreads) Sg[b + k] = dsmem_ld(&Sg[k], 0);
+    __syncthreads();
+    // ---- write back: R_H = S Racc above the diagonal (CTA 0), V below ----
+    for (int lr = tid; lr < nr; lr += kQrThreads) {
+        const int g = r0 + lr;
+        T row[kMaxNb];
+        for (int a = 0; a < b; ++a) row[a] = Ps[lr + (size_t)a * R];
+        for (int c = 0; c < b; ++c) {
+            T out, vv;
+            if (g < b) {
+                const T l = (g > c) ? G[g * LDG + c] : T(0);   // CTA 0 holds L
+                out = (g <= c) ? Sg[b + g] * Racc[g * LDG + c] : l;
+                vv = (g > c) ? l : (g == c ? T(1) : T(0));
+            } else {
+                T acc = T(0);
+                for (int a = 0; a <= c; ++a) acc += row[a] * Rinv[a * LDG + c];
+                out = acc;
+                vv = acc;
+            }
+            A[(int64_t)(j0 + g) + (int64_t)(j0 + c) * ld] = out;
+            V[(int64_t)g + (int64_t)c * ldv] = vv;
+        }
+    }
+    if (crank == 0 && tid == 0) *fail = 0;
+    cluster_sync();   // CTA 0's shared memory stays alive until every CTA read it
+}
+
 // ------------------------------------------------- Q^T c for one panel --
-// c(j0:m) <- (I - V T^T V^T) c(j0:m), FP64 accumulation.
+// c(j0:m) <- (I - V T^T V^T) c(j0:m), FP64 accumulation.  w = V^T c: one
+// block per column of V; the update: one warp per 32 rows, z = T^T w in smem.
 template <typename T>
 __global__ void k_qt_w(const T* __restrict__ V, int64_t ldv, int M, int b,
                        const double* __restrict__ c, double* __restrict__ w)
 {
-    __shared__ double red[kQrWarps];
+    __shared__ double red[32];
     const int a = blockIdx.x;
+    const T* va = V + (int64_t)a * ldv;
     double acc = 0.0;
-    for (int r = threadIdx.x; r < M; r += blockDim.x) acc = fma((double)V[r + (int64_t)a * ldv], c[r], acc);
+    for (int r = a + threadIdx.x; r < M; r += blockDim.x) acc = fma((double)va[r], c[r], acc);
     acc = block_sum(acc, red);
     if (threadIdx.x == 0) w[a] = acc;
 }
@@ -665,9 +924,8 @@ __global__ void k_qt_update(const T* __restrict__ V, int64_t ldv, int M, int b,
                             double* __restrict__ c)
 {
     __shared__ double z[kMaxNb];
-    // z = T^T w
     if (threadIdx.x < b) {
-        int i = threadIdx.x;
+        const int i = threadIdx.x;
         double acc = 0.0;
         for (int a = 0; a <= i; ++a) acc = fma((double)Tm[a + (int64_t)i * ldt], w[a], acc);
         z[i] = acc;
@@ -675,7 +933,8 @@ __global__ void k_qt_update(const T* __restrict__ V, int64_t ldv, int M, int b,
     __syncthreads();
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < M; r += gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int a = 0; a < b; ++a) acc = fma((double)V[r + (int64_t)a * ldv], z[a], acc);
+        const int amax = min(b, r + 1);   // V is zero above its diagonal
+        for (int a = 0; a < amax; ++a) acc = fma((double)V[r + (int64_t)a * ldv], z[a], acc);
         c[r] -= acc;
     }
 }
@@ -696,6 +955,23 @@ __global__ void k_iota_int(int* v, int n)
 }
 
 // ------------------------------------------------------------ host side --
+// Panel method: CholeskyQR2 + Householder reconstruction by default on the
+// FP64 path, the column-by-column pivoted panel on the FP32 path;
+// SKILLS_QR_PANEL=chol|pivoted overrides.
+template <typename T>
+static bool qr_chol_enabled()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("SKILLS_QR_PANEL");
+        if (e && std::string(e) == "pivoted") v = 0;
+        else if (e && std::string(e) == "chol") v = 1;
+        else v = 2;
+    }
+    if (v == 2) return std::is_same<T, double>::value;
+    return v == 1;
+}
+
 struct QrPlan {
     int nb, nbp, R;
 };
@@ -724,7 +1000,7 @@ static QrPlan qr_plan(int64_t m, int64_t d)
 template <typename T>
 struct QrBuffers {
     T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *tmp;
-    int *sel, *plan_src, *plan_dst, *plan_n;
+    int *sel, *plan_src, *plan_dst, *plan_n, *chol_fail;
     double *qw;
     int64_t part_cap, tmp_rows;
 };
@@ -759,6 +1035,7 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.plan_src = (int*)take(2 * kMaxNb * sizeof(int));
     B.plan_dst = (int*)take(2 * kMaxNb * sizeof(int));
     B.plan_n = (int*)take(sizeof(int));
+    B.chol_fail = (int*)take(sizeof(int));
     B.qw = (double*)take(kMaxNb * sizeof(double));
     if (total) *total = off;
     return B;
@@ -860,6 +1137,10 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     }
     const size_t ysm_max = YqrpSmem<T>::bytes(nbp, (int)((d + kCluster - 1) / kCluster));
     const size_t psm = panel_smem_bytes<T>(p.R, nb);
+    const size_t csm = chol_panel_smem_bytes<T>(p.R, nb);
+    // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
+    // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
+    const bool use_chol = pivoting && p.R >= nb && csm <= 226 * 1024 && qr_chol_enabled<T>();
     for (int64_t j = 0; j < mn; j += nb) {
         const int b = (int)std::min<int64_t>(nb, std::min<int64_t>(d - j, m - j));
         const bool last = (j + nb >= m) || (j + nb >= d);
@@ -877,7 +1158,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             tm.end(0, t0);
             trace_phase(st, "qr: yqrp");
             t0 = tm.begin();
-            k_perm_plan<<<1, kMaxNb, 0, st>>>(B.sel, b, B.plan_src, B.plan_dst, B.plan_n);
+            k_perm_plan<<<1, 32, 0, st>>>(B.sel, b, B.plan_src, B.plan_dst, B.plan_n);
             SKL_LAUNCHED();
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
             k_perm_gather<T><<<gA, 256, 0, st>>>(A, ld, (int)m, jj, B.plan_src, B.plan_n, B.tmp);
@@ -899,9 +1180,17 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             T* Yp = pivoting ? B.Y : nullptr;
             int ldy = nbp;
             int pp = pivoting ? 1 : 0;
-            void* args[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
-                            &ldv, &jpvt, &Yp, &ldy, &nbpp, &pp};
             cudaEvent_t t0 = tm.begin();
+            const int* cf = nullptr;
+            if (use_chol && !last) {
+                int* failp = B.chol_fail;
+                void* cargs[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
+                                 &ldv, &failp};
+                launch_cluster<T>((const void*)k_panel_chol<T>, dim3(kQrThreads), csm, st, cargs);
+                cf = B.chol_fail;
+            }
+            void* args[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
+                            &ldv, &jpvt, &Yp, &ldy, &nbpp, &pp, (void*)&cf};
             launch_cluster<T>((const void*)k_panel<T>, dim3(kQrThreads), psm, st, args);
             tm.end(2, t0);
             trace_phase(st, "qr: panel");
@@ -909,7 +1198,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         if (c) {
             cudaEvent_t t0 = tm.begin();
             k_qt_w<T><<<b, 256, 0, st>>>(B.V, m, M, b, c + j, B.qw);
-            k_qt_update<T><<<(unsigned)std::min<int64_t>((M + 255) / 256, 256), 256, 0, st>>>(
+            k_qt_update<T><<<(unsigned)std::max<int64_t>(1, (M + 127) / 128), 128, 0, st>>>(
                 B.V, m, M, b, B.Tm, nb, B.qw, c + j);
             SKL_LAUNCHED();
             SKL_LAUNCHED();

@@ -73,22 +73,49 @@ __global__ void k_zero_lower(T* __restrict__ M, int64_t ldm, int r)
 template <typename T>
 size_t trinv_workspace_bytes(int64_t r)
 {
-    return (size_t)r * r * sizeof(T) / 2 + (size_t)kTB * kTB * sizeof(T) + 4096;
+    const size_t a = (size_t)r * r * sizeof(T) / 2 + (size_t)kTB * kTB * sizeof(T);
+    const size_t b = (size_t)((r + 127) / 128) * r * sizeof(double);   // row-sum partials
+    return (a > b ? a : b) + 4096;
 }
 
-// row sums of |upper triangle| -> max, for ||.||_inf
+// ||upper triangle||_inf: row sums of |X| accumulated per (row block, column
+// chunk) tile in fixed order, then the max over rows.  FP64 sums.
+constexpr int kInfRows = 128, kInfCols = 128;
 template <typename T>
-__global__ void k_inf_norm_upper(const T* __restrict__ X, int64_t ld, int r, double* out)
+__global__ void k_inf_rowsum_tiles(const T* __restrict__ X, int64_t ld, int r, double* __restrict__ part)
+{
+    const int i = blockIdx.x * kInfRows + threadIdx.x;
+    const int j0 = blockIdx.y * kInfCols;
+    double s = 0.0;
+    if (i < r) {
+        const int jb = max(i, j0), je = min(r, j0 + kInfCols);
+        for (int j = jb; j < je; ++j) s += fabs((double)X[i + (int64_t)j * ld]);
+    }
+    if (i < r) part[(int64_t)blockIdx.y * r + i] = s;
+}
+
+__global__ void k_inf_rowsum_max(const double* __restrict__ part, int nchunks, int r, double* out)
 {
     __shared__ double red[32];
     double mx = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
         double s = 0.0;
-        for (int j = i; j < r; ++j) s += fabs((double)X[i + (int64_t)j * ld]);
+        for (int q = 0; q < nchunks; ++q) s += part[(int64_t)q * r + i];
         mx = s > mx ? s : mx;
     }
     mx = block_max(mx, red);
     if (threadIdx.x == 0) atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong(mx));
+}
+
+template <typename T>
+static void inf_norm_upper(const T* X, int64_t ld, int64_t r, double* part, double* out, cudaStream_t st)
+{
+    const int nchunks = (int)((r + kInfCols - 1) / kInfCols);
+    dim3 g((unsigned)((r + kInfRows - 1) / kInfRows), nchunks);
+    k_inf_rowsum_tiles<T><<<g, kInfRows, 0, st>>>(X, ld, (int)r, part);
+    k_inf_rowsum_max<<<(unsigned)std::min<int64_t>((r + 255) / 256, 64), 256, 0, st>>>(part, nchunks, (int)r, out);
+    SKL_LAUNCHED();
+    SKL_LAUNCHED();
 }
 
 template <typename T>
@@ -118,11 +145,10 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
     k_zero_lower<T><<<1024, 256, 0, st>>>(M, ldm, (int)r);
     SKL_LAUNCHED();
     cudaMemsetAsync(norms, 0, 2 * sizeof(double), st);
-    unsigned g = (unsigned)std::min<int64_t>((r + 255) / 256, 256);
-    k_inf_norm_upper<T><<<g, 256, 0, st>>>(R, ld, (int)r, norms);
-    k_inf_norm_upper<T><<<g, 256, 0, st>>>(M, ldm, (int)r, norms + 1);
-    SKL_LAUNCHED();
-    SKL_LAUNCHED();
+    // row-sum partials reuse the inverse's scratch (free again here)
+    double* part = (double*)work;
+    inf_norm_upper<T>(R, ld, r, part, norms, st);
+    inf_norm_upper<T>(M, ldm, r, part, norms + 1, st);
 }
 
 // Number of leading diagonal entries with |R_ii| > max(abs_thresh, rel_thresh*|R_00|).
