@@ -170,6 +170,34 @@ skl_status skl_sketch_sparse(const skl_csc* A, const double* b, int64_t m, int64
 skl_status skl_dht(const double* A, int64_t lda, int64_t n, int64_t d, const double* D,
                    int64_t N, int precision, double* Y);
 
+/* skl_dht on device buffers without any device allocation.  No counterpart
+ * in the reference: it exists for callers that cannot let a library allocate
+ * device memory -- a host framework whose caching allocator already owns
+ * (nearly) all of the device, code that must keep a fixed device footprint
+ * known when the library is loaded, and latency-critical loops where a
+ * cudaFree (which synchronises the whole device) would stall other streams.
+ *
+ * A (lda >= n), D (n entries) and Y (ldy >= N, N x d written) are DEVICE
+ * pointers on the current device; the work is enqueued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) and the call returns
+ * without waiting for it.  Results are bit-identical to skl_dht with the same
+ * arguments and precision.
+ *  - Scratch: one static device array of SKL_DHT_NOALLOC_SCRATCH_BYTES per
+ *    device, so N <= SKL_DHT_NOALLOC_MAX_N; a larger N is rejected with
+ *    SKL_ERR_INVALID and a message naming the limit.  Nothing in it needs to
+ *    start at zero.
+ *  - The first call on each device does a one-time set-up (scratch address
+ *    lookup, which loads the module holding it, and kernel loading): make that
+ *    first call before any stream capture begins.
+ *  - All calls on one device share that scratch: calls that may overlap in
+ *    time (different streams or host threads without ordering between them)
+ *    race on it and give wrong results.  Order them (one stream, or events). */
+#define SKL_DHT_NOALLOC_SCRATCH_BYTES (64u << 20)
+#define SKL_DHT_NOALLOC_MAX_N 4194304
+skl_status skl_dht_device_noalloc(const double* A, int64_t lda, int64_t n, int64_t d,
+                                  const double* D, int64_t N, int precision, double* Y,
+                                  int64_t ldy, void* stream);
+
 /* Transform length the dense solver uses for n rows (wisdom as in skl_opts). */
 int64_t skl_dht_length(int64_t n, int wisdom);
 

@@ -407,6 +407,13 @@ static void launch_dht(const double* A, int64_t lda, int64_t n, int64_t d, const
     SKL_LAUNCHED();
 }
 
+void dht_load_kernels()
+{
+    cudaFuncAttributes fa;
+    SKL_CUDA(cudaFuncGetAttributes(&fa, k_dht_hash<float>));
+    SKL_CUDA(cudaFuncGetAttributes(&fa, k_dht_hash<double>));
+}
+
 size_t dht_scratch_bytes(int64_t N, int precision)
 {
     const size_t csz = precision == SKL_PREC_FP64 ? sizeof(double2) : sizeof(float2);

@@ -110,6 +110,8 @@ void sketch_rhs(const int* bptr, const unsigned* bent, int64_t m, int k, const d
 // `scratch` (dht_scratch_bytes).
 int64_t dht_length(int64_t n, int wisdom);
 size_t dht_scratch_bytes(int64_t N, int precision);
+// Load the DHT kernels' module on the current device (one-time set-up).
+void dht_load_kernels();
 template <typename T>
 void dht_hash(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
               const int* bptr, const unsigned* bent, int k, int64_t m, T* SA, int64_t ld,

@@ -118,6 +118,9 @@ def lib():
         L.skl_sketch_sparse.restype = ctypes.c_int
         L.skl_dht.argtypes = [vp, i64, i64, i64, vp, i64, ctypes.c_int, vp]
         L.skl_dht.restype = ctypes.c_int
+        L.skl_dht_device_noalloc.argtypes = [vp, i64, i64, i64, vp, i64, ctypes.c_int, vp, i64,
+                                             vp]
+        L.skl_dht_device_noalloc.restype = ctypes.c_int
         L.skl_dht_length.argtypes = [i64, ctypes.c_int]
         L.skl_dht_length.restype = i64
         L.skl_sketch_dense.argtypes = [vp, i64, i64, i64, vp, vp, i64, i64, i64, vp, vp,
@@ -322,6 +325,14 @@ def dht(A, D, N=None, precision="mixed"):
     D = np.ascontiguousarray(D, dtype=np.float64)
     _check(lib().skl_dht(_ptr(A), max(n, 1), n, d, _ptr(D), N, PREC[precision], _ptr(Y)))
     return Y
+
+
+def dht_device_noalloc(A_ptr, lda, n, d, D_ptr, N, Y_ptr, ldy, precision="mixed", stream=0):
+    """skl_dht on device pointers with static scratch (no device allocation);
+    enqueued on `stream` (a raw cudaStream_t handle, 0 = default stream)."""
+    _check(lib().skl_dht_device_noalloc(ctypes.c_void_p(A_ptr), lda, n, d, ctypes.c_void_p(D_ptr),
+                                        N, PREC[precision], ctypes.c_void_p(Y_ptr), ldy,
+                                        ctypes.c_void_p(stream)))
 
 
 def sketch_dense(A, b, D, N, m, k, rows, vals, precision="mixed"):
