@@ -159,6 +159,7 @@ enum : unsigned {
     kDevErrTimeout = 1u,
     kDevErrBounds = 2u,
     kDevErrNumeric = 4u,
+    kDevErrQrSelect = 8u,   // the sample QRP picked an invalid column (non-finite sketch)
 };
 
 constexpr long long kSpinLimit = 1ll << 24;

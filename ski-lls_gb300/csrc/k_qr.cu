@@ -159,8 +159,12 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         // (a) local argmax (largest norm; ties -> smallest index)
         T bv = T(-1);
         int bi = -1;
-        for (int c = tid; c < ncols; c += kQrThreads)
-            if (!taken[c] && nrm[c] > bv) { bv = nrm[c]; bi = c; }
+        for (int c = tid; c < ncols; c += kQrThreads) {
+            // a NaN norm ranks below every real one but stays selectable, so
+            // a winner always exists while untaken columns remain
+            const T nv = nrm[c] == nrm[c] ? nrm[c] : T(-0.5);
+            if (!taken[c] && nv > bv) { bv = nv; bi = c; }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             T ov = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -268,8 +272,9 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
 // Moves the selected columns (sel, relative to j0) to positions j0..j0+b-1;
 // the columns they displace fill the vacated positions in increasing order.
 // plan: src[t] for t in [0, 2b): dest position dst[t] (relative) <- src.
-__global__ void k_perm_plan(const int* __restrict__ sel, int b, int* __restrict__ plan_src,
-                            int* __restrict__ plan_dst, int* __restrict__ plan_n)
+__global__ void k_perm_plan(const int* __restrict__ sel, int b, int N, int* __restrict__ plan_src,
+                            int* __restrict__ plan_dst, int* __restrict__ plan_n,
+                            unsigned* __restrict__ status)
 {
     // one warp: lanes own positions t and t+32 (b <= 64)
     __shared__ int s_sel[kMaxNb];
@@ -280,6 +285,22 @@ __global__ void k_perm_plan(const int* __restrict__ sel, int b, int* __restrict_
         in_low[t] = 0;
     }
     __syncwarp();
+    // a selection outside [0, N) or a repeated one (only possible after
+    // non-finite values): flag it and leave the columns where they are
+    bool badsel = false;
+    for (int t = lane; t < b; t += 32) {
+        const int v = s_sel[t];
+        bool bad = v < 0 || v >= N;
+        for (int u = 0; u < t; ++u) bad = bad || s_sel[u] == v;
+        badsel = badsel || bad;
+    }
+    if (__any_sync(0xffffffffu, badsel)) {
+        if (lane == 0) {
+            *plan_n = 0;
+            dev_flag(status, kDevErrQrSelect);
+        }
+        return;
+    }
     for (int t = lane; t < b; t += 32)
         if (s_sel[t] < b) in_low[s_sel[t]] = 1;
     __syncwarp();
@@ -653,253 +674,444 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
 
 // --------------------------------------------------- CholeskyQR2 panel ----
 // Unpivoted QR of the panel P = A(j0:m, j0:j0+b) (column order from the
-// sample QRP) in the cluster's shared memory by CholeskyQR2, then Householder
-// reconstruction by the modified LU of Ballard, Demmel, Grigori, Jacquelin,
-// Knight and Nguyen ("Reconstructing Householder vectors from TSQR", 2015):
-//   Q1 - S = L U (no pivoting, S_kk = -sign of the k-th pivot),
-//   V = [L; Q2 U^{-1}],  T = -U S L^{-T},  R_H = S R,
+// sample QRP) by CholeskyQR2, then Householder reconstruction by the
+// modified LU of Ballard, Demmel, Grigori, Jacquelin, Knight and Nguyen
+// ("Reconstructing Householder vectors from TSQR", 2015):
+//   G1 = P^T P = R1^T R1,  Q = P R1^{-1},  G2 = Q^T Q = R2^T R2,
+//   Q1 = Q(0:b,:) R2^{-1},  Q1 - S = L U (no pivoting, S_kk = -sign of pivot),
+//   V = [L; Q(b:,:) W],  W = R2^{-1} U^{-1},  T = -U S L^{-T},  R_H = S R2 R1,
 // so I - V T V^T has Q S as its first b columns and the trailing update and
 // the sample downdate use (V, T) exactly as with the column-by-column panel.
-// A Cholesky pivot below 32 eps of its column's mass (kappa(P) too large for
-// CholeskyQR2, e.g. dependent columns) sets *fail = 1 and leaves A untouched;
-// the pivoted panel kernel launched next then factors the panel instead.
+//
+// The tall products (the two Grams, P R1^{-1}, Q W) are GEMMs over the whole
+// GPU, the panel staying in L2; the b x b algebra runs in one CTA
+// (k_chol_small1/2) with room for the registers its 32-wide warp
+// factorizations need: 2 x 2 blocks of 32, each diagonal block factored by
+// one warp holding it in registers (shuffles, no block barrier), the
+// off-diagonal blocks by register-tiled block products.
+//
+// A Cholesky pivot below 32 eps of its column's mass, or a second Gram
+// farther than 1/2 from the identity (Gershgorin), means kappa(P) is too large
+// for CholeskyQR2: *fail = 1, A is left untouched and the pivoted panel kernel
+// launched next factors the panel instead.
+constexpr int kSmallThreads = 256;
+
+// ---- small dense algebra on b x b (b <= 64) row-major shared-memory blocks --
+// Diagonal 32 x 32 blocks are factored by one warp with the block in
+// registers (lane c holds column c; pivots and multipliers travel by
+// shuffles, no block barrier); off-diagonal blocks are formed with
+// register-tiled block products.  Indices >= n of a 32-block act as identity.
+constexpr int kWB = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Cholesky of the symmetric n x n block A (n <= 32): R (upper, zeros below)
+// to Rw.  A may alias Rw.  Sets *bad when a pivot is below 32 eps times its
+// mass (mass[k], the column's squared norm).  Run by one warp.  Rows stay
+// unnormalised during the elimination (a_ic -= a_ki a_kc / d_k); row k is
+// scaled by 1/sqrt(d_k) at the end, all rows at once.
 template <typename T>
-size_t chol_panel_smem_bytes(int R, int b)
+SKL_DEV void warp_chol32(const T* A, int lda, int n, const T* __restrict__ mass, T eps, T* Rw,
+                         int ldr, int* bad)
 {
-    const size_t ldg = (size_t)b + 1;
-    const int npairs = b * (b + 1) / 2;
-    size_t s = (size_t)R * b * sizeof(T);                  // Ps
-    s += 4 * (size_t)b * ldg * sizeof(T);                  // G/LU, Racc, Rinv/T, Tmp
-    s += (size_t)npairs * sizeof(T);                       // flat Gram pairs
-    s += (size_t)4 * b * sizeof(T);                        // signs, masses
-    s += (size_t)((npairs + kCluster - 1) / kCluster + 8) * sizeof(T);   // slice
-    return s + 512;
+    const int c = threadIdx.x & 31;
+    T a[kWB];
+#pragma unroll
+    for (int i = 0; i < kWB; ++i) a[i] = (i < n && c < n) ? A[i * lda + c] : (i == c ? T(1) : T(0));
+    bool okall = true;
+    T dmine = T(1);
+#pragma unroll
+    for (int k = 0; k < kWB; ++k) {
+        const T d = __shfl_sync(kFull, a[k], k);
+        const T mk = k < n ? mass[k] : T(1);
+        const bool ok = d > T(32) * eps * mk && mk > T(0);
+        okall = okall && ok;
+        const T inv = ok ? T(1) / d : T(0);
+        if (c == k) dmine = ok ? d : T(1);
+#pragma unroll
+        for (int i = k + 1; i < kWB; ++i) {
+            const T m = __shfl_sync(kFull, a[k], i) * inv;   // a_ki / d_k
+            a[i] = (c >= i) ? a[i] - m * a[k] : a[i];
+        }
+    }
+    if (!okall && c == 0) *bad = 1;
+    const T rs = T(1) / t_sqrt(dmine);                         // row c's scale
+#pragma unroll
+    for (int k = 0; k < kWB; ++k) {
+        const T rk = __shfl_sync(kFull, rs, k);
+        if (k < n && c < n) Rw[k * ldr + c] = (k <= c) ? a[k] * rk : T(0);
+    }
 }
 
+// X = U^{-1} for the upper triangle of the n x n block U (n <= 32), right-
+// looking: lane c holds column c of the right-hand side; after x_k is final
+// every s_i (i < k) takes its update at once, so the only serial chain is
+// one multiply and one FMA per step.  Writes X's upper triangle, and zeros
+// below it when zero_lower.
 template <typename T>
-__global__ void __launch_bounds__(kQrThreads)
-k_panel_chol(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restrict__ tau_out,
-             T* __restrict__ Tout, int ldt, T* __restrict__ V, int64_t ldv, int* __restrict__ fail)
+SKL_DEV void warp_tri_inv_upper32(const T* U, int ldu, int n, T* X, int ldx, bool zero_lower)
+{
+    const int c = threadIdx.x & 31;
+    const T invme = c < n ? T(1) / U[c * ldu + c] : T(1);
+    T s[kWB];
+#pragma unroll
+    for (int i = 0; i < kWB; ++i) s[i] = (i == c) ? T(1) : T(0);
+#pragma unroll
+    for (int k = kWB - 1; k >= 0; --k) {
+        const T ik = __shfl_sync(kFull, invme, k);
+        const T xk = s[k] * ik;
+        s[k] = xk;
+        if (k < n) {
+#pragma unroll
+            for (int i = 0; i < k; ++i) s[i] -= U[i * ldu + k] * xk;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kWB; ++i) {
+        if (i < n && c < n) {
+            if (i <= c) X[i * ldx + c] = s[i];
+            else if (zero_lower) X[i * ldx + c] = T(0);
+        }
+    }
+}
+
+// Y = L^{-1} for the unit lower triangle of the n x n block L (strict lower
+// part read; n <= 32), right-looking: writes Y's strict lower part only
+// (unit diagonal implied).
+template <typename T>
+SKL_DEV void warp_tri_inv_unit_lower32(const T* L, int ldl, int n, T* Y, int ldy)
+{
+    const int c = threadIdx.x & 31;
+    T s[kWB];
+#pragma unroll
+    for (int i = 0; i < kWB; ++i) s[i] = (i == c) ? T(1) : T(0);
+#pragma unroll
+    for (int k = 0; k < kWB; ++k) {
+        const T yk = s[k];
+        if (k < n) {
+#pragma unroll
+            for (int i = k + 1; i < kWB; ++i)
+                if (i < n) s[i] -= L[i * ldl + k] * yk;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kWB; ++i)
+        if (i < n && c < n && i > c) Y[i * ldy + c] = s[i];
+}
+
+// Modified LU without pivoting of the n x n block A (n <= 32) in place:
+// at step k, S_k = -sign(pivot), U_kk = pivot - S_k (|U_kk| >= 1); L's
+// multipliers below the diagonal, U on and above it; S_k to sg[k].
+template <typename T>
+SKL_DEV void warp_mlu32(T* A, int lda, int n, T* __restrict__ sg)
+{
+    const int c = threadIdx.x & 31;
+    T a[kWB];
+#pragma unroll
+    for (int i = 0; i < kWB; ++i) a[i] = (i < n && c < n) ? A[i * lda + c] : (i == c ? T(1) : T(0));
+#pragma unroll
+    for (int k = 0; k < kWB; ++k) {
+        const T p = __shfl_sync(kFull, a[k], k);
+        const T sk = p >= T(0) ? T(-1) : T(1);
+        const T u = p - sk;
+        const T iu = T(1) / u;
+        if (c == 0 && k < n) sg[k] = sk;
+        const T ukc = (c == k) ? u : a[k];                   // U[k][c] for c >= k
+        a[k] = ukc;
+#pragma unroll
+        for (int i = k + 1; i < kWB; ++i) {
+            const T l = __shfl_sync(kFull, a[i], k) * iu;    // L[i][k]
+            a[i] = (c > k) ? a[i] - l * ukc : ((c == k) ? l : a[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kWB; ++i)
+        if (i < n && c < n) A[i * lda + c] = a[i];
+}
+
+// Operand views for blk_mul, in the coordinates (r, s) of op(X):
+enum : int { kMFull = 0, kMUpper = 1, kMUpperUnit = 2, kMLowerUnit = 3 };
+
+template <typename T, bool TR, int MASK>
+SKL_DEV T op_at(const T* X, int ld, int r, int s)
+{
+    if (MASK == kMUpper && s < r) return T(0);
+    if (MASK == kMUpperUnit && s <= r) return s == r ? T(1) : T(0);
+    if (MASK == kMLowerUnit && s >= r) return s == r ? T(1) : T(0);
+    return TR ? X[s * ld + r] : X[r * ld + s];
+}
+
+// k range of a product term for masked operands: A upper restricts k >= i,
+// B upper / upper-unit restricts k <= c, A lower-unit restricts k <= i.
+template <int MA, int MB>
+SKL_DEV void k_range(int i0, int c0, int tr, int tc, int kk, int& klo, int& khi)
+{
+    klo = 0;
+    khi = kk;
+    if (MA == kMUpper) klo = i0;
+    if (MA == kMLowerUnit) khi = min(khi, i0 + tr);
+    if (MB == kMUpper || MB == kMUpperUnit) khi = min(khi, c0 + tc);
+    if (MB == kMLowerUnit) klo = max(klo, c0);
+}
+
+// C (m x n) = alpha * op(A) (m x kk) * op(B) (kk x n) [* diag(sB) on B's
+// rows] (+ C when ACC), row-major shared memory; 4 x 4 register tiles, one
+// per thread (m * n <= 16 * kSmallThreads); k runs only over the range the
+// operand masks leave nonzero.  Results wait for a block barrier, so C may
+// alias A or B.  With Cg set, C goes to global memory column-major (ldg)
+// instead and its diagonal also to tau.
+template <typename T, bool TA, int MA, bool TB, int MB, bool ACC = false>
+SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
+                     const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg = nullptr,
+                     int ldg = 0, T* __restrict__ tau = nullptr)
+{
+    const int ntc = (n + 3) / 4;
+    const int t = threadIdx.x;
+    const int i0 = (t / ntc) * 4, c0 = (t % ntc) * 4;
+    const bool act = i0 < m;
+    T acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] = T(0);
+    if (act) {
+        int klo, khi;
+        k_range<MA, MB>(i0, c0, 4, 4, kk, klo, khi);
+        for (int k = klo; k < khi; ++k) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) av[r] = (i0 + r < m) ? op_at<T, TA, MA>(A, lda, i0 + r, k) : T(0);
+            const T sc = sB ? sB[k] : T(1);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) bv[q] = (c0 + q < n) ? sc * op_at<T, TB, MB>(B, ldb, k, c0 + q) : T(0);
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[r][q] += av[r] * bv[q];
+        }
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + r;
+            if (i >= m) continue;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = c0 + q;
+                if (c >= n) continue;
+                const T v = alpha * acc[r][q];
+                if (Cg) {
+                    Cg[i + (int64_t)c * ldg] = v;
+                    if (i == c) tau[i] = v;
+                } else if (ACC) {
+                    C[i * ldc + c] += v;
+                } else {
+                    C[i * ldc + c] = v;
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Cholesky G = R^T R (b <= 64) with X = R^{-1}: 2 x 2 blocks of 32.
+// R (upper, zeros below) over G in place; X (upper, zeros below) to Xs.
+template <typename T>
+SKL_DEV void chol_inv_blocked(T* G, int ldx, int b, const T* __restrict__ mass, T eps, T* Xs,
+                              int* bad)
+{
+    const int wid = threadIdx.x >> 5;
+    const int n1 = min(b, kWB), n2 = b - n1;
+    if (wid == 0) {
+        warp_chol32<T>(G, ldx, n1, mass, eps, G, ldx, bad);
+        __syncwarp();
+        warp_tri_inv_upper32<T>(G, ldx, n1, Xs, ldx, true);
+    }
+    __syncthreads();
+    if (n2 > 0) {
+        T* G12 = G + n1;
+        T* G21 = G + n1 * ldx;
+        T* G22 = G + n1 * ldx + n1;
+        // R12 = R11^{-T} G12 = X11^T G12
+        blk_mul<T, true, kMFull, false, kMFull>(n1, n2, n1, Xs, ldx, G12, ldx, nullptr, T(1), G12, ldx);
+        // G22 -= R12^T R12
+        blk_mul<T, true, kMFull, false, kMFull, true>(n2, n2, n1, G12, ldx, G12, ldx, nullptr, T(-1), G22, ldx);
+        if (wid == 0) {
+            warp_chol32<T>(G22, ldx, n2, mass + n1, eps, G22, ldx, bad);
+            __syncwarp();
+            warp_tri_inv_upper32<T>(G22, ldx, n2, Xs + n1 * ldx + n1, ldx, true);
+        }
+        __syncthreads();
+        // X12 = -(X11 R12) X22, formed in place in X's upper-right block
+        T* X21 = Xs + n1 * ldx;
+        T* X12 = Xs + n1;
+        blk_mul<T, false, kMFull, false, kMFull>(n1, n2, n1, Xs, ldx, G12, ldx, nullptr, T(1), X12, ldx);
+        blk_mul<T, false, kMFull, false, kMFull>(n1, n2, n2, X12, ldx, Xs + n1 * ldx + n1, ldx, nullptr,
+                                                 T(-1), X12, ldx);
+        for (int e = threadIdx.x; e < n2 * n1; e += kSmallThreads) {
+            const int i = e / n1, c = e - i * n1;
+            X21[i * ldx + c] = T(0);
+            G21[i * ldx + c] = T(0);
+        }
+        __syncthreads();
+    }
+}
+
+// Modified LU of A (b <= 64) in place (L strict lower, U upper), signs to
+// sg, and in Z: L^{-1} (strict lower, unit diagonal implied) and U^{-1}
+// (upper).  2 x 2 blocks of 32.
+template <typename T>
+SKL_DEV void mlu_inv_blocked(T* A, int ldx, int b, T* __restrict__ sg, T* Z)
+{
+    const int wid = threadIdx.x >> 5;
+    const int n1 = min(b, kWB), n2 = b - n1;
+    if (wid == 0) {
+        warp_mlu32<T>(A, ldx, n1, sg);
+        __syncwarp();
+        warp_tri_inv_unit_lower32<T>(A, ldx, n1, Z, ldx);
+        warp_tri_inv_upper32<T>(A, ldx, n1, Z, ldx, false);
+    }
+    __syncthreads();
+    if (n2 > 0) {
+        T* A12 = A + n1;
+        T* A21 = A + n1 * ldx;
+        T* A22 = A + n1 * ldx + n1;
+        T* Z12 = Z + n1;
+        T* Z21 = Z + n1 * ldx;
+        T* Z22 = Z + n1 * ldx + n1;
+        // U12 = L11^{-1} A12 ; L21 = A21 U11^{-1}
+        blk_mul<T, false, kMLowerUnit, false, kMFull>(n1, n2, n1, Z, ldx, A12, ldx, nullptr, T(1), A12, ldx);
+        blk_mul<T, false, kMFull, false, kMUpper>(n2, n1, n1, A21, ldx, Z, ldx, nullptr, T(1), A21, ldx);
+        // A22 -= L21 U12
+        blk_mul<T, false, kMFull, false, kMFull, true>(n2, n2, n1, A21, ldx, A12, ldx, nullptr, T(-1), A22, ldx);
+        if (wid == 0) {
+            warp_mlu32<T>(A22, ldx, n2, sg + n1);
+            __syncwarp();
+            warp_tri_inv_unit_lower32<T>(A22, ldx, n2, Z22, ldx);
+            warp_tri_inv_upper32<T>(A22, ldx, n2, Z22, ldx, false);
+        }
+        __syncthreads();
+        // L^{-1}_21 = -L22^{-1} (L21 L11^{-1}) ; U^{-1}_12 = -(U11^{-1} U12) U22^{-1}
+        blk_mul<T, false, kMFull, false, kMLowerUnit>(n2, n1, n1, A21, ldx, Z, ldx, nullptr, T(1), Z21, ldx);
+        blk_mul<T, false, kMUpper, false, kMFull>(n1, n2, n1, Z, ldx, A12, ldx, nullptr, T(1), Z12, ldx);
+        blk_mul<T, false, kMLowerUnit, false, kMFull>(n2, n1, n2, Z22, ldx, Z21, ldx, nullptr, T(-1), Z21, ldx);
+        blk_mul<T, false, kMFull, false, kMUpper>(n1, n2, n2, Z12, ldx, Z22, ldx, nullptr, T(-1), Z12, ldx);
+    }
+}
+
+// b x b workspace layout of the small kernels (row-major, ld = b + 4).
+template <typename T>
+size_t chol_small_smem_bytes(int b)
+{
+    return (4 * (size_t)b * (b + 4) + 2 * (size_t)b) * sizeof(T) + 256;
+}
+
+// Pass 1: R1 and X1 = R1^{-1} from G1 (column-major b x b, ldg = b).  Sets
+// *fail (1 on a Cholesky breakdown, else 0).
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads, 1)
+k_chol_small1(const T* __restrict__ G, int b, T* __restrict__ R1, T* __restrict__ X1,
+              int* __restrict__ fail)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int LDG = b + 1;
-    const unsigned crank = cluster_ctarank();
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int r0 = (int)crank * R;
-    const int nr = max(0, min(R, M - r0));
-    const int npairs = b * (b + 1) / 2;
-    const int per = (npairs + kCluster - 1) / kCluster;
-    T* Ps = (T*)smem_raw;                        // [b][R]
-    T* G = Ps + (size_t)R * b;                   // Gram -> Cholesky factor; later the LU (L below, U above)
-    T* Racc = G + b * LDG;                       // accumulated R (upper)
-    T* Rinv = Racc + b * LDG;                    // Rc^{-1}; staging; later T
-    T* Tmp = Rinv + b * LDG;                     // L^{-1}, then U^{-1}
-    T* flat = Tmp + b * LDG;                     // Gram pairs (a <= c), this CTA's partial
-    T* Sg = flat + npairs;                       // signs S (CTA 0) and the copy of S (all)
-    T* mass = Sg + 2 * b;                        // ||P(:,k)||^2 before each pass
-    T* slice = mass + 2 * b;                     // this CTA's reduced slice of the Gram
+    const int LDX = b + 4;
+    T* S0 = (T*)smem_raw;
+    T* S1 = S0 + (size_t)b * LDX;
+    T* mass = S1 + (size_t)b * LDX;
     __shared__ int s_bad;
     const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
-
-    for (int e = tid; e < R * b; e += kQrThreads) {
-        int lr = e % R, c = e / R;
-        Ps[lr + (size_t)c * R] = (lr < nr) ? A[(int64_t)(j0 + r0 + lr) + (int64_t)(j0 + c) * ld] : T(0);
+    if (threadIdx.x == 0) s_bad = 0;
+    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
+        const int i = e % b, c = e / b;
+        S0[i * LDX + c] = G[e];
     }
-    if (tid == 0) s_bad = 0;
-    for (int e = tid; e < b * LDG; e += kQrThreads) Racc[e] = T(0);
+    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = G[k * b + k];
     __syncthreads();
-    for (int a = tid; a < b; a += kQrThreads) Racc[a * LDG + a] = T(1);
-
-    for (int pass = 0; pass < 2; ++pass) {
-        // ---- local Gram, pairs (a <= c) in row order of the upper triangle ----
-        for (int q = wid; q < npairs; q += kQrWarps) {
-            int a = 0, rem = q;
-            while (rem >= b - a) { rem -= b - a; ++a; }
-            const int c = a + rem;
-            const T* pa = Ps + (size_t)a * R;
-            const T* pc = Ps + (size_t)c * R;
-            T acc = T(0);
-            for (int lr = lane; lr < nr; lr += 32) acc += pa[lr] * pc[lr];
-            acc = warp_sum(acc);
-            if (lane == 0) flat[q] = acc;
-        }
-        cluster_sync();
-        // reduce-scatter: CTA crank sums pairs [crank*per, crank*per + per)
-        for (int q = (int)crank * per + tid; q < min(npairs, ((int)crank + 1) * per); q += kQrThreads) {
-            T v[kCluster];
-#pragma unroll
-            for (int w = 0; w < kCluster; ++w) v[w] = dsmem_ld(&flat[q], w);
-            T acc = T(0);
-#pragma unroll
-            for (int w = 0; w < kCluster; ++w) acc += v[w];
-            slice[q - (int)crank * per] = acc;
-        }
-        cluster_sync();
-        // all-gather straight into the symmetric G
-        for (int q = tid; q < npairs; q += kQrThreads) {
-            const int owner = q / per;
-            const T g = dsmem_ld(&slice[q - owner * per], owner);
-            int a = 0, rem = q;
-            while (rem >= b - a) { rem -= b - a; ++a; }
-            const int c = a + rem;
-            G[a * LDG + c] = g;
-            G[c * LDG + a] = g;
-            if (a == c) mass[a] = g;
-        }
-        cluster_sync();   // all slices read before they are reused
-        // ---- Cholesky G = Rc^T Rc (upper Rc in G's upper triangle) ----
-        for (int k = 0; k < b; ++k) {
-            if (tid == 0) {
-                const T gk = G[k * LDG + k];
-                if (!(gk > T(32) * eps * mass[k]) || !(mass[k] > T(0))) s_bad = 1;
-                G[k * LDG + k] = gk > T(0) ? t_sqrt(gk) : T(1);
-            }
-            __syncthreads();
-            const T idk = T(1) / G[k * LDG + k];
-            for (int c = k + 1 + tid; c < b; c += kQrThreads) G[k * LDG + c] *= idk;
-            __syncthreads();
-            const int rem_n = b - k - 1;
-            for (int e = tid; e < rem_n * rem_n; e += kQrThreads) {
-                const int i = k + 1 + e / rem_n, c = k + 1 + e % rem_n;
-                if (c >= i) G[i * LDG + c] -= G[k * LDG + i] * G[k * LDG + c];
-            }
-            __syncthreads();
-        }
-        if (s_bad) break;   // uniform: every CTA computed the same G
-        // ---- Rinv = Rc^{-1} (upper), column per thread ----
-        for (int c = tid; c < b; c += kQrThreads) {
-            Rinv[c * LDG + c] = T(1) / G[c * LDG + c];
-            for (int i = c - 1; i >= 0; --i) {
-                T acc = T(0);
-                for (int kk = i + 1; kk <= c; ++kk) acc += G[i * LDG + kk] * Rinv[kk * LDG + c];
-                Rinv[i * LDG + c] = -acc / G[i * LDG + i];
-            }
-            for (int i = c + 1; i < b; ++i) Rinv[i * LDG + c] = T(0);
-        }
-        __syncthreads();
-        // ---- P <- P Rc^{-1}: thread per local row ----
-        for (int lr = tid; lr < nr; lr += kQrThreads) {
-            T row[kMaxNb];
-            for (int a = 0; a < b; ++a) row[a] = Ps[lr + (size_t)a * R];
-            for (int c = b - 1; c >= 0; --c) {
-                T acc = T(0);
-                for (int a = 0; a <= c; ++a) acc += row[a] * Rinv[a * LDG + c];
-                Ps[lr + (size_t)c * R] = acc;
-            }
-        }
-        __syncthreads();
-        // ---- Racc <- Rc * Racc (staged in Rinv, now free) ----
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            const int i = e / b, c = e % b;
-            T acc = T(0);
-            if (i <= c)
-                for (int kk = i; kk <= c; ++kk) acc += G[i * LDG + kk] * Racc[kk * LDG + c];
-            Rinv[i * LDG + c] = acc;
-        }
-        __syncthreads();
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            const int i = e / b, c = e % b;
-            Racc[i * LDG + c] = Rinv[i * LDG + c];
-        }
-        __syncthreads();
+    chol_inv_blocked<T>(S0, LDX, b, mass, eps, S1, &s_bad);
+    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
+        const int i = e / b, c = e % b;
+        R1[e] = S0[i * LDX + c];     // row-major b x b
+        X1[c * b + i] = S1[i * LDX + c];   // column-major (a GEMM operand)
     }
+    if (threadIdx.x == 0) *fail = s_bad ? 1 : 0;
+}
+
+// Pass 2 and the reconstruction: from G2 (column-major), R1 (row-major) and
+// the first b rows of Q (column-major, ldq) writes W = R2^{-1} U^{-1}
+// (column-major b x b), T (ldt), tau, the panel's first b rows of A (R_H on
+// and above the diagonal, L below) and of V (unit lower L).  Does nothing if
+// pass 1 failed; sets *fail on a pass-2 breakdown (A untouched).
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads, 1)
+k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T* __restrict__ Q,
+              int64_t ldq, T* __restrict__ A, int64_t ld, int j0, T* __restrict__ V, int64_t ldv,
+              T* __restrict__ Tout, int ldt, T* __restrict__ tau_out, T* __restrict__ Wg,
+              int* __restrict__ fail)
+{
+    if (*fail) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int LDX = b + 4;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T* S0 = (T*)smem_raw;                        // R1 -> R = R2 R1
+    T* S1 = S0 + (size_t)b * LDX;                // G2 -> R2 -> L^{-1} \ U^{-1}
+    T* S2 = S1 + (size_t)b * LDX;                // X2 -> W
+    T* S3 = S2 + (size_t)b * LDX;                // Q(0:b,:) -> Q1 -> L \ U
+    T* Sg = S3 + (size_t)b * LDX;
+    T* mass = Sg + b;
+    __shared__ int s_bad;
+    const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
+    if (threadIdx.x == 0) s_bad = 0;
+    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
+        const int i = e % b, c = e / b;          // column-major sources
+        S1[i * LDX + c] = G[e];
+        S3[i * LDX + c] = Q[i + (int64_t)c * ldq];
+        const int r = e / b, q = e % b;          // row-major source
+        S0[r * LDX + q] = R1g[e];
+    }
+    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = T(1);
+    __syncthreads();
+    // Gershgorin distance of G2 from the identity
+    for (int i = wid; i < b; i += kSmallThreads / 32) {
+        T sabs = T(0);
+        for (int c = lane; c < b; c += 32) sabs += t_abs(S1[i * LDX + c] - (c == i ? T(1) : T(0)));
+        sabs = warp_sum(sabs);
+        if (lane == 0 && !(sabs <= T(0.5))) s_bad = 1;
+    }
+    __syncthreads();
     if (s_bad) {
-        // every CTA reached the same verdict from the same data: A untouched
-        if (crank == 0 && tid == 0) *fail = 1;
-        cluster_sync();
+        if (threadIdx.x == 0) *fail = 1;
         return;
     }
-    // ---- modified LU of Q1 - S on CTA 0 (global panel rows 0..b-1, R >= b) ----
-    if (crank == 0) {
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            const int i = e % b, c = e / b;
-            G[i * LDG + c] = Ps[i + (size_t)c * R];
-        }
-        __syncthreads();
-        for (int k = 0; k < b; ++k) {
-            if (tid == 0) {
-                const T pv = G[k * LDG + k];
-                const T sk = pv >= T(0) ? T(-1) : T(1);   // S_kk = -sign(pivot)
-                Sg[k] = sk;
-                G[k * LDG + k] = pv - sk;
-            }
-            __syncthreads();
-            const T ukk = G[k * LDG + k];
-            for (int i = k + 1 + tid; i < b; i += kQrThreads) G[i * LDG + k] /= ukk;
-            __syncthreads();
-            const int rem_n = b - k - 1;
-            for (int e = tid; e < rem_n * rem_n; e += kQrThreads) {
-                const int i = k + 1 + e / rem_n, c = k + 1 + e % rem_n;
-                G[i * LDG + c] -= G[i * LDG + k] * G[k * LDG + c];
-            }
-            __syncthreads();
-        }
-        // Tmp = L^{-1} (unit lower), column per thread
-        for (int c = tid; c < b; c += kQrThreads) {
-            for (int i = 0; i < b; ++i) {
-                T acc = (i == c) ? T(1) : T(0);
-                for (int kk = c; kk < i; ++kk) acc -= G[i * LDG + kk] * Tmp[kk * LDG + c];
-                Tmp[i * LDG + c] = (i < c) ? T(0) : acc;
-            }
-        }
-        __syncthreads();
-        // T = -U S L^{-T} into Rinv:  T[i][c] = -sum_{k=i..c} U[i][k] S_k L^{-1}[c][k]
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            const int i = e / b, c = e % b;
-            T acc = T(0);
-            if (i <= c)
-                for (int kk = i; kk <= c; ++kk) acc += G[i * LDG + kk] * Sg[kk] * Tmp[c * LDG + kk];
-            Rinv[i * LDG + c] = -acc;
-        }
-        __syncthreads();
-        for (int e = tid; e < b * b; e += kQrThreads) {
-            const int i = e % b, c = e / b;
-            Tout[i + (int64_t)c * ldt] = (i <= c) ? Rinv[i * LDG + c] : T(0);
-            if (i == c) tau_out[j0 + i] = Rinv[i * LDG + i];
-        }
-        __syncthreads();
-        // Tmp = U^{-1} (upper), column per thread
-        for (int c = tid; c < b; c += kQrThreads) {
-            Tmp[c * LDG + c] = T(1) / G[c * LDG + c];
-            for (int i = c - 1; i >= 0; --i) {
-                T acc = T(0);
-                for (int kk = i + 1; kk <= c; ++kk) acc += G[i * LDG + kk] * Tmp[kk * LDG + c];
-                Tmp[i * LDG + c] = -acc / G[i * LDG + i];
-            }
-            for (int i = c + 1; i < b; ++i) Tmp[i * LDG + c] = T(0);
-        }
+    chol_inv_blocked<T>(S1, LDX, b, mass, eps, S2, &s_bad);    // R2 over S1, X2 -> S2
+    if (s_bad) {
+        if (threadIdx.x == 0) *fail = 1;
+        return;
     }
-    cluster_sync();   // CTA 0's S, L (in G) and U^{-1} (in Tmp) published
-    // every CTA fetches U^{-1} into Rinv and S into Sg[b..2b)
-    for (int e = tid; e < b * b; e += kQrThreads) {
-        const int i = e / b, c = e % b;
-        Rinv[i * LDG + c] = (i <= c) ? dsmem_ld(&Tmp[i * LDG + c], 0) : T(0);
+    blk_mul<T, false, kMFull, false, kMUpper>(b, b, b, S3, LDX, S2, LDX, nullptr, T(1), S3, LDX);   // Q1 = Q(0:b,:) X2
+    blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S1, LDX, S0, LDX, nullptr, T(1), S0, LDX);  // R = R2 R1
+    mlu_inv_blocked<T>(S3, LDX, b, Sg, S1);                      // Q1 - S = L U; S1 = L^{-1} \ U^{-1}
+    blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S2, LDX, S1, LDX, nullptr, T(1), S2, LDX);  // W = X2 U^{-1}
+    blk_mul<T, false, kMUpper, true, kMUpperUnit>(b, b, b, S3, LDX, S1, LDX, Sg, T(-1), nullptr, 0,
+                                                   Tout, ldt, tau_out + j0);   // T = -U S L^{-T}
+    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
+        const int g = e % b, c = e / b;          // column-major targets
+        Wg[e] = S2[g * LDX + c];
+        const T l = (g > c) ? S3[g * LDX + c] : T(0);
+        A[(int64_t)(j0 + g) + (int64_t)(j0 + c) * ld] = (g <= c) ? Sg[g] * S0[g * LDX + c] : l;
+        V[(int64_t)g + (int64_t)c * ldv] = (g > c) ? l : (g == c ? T(1) : T(0));
     }
-    for (int k = tid; k < b; k += kQrThreads) Sg[b + k] = dsmem_ld(&Sg[k], 0);
-    __syncthreads();
-    // ---- write back: R_H = S Racc above the diagonal (CTA 0), V below ----
-    for (int lr = tid; lr < nr; lr += kQrThreads) {
-        const int g = r0 + lr;
-        T row[kMaxNb];
-        for (int a = 0; a < b; ++a) row[a] = Ps[lr + (size_t)a * R];
-        for (int c = 0; c < b; ++c) {
-            T out, vv;
-            if (g < b) {
-                const T l = (g > c) ? G[g * LDG + c] : T(0);   // CTA 0 holds L
-                out = (g <= c) ? Sg[b + g] * Racc[g * LDG + c] : l;
-                vv = (g > c) ? l : (g == c ? T(1) : T(0));
-            } else {
-                T acc = T(0);
-                for (int a = 0; a <= c; ++a) acc += row[a] * Rinv[a * LDG + c];
-                out = acc;
-                vv = acc;
-            }
-            A[(int64_t)(j0 + g) + (int64_t)(j0 + c) * ld] = out;
-            V[(int64_t)g + (int64_t)c * ldv] = vv;
-        }
-    }
-    if (crank == 0 && tid == 0) *fail = 0;
-    cluster_sync();   // CTA 0's shared memory stays alive until every CTA read it
+}
+
+// A(j0+b : j0+M, j0 : j0+b) = V(b : M, :) once the panel succeeded.
+template <typename T>
+__global__ void k_chol_copy_down(const T* __restrict__ V, int64_t ldv, T* __restrict__ A, int64_t ld,
+                                 int j0, int M, int b, const int* __restrict__ fail)
+{
+    if (*fail) return;
+    const int rows = M - b;
+    const int c = blockIdx.y;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+        A[(int64_t)(j0 + b + r) + (int64_t)(j0 + c) * ld] = V[(int64_t)(b + r) + (int64_t)c * ldv];
 }
 
 // ------------------------------------------------- Q^T c for one panel --
@@ -956,8 +1168,9 @@ __global__ void k_iota_int(int* v, int n)
 
 // ------------------------------------------------------------ host side --
 // Panel method: CholeskyQR2 + Householder reconstruction by default on the
-// FP64 path, the column-by-column pivoted panel on the FP32 path;
-// SKILLS_QR_PANEL=chol|pivoted overrides.
+// FP32 path (its tall products run at full-GPU GEMM speed), the column-by-
+// column pivoted panel on the FP64 path (there the FP64 GEMMs cost more than
+// the latency the pivoted panel spends); SKILLS_QR_PANEL=chol|pivoted overrides.
 template <typename T>
 static bool qr_chol_enabled()
 {
@@ -968,7 +1181,7 @@ static bool qr_chol_enabled()
         else if (e && std::string(e) == "chol") v = 1;
         else v = 2;
     }
-    if (v == 2) return std::is_same<T, double>::value;
+    if (v == 2) return std::is_same<T, float>::value;
     return v == 1;
 }
 
@@ -1001,6 +1214,7 @@ template <typename T>
 struct QrBuffers {
     T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *tmp;
     int *sel, *plan_src, *plan_dst, *plan_n, *chol_fail;
+    T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
     double *qw;
     int64_t part_cap, tmp_rows;
 };
@@ -1036,6 +1250,10 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.plan_dst = (int*)take(2 * kMaxNb * sizeof(int));
     B.plan_n = (int*)take(sizeof(int));
     B.chol_fail = (int*)take(sizeof(int));
+    B.cg = (T*)take((size_t)p.nb * p.nb * sizeof(T));
+    B.cr1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
+    B.cx1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
+    B.cw = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.qw = (double*)take(kMaxNb * sizeof(double));
     if (total) *total = off;
     return B;
@@ -1116,7 +1334,7 @@ struct QrTimer {
 
 template <typename T>
 static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
-                    cudaStream_t st, double* c, bool pivoting, double* qr_prof)
+                    unsigned* status, cudaStream_t st, double* c, bool pivoting, double* qr_prof)
 {
     QrTimer tm{qr_prof, {}, {}, 0, st};
     QrPlan p = qr_plan<T>(m, d);
@@ -1137,10 +1355,10 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     }
     const size_t ysm_max = YqrpSmem<T>::bytes(nbp, (int)((d + kCluster - 1) / kCluster));
     const size_t psm = panel_smem_bytes<T>(p.R, nb);
-    const size_t csm = chol_panel_smem_bytes<T>(p.R, nb);
+
     // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
     // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
-    const bool use_chol = pivoting && p.R >= nb && csm <= 226 * 1024 && qr_chol_enabled<T>();
+    const bool use_chol = pivoting && nb <= 2 * kWB && qr_chol_enabled<T>();
     for (int64_t j = 0; j < mn; j += nb) {
         const int b = (int)std::min<int64_t>(nb, std::min<int64_t>(d - j, m - j));
         const bool last = (j + nb >= m) || (j + nb >= d);
@@ -1158,7 +1376,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             tm.end(0, t0);
             trace_phase(st, "qr: yqrp");
             t0 = tm.begin();
-            k_perm_plan<<<1, 32, 0, st>>>(B.sel, b, B.plan_src, B.plan_dst, B.plan_n);
+            k_perm_plan<<<1, 32, 0, st>>>(B.sel, b, N, B.plan_src, B.plan_dst, B.plan_n, status);
             SKL_LAUNCHED();
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
             k_perm_gather<T><<<gA, 256, 0, st>>>(A, ld, (int)m, jj, B.plan_src, B.plan_n, B.tmp);
@@ -1183,10 +1401,29 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             cudaEvent_t t0 = tm.begin();
             const int* cf = nullptr;
             if (use_chol && !last) {
-                int* failp = B.chol_fail;
-                void* cargs[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
-                                 &ldv, &failp};
-                launch_cluster<T>((const void*)k_panel_chol<T>, dim3(kQrThreads), csm, st, cargs);
+                T* P = A + j + j * ld;
+                const size_t ssm = chol_small_smem_bytes<T>(b);
+                static bool attr_set = false;
+                if (!attr_set) {
+                    const size_t mx = chol_small_smem_bytes<T>(kMaxNb);
+                    SKL_CUDA(cudaFuncSetAttribute(k_chol_small1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+                    SKL_CUDA(cudaFuncSetAttribute(k_chol_small2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+                    attr_set = true;
+                }
+                gemm<T>(true, false, b, b, M, T(1), P, ld, P, ld, T(0), B.cg, b, B.part, B.part_cap, st);
+                k_chol_small1<T><<<1, kSmallThreads, ssm, st>>>(B.cg, b, B.cr1, B.cx1, B.chol_fail);
+                SKL_CUDA(cudaGetLastError());
+                SKL_LAUNCHED();
+                gemm<T>(false, false, M, b, b, T(1), P, ld, B.cx1, b, T(0), B.tmp, M, nullptr, 0, st);
+                gemm<T>(true, false, b, b, M, T(1), B.tmp, M, B.tmp, M, T(0), B.cg, b, B.part, B.part_cap, st);
+                k_chol_small2<T><<<1, kSmallThreads, ssm, st>>>(B.cg, b, B.cr1, B.tmp, M, A, ld, jj, B.V, m,
+                                                                B.Tm, nb, tau, B.cw, B.chol_fail);
+                SKL_CUDA(cudaGetLastError());
+                SKL_LAUNCHED();
+                gemm<T>(false, false, M - b, b, b, T(1), B.tmp + b, M, B.cw, b, T(0), B.V + b, m, nullptr, 0, st);
+                dim3 gc((unsigned)std::max<int64_t>(1, std::min<int64_t>((M - b + 255) / 256, 64)), b);
+                k_chol_copy_down<T><<<gc, 256, 0, st>>>(B.V, m, A, ld, jj, M, b, B.chol_fail);
+                SKL_LAUNCHED();
                 cf = B.chol_fail;
             }
             void* args[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,
@@ -1246,8 +1483,7 @@ template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work, unsigned* status,
           cudaStream_t st, double* c, int pivoting, double* qr_prof)
 {
-    (void)status;
-    qr_core<T>(A, m, d, ld, jpvt, tau, work, st, c, pivoting != 0, qr_prof);
+    qr_core<T>(A, m, d, ld, jpvt, tau, work, status, st, c, pivoting != 0, qr_prof);
 }
 
 template void cpqr<float>(float*, int64_t, int64_t, int64_t, int*, float*, void*, unsigned*,

@@ -194,6 +194,9 @@ static void check_opts(const skl_opts& o)
         fail(SKL_ERR_INVALID, "unknown precision");
 }
 
+// Status bit a QR pivot selection sets when it meets non-finite values.
+constexpr unsigned kQrSelectBit = 8u;
+
 static unsigned read_status(Context& C, cudaStream_t st)
 {
     unsigned v = 0;
@@ -309,6 +312,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     // ---- randomized CPQR, c = Q^T S b ----
     cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1,
             o.profile ? info.qr_prof_ms : nullptr);
+    if (read_status(C, st) & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
     trace_phase(st, "cpqr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank, inverse, condition ----
@@ -632,8 +636,10 @@ static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
     trace_phase(st, "dense sketch");
     SKL_CUDA(cudaEventRecord(ev[3], st));
     // ---- QR (pivoted for the CPQR path) ----
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
     cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cpqr_on ? cvec : nullptr,
             cpqr_on ? 1 : 0, o.profile ? info.qr_prof_ms : nullptr);
+    if (read_status(C, st) & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
     trace_phase(st, "dense qr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank: leading |R_ii| > rcond (absolute, :79-89); noCPQR keeps all ----

@@ -108,7 +108,14 @@ static void cpqr_block(double* A, int64_t m, int64_t d, int64_t* jpvt, double* t
     T* td = C.arena.alloc<T>(mn);
     void* work = C.arena.take(ws);
     to_device_as<T>(A, m, d, m, Ad, ld, st);
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
     cpqr<T>(Ad, m, d, ld, jp, td, work, C.dev_status, st, nullptr, 1);
+    {
+        unsigned stt = 0;
+        SKL_CUDA(cudaMemcpyAsync(&stt, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        if (stt & 8u) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
+    }
     from_device_as<T>(Ad, m, d, ld, A, m, st);
     std::vector<int> hj((size_t)d);
     std::vector<T> ht((size_t)mn);
