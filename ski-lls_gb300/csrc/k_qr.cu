@@ -685,435 +685,14 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
 //
 // The tall products (the two Grams, P R1^{-1}, Q W) are GEMMs over the whole
 // GPU, the panel staying in L2; the b x b algebra runs in one CTA
-// (k_chol_small1/2) with room for the registers its 32-wide warp
-// factorizations need: 2 x 2 blocks of 32, each diagonal block factored by
-// one warp holding it in registers (shuffles, no block barrier), the
-// off-diagonal blocks by register-tiled block products.
+// (k_chol_small1/2) with room for the registers its factorizations need:
+// two warps hold the matrix a column per thread and take one 64-thread
+// barrier per step; products use register-tiled block multiplies.
 //
 // A Cholesky pivot below 32 eps of its column's mass, or a second Gram
 // farther than 1/2 from the identity (Gershgorin), means kappa(P) is too large
 // for CholeskyQR2: *fail = 1, A is left untouched and the pivoted panel kernel
 // launched next factors the panel instead.
-constexpr int kSmallThreads = 256;
-
-// ---- small dense algebra on b x b (b <= 64) row-major shared-memory blocks --
-// Diagonal 32 x 32 blocks are factored by one warp with the block in
-// registers (lane c holds column c; pivots and multipliers travel by
-// shuffles, no block barrier); off-diagonal blocks are formed with
-// register-tiled block products.  Indices >= n of a 32-block act as identity.
-constexpr int kWB = 32;
-constexpr unsigned kFull = 0xffffffffu;
-
-// Cholesky of the symmetric n x n block A (n <= 32): R (upper, zeros below)
-// to Rw.  A may alias Rw.  Sets *bad when a pivot is below 32 eps times its
-// mass (mass[k], the column's squared norm).  Run by one warp.  Rows stay
-// unnormalised during the elimination (a_ic -= a_ki a_kc / d_k); row k is
-// scaled by 1/sqrt(d_k) at the end, all rows at once.
-template <typename T>
-SKL_DEV void warp_chol32(const T* A, int lda, int n, const T* __restrict__ mass, T eps, T* Rw,
-                         int ldr, int* bad)
-{
-    const int c = threadIdx.x & 31;
-    T a[kWB];
-#pragma unroll
-    for (int i = 0; i < kWB; ++i) a[i] = (i < n && c < n) ? A[i * lda + c] : (i == c ? T(1) : T(0));
-    bool okall = true;
-    T dmine = T(1);
-#pragma unroll
-    for (int k = 0; k < kWB; ++k) {
-        const T d = __shfl_sync(kFull, a[k], k);
-        const T mk = k < n ? mass[k] : T(1);
-        const bool ok = d > T(32) * eps * mk && mk > T(0);
-        okall = okall && ok;
-        const T inv = ok ? T(1) / d : T(0);
-        if (c == k) dmine = ok ? d : T(1);
-#pragma unroll
-        for (int i = k + 1; i < kWB; ++i) {
-            const T m = __shfl_sync(kFull, a[k], i) * inv;   // a_ki / d_k
-            a[i] = (c >= i) ? a[i] - m * a[k] : a[i];
-        }
-    }
-    if (!okall && c == 0) *bad = 1;
-    const T rs = T(1) / t_sqrt(dmine);                         // row c's scale
-#pragma unroll
-    for (int k = 0; k < kWB; ++k) {
-        const T rk = __shfl_sync(kFull, rs, k);
-        if (k < n && c < n) Rw[k * ldr + c] = (k <= c) ? a[k] * rk : T(0);
-    }
-}
-
-// X = U^{-1} for the upper triangle of the n x n block U (n <= 32), right-
-// looking: lane c holds column c of the right-hand side; after x_k is final
-// every s_i (i < k) takes its update at once, so the only serial chain is
-// one multiply and one FMA per step.  Writes X's upper triangle, and zeros
-// below it when zero_lower.
-template <typename T>
-SKL_DEV void warp_tri_inv_upper32(const T* U, int ldu, int n, T* X, int ldx, bool zero_lower)
-{
-    const int c = threadIdx.x & 31;
-    const T invme = c < n ? T(1) / U[c * ldu + c] : T(1);
-    T s[kWB];
-#pragma unroll
-    for (int i = 0; i < kWB; ++i) s[i] = (i == c) ? T(1) : T(0);
-#pragma unroll
-    for (int k = kWB - 1; k >= 0; --k) {
-        const T ik = __shfl_sync(kFull, invme, k);
-        const T xk = s[k] * ik;
-        s[k] = xk;
-        if (k < n) {
-#pragma unroll
-            for (int i = 0; i < k; ++i) s[i] -= U[i * ldu + k] * xk;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kWB; ++i) {
-        if (i < n && c < n) {
-            if (i <= c) X[i * ldx + c] = s[i];
-            else if (zero_lower) X[i * ldx + c] = T(0);
-        }
-    }
-}
-
-// Y = L^{-1} for the unit lower triangle of the n x n block L (strict lower
-// part read; n <= 32), right-looking: writes Y's strict lower part only
-// (unit diagonal implied).
-template <typename T>
-SKL_DEV void warp_tri_inv_unit_lower32(const T* L, int ldl, int n, T* Y, int ldy)
-{
-    const int c = threadIdx.x & 31;
-    T s[kWB];
-#pragma unroll
-    for (int i = 0; i < kWB; ++i) s[i] = (i == c) ? T(1) : T(0);
-#pragma unroll
-    for (int k = 0; k < kWB; ++k) {
-        const T yk = s[k];
-        if (k < n) {
-#pragma unroll
-            for (int i = k + 1; i < kWB; ++i)
-                if (i < n) s[i] -= L[i * ldl + k] * yk;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kWB; ++i)
-        if (i < n && c < n && i > c) Y[i * ldy + c] = s[i];
-}
-
-// Modified LU without pivoting of the n x n block A (n <= 32) in place:
-// at step k, S_k = -sign(pivot), U_kk = pivot - S_k (|U_kk| >= 1); L's
-// multipliers below the diagonal, U on and above it; S_k to sg[k].
-template <typename T>
-SKL_DEV void warp_mlu32(T* A, int lda, int n, T* __restrict__ sg)
-{
-    const int c = threadIdx.x & 31;
-    T a[kWB];
-#pragma unroll
-    for (int i = 0; i < kWB; ++i) a[i] = (i < n && c < n) ? A[i * lda + c] : (i == c ? T(1) : T(0));
-#pragma unroll
-    for (int k = 0; k < kWB; ++k) {
-        const T p = __shfl_sync(kFull, a[k], k);
-        const T sk = p >= T(0) ? T(-1) : T(1);
-        const T u = p - sk;
-        const T iu = T(1) / u;
-        if (c == 0 && k < n) sg[k] = sk;
-        const T ukc = (c == k) ? u : a[k];                   // U[k][c] for c >= k
-        a[k] = ukc;
-#pragma unroll
-        for (int i = k + 1; i < kWB; ++i) {
-            const T l = __shfl_sync(kFull, a[i], k) * iu;    // L[i][k]
-            a[i] = (c > k) ? a[i] - l * ukc : ((c == k) ? l : a[i]);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kWB; ++i)
-        if (i < n && c < n) A[i * lda + c] = a[i];
-}
-
-// Operand views for blk_mul, in the coordinates (r, s) of op(X):
-enum : int { kMFull = 0, kMUpper = 1, kMUpperUnit = 2, kMLowerUnit = 3 };
-
-template <typename T, bool TR, int MASK>
-SKL_DEV T op_at(const T* X, int ld, int r, int s)
-{
-    if (MASK == kMUpper && s < r) return T(0);
-    if (MASK == kMUpperUnit && s <= r) return s == r ? T(1) : T(0);
-    if (MASK == kMLowerUnit && s >= r) return s == r ? T(1) : T(0);
-    return TR ? X[s * ld + r] : X[r * ld + s];
-}
-
-// k range of a product term for masked operands: A upper restricts k >= i,
-// B upper / upper-unit restricts k <= c, A lower-unit restricts k <= i.
-template <int MA, int MB>
-SKL_DEV void k_range(int i0, int c0, int tr, int tc, int kk, int& klo, int& khi)
-{
-    klo = 0;
-    khi = kk;
-    if (MA == kMUpper) klo = i0;
-    if (MA == kMLowerUnit) khi = min(khi, i0 + tr);
-    if (MB == kMUpper || MB == kMUpperUnit) khi = min(khi, c0 + tc);
-    if (MB == kMLowerUnit) klo = max(klo, c0);
-}
-
-// C (m x n) = alpha * op(A) (m x kk) * op(B) (kk x n) [* diag(sB) on B's
-// rows] (+ C when ACC), row-major shared memory; 4 x 4 register tiles, one
-// per thread (m * n <= 16 * kSmallThreads); k runs only over the range the
-// operand masks leave nonzero.  Results wait for a block barrier, so C may
-// alias A or B.  With Cg set, C goes to global memory column-major (ldg)
-// instead and its diagonal also to tau.
-template <typename T, bool TA, int MA, bool TB, int MB, bool ACC = false>
-SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
-                     const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg = nullptr,
-                     int ldg = 0, T* __restrict__ tau = nullptr)
-{
-    const int ntc = (n + 3) / 4;
-    const int t = threadIdx.x;
-    const int i0 = (t / ntc) * 4, c0 = (t % ntc) * 4;
-    const bool act = i0 < m;
-    T acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[r][q] = T(0);
-    if (act) {
-        int klo, khi;
-        k_range<MA, MB>(i0, c0, 4, 4, kk, klo, khi);
-        for (int k = klo; k < khi; ++k) {
-            T av[4], bv[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) av[r] = (i0 + r < m) ? op_at<T, TA, MA>(A, lda, i0 + r, k) : T(0);
-            const T sc = sB ? sB[k] : T(1);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) bv[q] = (c0 + q < n) ? sc * op_at<T, TB, MB>(B, ldb, k, c0 + q) : T(0);
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) acc[r][q] += av[r] * bv[q];
-        }
-    }
-    __syncthreads();
-    if (act) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int i = i0 + r;
-            if (i >= m) continue;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int c = c0 + q;
-                if (c >= n) continue;
-                const T v = alpha * acc[r][q];
-                if (Cg) {
-                    Cg[i + (int64_t)c * ldg] = v;
-                    if (i == c) tau[i] = v;
-                } else if (ACC) {
-                    C[i * ldc + c] += v;
-                } else {
-                    C[i * ldc + c] = v;
-                }
-            }
-        }
-    }
-    __syncthreads();
-}
-
-// Cholesky G = R^T R (b <= 64) with X = R^{-1}: 2 x 2 blocks of 32.
-// R (upper, zeros below) over G in place; X (upper, zeros below) to Xs.
-template <typename T>
-SKL_DEV void chol_inv_blocked(T* G, int ldx, int b, const T* __restrict__ mass, T eps, T* Xs,
-                              int* bad)
-{
-    const int wid = threadIdx.x >> 5;
-    const int n1 = min(b, kWB), n2 = b - n1;
-    if (wid == 0) {
-        warp_chol32<T>(G, ldx, n1, mass, eps, G, ldx, bad);
-        __syncwarp();
-        warp_tri_inv_upper32<T>(G, ldx, n1, Xs, ldx, true);
-    }
-    __syncthreads();
-    if (n2 > 0) {
-        T* G12 = G + n1;
-        T* G21 = G + n1 * ldx;
-        T* G22 = G + n1 * ldx + n1;
-        // R12 = R11^{-T} G12 = X11^T G12
-        blk_mul<T, true, kMFull, false, kMFull>(n1, n2, n1, Xs, ldx, G12, ldx, nullptr, T(1), G12, ldx);
-        // G22 -= R12^T R12
-        blk_mul<T, true, kMFull, false, kMFull, true>(n2, n2, n1, G12, ldx, G12, ldx, nullptr, T(-1), G22, ldx);
-        if (wid == 0) {
-            warp_chol32<T>(G22, ldx, n2, mass + n1, eps, G22, ldx, bad);
-            __syncwarp();
-            warp_tri_inv_upper32<T>(G22, ldx, n2, Xs + n1 * ldx + n1, ldx, true);
-        }
-        __syncthreads();
-        // X12 = -(X11 R12) X22, formed in place in X's upper-right block
-        T* X21 = Xs + n1 * ldx;
-        T* X12 = Xs + n1;
-        blk_mul<T, false, kMFull, false, kMFull>(n1, n2, n1, Xs, ldx, G12, ldx, nullptr, T(1), X12, ldx);
-        blk_mul<T, false, kMFull, false, kMFull>(n1, n2, n2, X12, ldx, Xs + n1 * ldx + n1, ldx, nullptr,
-                                                 T(-1), X12, ldx);
-        for (int e = threadIdx.x; e < n2 * n1; e += kSmallThreads) {
-            const int i = e / n1, c = e - i * n1;
-            X21[i * ldx + c] = T(0);
-            G21[i * ldx + c] = T(0);
-        }
-        __syncthreads();
-    }
-}
-
-// Modified LU of A (b <= 64) in place (L strict lower, U upper), signs to
-// sg, and in Z: L^{-1} (strict lower, unit diagonal implied) and U^{-1}
-// (upper).  2 x 2 blocks of 32.
-template <typename T>
-SKL_DEV void mlu_inv_blocked(T* A, int ldx, int b, T* __restrict__ sg, T* Z)
-{
-    const int wid = threadIdx.x >> 5;
-    const int n1 = min(b, kWB), n2 = b - n1;
-    if (wid == 0) {
-        warp_mlu32<T>(A, ldx, n1, sg);
-        __syncwarp();
-        warp_tri_inv_unit_lower32<T>(A, ldx, n1, Z, ldx);
-        warp_tri_inv_upper32<T>(A, ldx, n1, Z, ldx, false);
-    }
-    __syncthreads();
-    if (n2 > 0) {
-        T* A12 = A + n1;
-        T* A21 = A + n1 * ldx;
-        T* A22 = A + n1 * ldx + n1;
-        T* Z12 = Z + n1;
-        T* Z21 = Z + n1 * ldx;
-        T* Z22 = Z + n1 * ldx + n1;
-        // U12 = L11^{-1} A12 ; L21 = A21 U11^{-1}
-        blk_mul<T, false, kMLowerUnit, false, kMFull>(n1, n2, n1, Z, ldx, A12, ldx, nullptr, T(1), A12, ldx);
-        blk_mul<T, false, kMFull, false, kMUpper>(n2, n1, n1, A21, ldx, Z, ldx, nullptr, T(1), A21, ldx);
-        // A22 -= L21 U12
-        blk_mul<T, false, kMFull, false, kMFull, true>(n2, n2, n1, A21, ldx, A12, ldx, nullptr, T(-1), A22, ldx);
-        if (wid == 0) {
-            warp_mlu32<T>(A22, ldx, n2, sg + n1);
-            __syncwarp();
-            warp_tri_inv_unit_lower32<T>(A22, ldx, n2, Z22, ldx);
-            warp_tri_inv_upper32<T>(A22, ldx, n2, Z22, ldx, false);
-        }
-        __syncthreads();
-        // L^{-1}_21 = -L22^{-1} (L21 L11^{-1}) ; U^{-1}_12 = -(U11^{-1} U12) U22^{-1}
-        blk_mul<T, false, kMFull, false, kMLowerUnit>(n2, n1, n1, A21, ldx, Z, ldx, nullptr, T(1), Z21, ldx);
-        blk_mul<T, false, kMUpper, false, kMFull>(n1, n2, n1, Z, ldx, A12, ldx, nullptr, T(1), Z12, ldx);
-        blk_mul<T, false, kMLowerUnit, false, kMFull>(n2, n1, n2, Z22, ldx, Z21, ldx, nullptr, T(-1), Z21, ldx);
-        blk_mul<T, false, kMFull, false, kMUpper>(n1, n2, n2, Z12, ldx, Z22, ldx, nullptr, T(-1), Z12, ldx);
-    }
-}
-
-// b x b workspace layout of the small kernels (row-major, ld = b + 4).
-template <typename T>
-size_t chol_small_smem_bytes(int b)
-{
-    return (4 * (size_t)b * (b + 4) + 2 * (size_t)b) * sizeof(T) + 256;
-}
-
-// Pass 1: R1 and X1 = R1^{-1} from G1 (column-major b x b, ldg = b).  Sets
-// *fail (1 on a Cholesky breakdown, else 0).
-template <typename T>
-__global__ void __launch_bounds__(kSmallThreads, 1)
-k_chol_small1(const T* __restrict__ G, int b, T* __restrict__ R1, T* __restrict__ X1,
-              int* __restrict__ fail)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int LDX = b + 4;
-    T* S0 = (T*)smem_raw;
-    T* S1 = S0 + (size_t)b * LDX;
-    T* mass = S1 + (size_t)b * LDX;
-    __shared__ int s_bad;
-    const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
-    if (threadIdx.x == 0) s_bad = 0;
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e % b, c = e / b;
-        S0[i * LDX + c] = G[e];
-    }
-    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = G[k * b + k];
-    __syncthreads();
-    chol_inv_blocked<T>(S0, LDX, b, mass, eps, S1, &s_bad);
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e / b, c = e % b;
-        R1[e] = S0[i * LDX + c];     // row-major b x b
-        X1[c * b + i] = S1[i * LDX + c];   // column-major (a GEMM operand)
-    }
-    if (threadIdx.x == 0) *fail = s_bad ? 1 : 0;
-}
-
-// Pass 2 and the reconstruction: from G2 (column-major), R1 (row-major) and
-// the first b rows of Q (column-major, ldq) writes W = R2^{-1} U^{-1}
-// (column-major b x b), T (ldt), tau, the panel's first b rows of A (R_H on
-// and above the diagonal, L below) and of V (unit lower L).  Does nothing if
-// pass 1 failed; sets *fail on a pass-2 breakdown (A untouched).
-template <typename T>
-__global__ void __launch_bounds__(kSmallThreads, 1)
-k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T* __restrict__ Q,
-              int64_t ldq, T* __restrict__ A, int64_t ld, int j0, T* __restrict__ V, int64_t ldv,
-              T* __restrict__ Tout, int ldt, T* __restrict__ tau_out, T* __restrict__ Wg,
-              int* __restrict__ fail)
-{
-    if (*fail) return;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int LDX = b + 4;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    T* S0 = (T*)smem_raw;                        // R1 -> R = R2 R1
-    T* S1 = S0 + (size_t)b * LDX;                // G2 -> R2 -> L^{-1} \ U^{-1}
-    T* S2 = S1 + (size_t)b * LDX;                // X2 -> W
-    T* S3 = S2 + (size_t)b * LDX;                // Q(0:b,:) -> Q1 -> L \ U
-    T* Sg = S3 + (size_t)b * LDX;
-    T* mass = Sg + b;
-    __shared__ int s_bad;
-    const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
-    if (threadIdx.x == 0) s_bad = 0;
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e % b, c = e / b;          // column-major sources
-        S1[i * LDX + c] = G[e];
-        S3[i * LDX + c] = Q[i + (int64_t)c * ldq];
-        const int r = e / b, q = e % b;          // row-major source
-        S0[r * LDX + q] = R1g[e];
-    }
-    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = T(1);
-    __syncthreads();
-    // Gershgorin distance of G2 from the identity
-    for (int i = wid; i < b; i += kSmallThreads / 32) {
-        T sabs = T(0);
-        for (int c = lane; c < b; c += 32) sabs += t_abs(S1[i * LDX + c] - (c == i ? T(1) : T(0)));
-        sabs = warp_sum(sabs);
-        if (lane == 0 && !(sabs <= T(0.5))) s_bad = 1;
-    }
-    __syncthreads();
-    if (s_bad) {
-        if (threadIdx.x == 0) *fail = 1;
-        return;
-    }
-    chol_inv_blocked<T>(S1, LDX, b, mass, eps, S2, &s_bad);    // R2 over S1, X2 -> S2
-    if (s_bad) {
-        if (threadIdx.x == 0) *fail = 1;
-        return;
-    }
-    blk_mul<T, false, kMFull, false, kMUpper>(b, b, b, S3, LDX, S2, LDX, nullptr, T(1), S3, LDX);   // Q1 = Q(0:b,:) X2
-    blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S1, LDX, S0, LDX, nullptr, T(1), S0, LDX);  // R = R2 R1
-    mlu_inv_blocked<T>(S3, LDX, b, Sg, S1);                      // Q1 - S = L U; S1 = L^{-1} \ U^{-1}
-    blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S2, LDX, S1, LDX, nullptr, T(1), S2, LDX);  // W = X2 U^{-1}
-    blk_mul<T, false, kMUpper, true, kMUpperUnit>(b, b, b, S3, LDX, S1, LDX, Sg, T(-1), nullptr, 0,
-                                                   Tout, ldt, tau_out + j0);   // T = -U S L^{-T}
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int g = e % b, c = e / b;          // column-major targets
-        Wg[e] = S2[g * LDX + c];
-        const T l = (g > c) ? S3[g * LDX + c] : T(0);
-        A[(int64_t)(j0 + g) + (int64_t)(j0 + c) * ld] = (g <= c) ? Sg[g] * S0[g * LDX + c] : l;
-        V[(int64_t)g + (int64_t)c * ldv] = (g > c) ? l : (g == c ? T(1) : T(0));
-    }
-}
-
-// A(j0+b : j0+M, j0 : j0+b) = V(b : M, :) once the panel succeeded.
-template <typename T>
-__global__ void k_chol_copy_down(const T* __restrict__ V, int64_t ldv, T* __restrict__ A, int64_t ld,
-                                 int j0, int M, int b, const int* __restrict__ fail)
-{
-    if (*fail) return;
-    const int rows = M - b;
-    const int c = blockIdx.y;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
-        A[(int64_t)(j0 + b + r) + (int64_t)(j0 + c) * ld] = V[(int64_t)(b + r) + (int64_t)c * ldv];
-}
-
 // ------------------------------------------------- Q^T c for one panel --
 // c(j0:m) <- (I - V T^T V^T) c(j0:m), FP64 accumulation.  w = V^T c: one
 // block per column of V; the update: one warp per 32 rows, z = T^T w in smem.
@@ -1358,7 +937,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
 
     // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
     // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
-    const bool use_chol = pivoting && nb <= 2 * kWB && qr_chol_enabled<T>();
+    const bool use_chol = pivoting && nb <= 64 && std::is_same<T, float>::value && qr_chol_enabled<T>();
     for (int64_t j = 0; j < mn; j += nb) {
         const int b = (int)std::min<int64_t>(nb, std::min<int64_t>(d - j, m - j));
         const bool last = (j + nb >= m) || (j + nb >= d);
@@ -1401,29 +980,8 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             cudaEvent_t t0 = tm.begin();
             const int* cf = nullptr;
             if (use_chol && !last) {
-                T* P = A + j + j * ld;
-                const size_t ssm = chol_small_smem_bytes<T>(b);
-                static bool attr_set = false;
-                if (!attr_set) {
-                    const size_t mx = chol_small_smem_bytes<T>(kMaxNb);
-                    SKL_CUDA(cudaFuncSetAttribute(k_chol_small1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-                    SKL_CUDA(cudaFuncSetAttribute(k_chol_small2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-                    attr_set = true;
-                }
-                gemm<T>(true, false, b, b, M, T(1), P, ld, P, ld, T(0), B.cg, b, B.part, B.part_cap, st);
-                k_chol_small1<T><<<1, kSmallThreads, ssm, st>>>(B.cg, b, B.cr1, B.cx1, B.chol_fail);
-                SKL_CUDA(cudaGetLastError());
-                SKL_LAUNCHED();
-                gemm<T>(false, false, M, b, b, T(1), P, ld, B.cx1, b, T(0), B.tmp, M, nullptr, 0, st);
-                gemm<T>(true, false, b, b, M, T(1), B.tmp, M, B.tmp, M, T(0), B.cg, b, B.part, B.part_cap, st);
-                k_chol_small2<T><<<1, kSmallThreads, ssm, st>>>(B.cg, b, B.cr1, B.tmp, M, A, ld, jj, B.V, m,
-                                                                B.Tm, nb, tau, B.cw, B.chol_fail);
-                SKL_CUDA(cudaGetLastError());
-                SKL_LAUNCHED();
-                gemm<T>(false, false, M - b, b, b, T(1), B.tmp + b, M, B.cw, b, T(0), B.V + b, m, nullptr, 0, st);
-                dim3 gc((unsigned)std::max<int64_t>(1, std::min<int64_t>((M - b + 255) / 256, 64)), b);
-                k_chol_copy_down<T><<<gc, 256, 0, st>>>(B.V, m, A, ld, jj, M, b, B.chol_fail);
-                SKL_LAUNCHED();
+                chol_panel<T>(A + j + j * ld, ld, M, b, jj, A, B.cg, B.cr1, B.cx1, B.cw, B.tmp, B.V, m,
+                              B.Tm, nb, tau, B.part, B.part_cap, B.chol_fail, st);
                 cf = B.chol_fail;
             }
             void* args[] = {&A, &ld, &jj, (void*)&M, (void*)&b, &R, &tau_p, &Tm, &ldt, &V,

@@ -112,6 +112,16 @@ int64_t dht_length(int64_t n, int wisdom);
 size_t dht_scratch_bytes(int64_t N, int precision);
 // Load the DHT kernels' module on the current device (one-time set-up).
 void dht_load_kernels();
+
+// ---------------------------------------------------------- k_qr_chol.cu --
+// CholeskyQR2 + Householder reconstruction of one QR panel P (M x b) =
+// A(j0:, j0:j0+b) (FP32 only): V, T, tau and the panel of A on success;
+// *fail = 1 and A untouched otherwise.  cg, cr1, cx1, cw: b x b scratch;
+// tmp: M x b; part: split-K partials.
+template <typename T>
+void chol_panel(T* P, int64_t ld, int M, int b, int j0, T* A, T* cg, T* cr1, T* cx1, T* cw, T* tmp,
+                T* V, int64_t ldv, T* Tm, int ldt, T* tau, T* part, int64_t part_cap, int* fail,
+                cudaStream_t st);
 template <typename T>
 void dht_hash(const double* A, int64_t lda, int64_t n, int64_t d, const double* D, int64_t N,
               const int* bptr, const unsigned* bent, int k, int64_t m, T* SA, int64_t ld,
