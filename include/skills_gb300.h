@@ -144,6 +144,20 @@ skl_status skl_sparse_solve_device(const skl_csc* A_dev, const double* b_dev, do
 skl_status skl_dense_solve(const double* A, int64_t lda, int64_t n, int64_t d,
                            const double* b, double* x, const skl_opts* opts, skl_info* info);
 
+/* nprob independent sparse problems (host buffers, each as for
+ * skl_sparse_solve) with one set of options.  No counterpart in the reference
+ * (it solves one problem per call); it serves batched workloads of many small
+ * problems, which a single solve cannot keep the GPU busy with.  The hashing
+ * of every problem is drawn in problem order exactly as a loop of
+ * skl_sparse_solve calls with the same options would draw it, so each x[p] is
+ * bit-identical to that loop's; the problems then run concurrently on worker
+ * threads, each with its own stream (SKILLS_BATCH_STREAMS, default 8;
+ * opts->stream is not used).  info[p] and status[p] (both optional) per
+ * problem; the return value is the first failing problem's status. */
+skl_status skl_batched_sparse_solve(int64_t nprob, const skl_csc* A, const double* const* b,
+                                    double* const* x, const skl_opts* opts, skl_info* info,
+                                    skl_status* status);
+
 /* Same with A, b, x in device memory. */
 skl_status skl_dense_solve_device(const double* A_dev, int64_t lda, int64_t n, int64_t d,
                                   const double* b_dev, double* x_dev, const skl_opts* opts,

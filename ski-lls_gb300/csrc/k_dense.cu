@@ -391,8 +391,7 @@ static void launch_dht(const double* A, int64_t lda, int64_t n, int64_t d, const
     const double alpha_v = (1.0 / std::sqrt((double)k)) * (1.0 / std::sqrt((double)k));
     unsigned grid = (unsigned)std::min<int64_t>(d, 152);
     if (in_smem) {
-        SKL_CUDA(cudaFuncSetAttribute(k_dht_hash<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)need));
+        allow_max_dynamic_smem((const void*)k_dht_hash<T>);
         k_dht_hash<T><<<grid, kFftThreads, need, st>>>(A, lda, (int)n, (int)d, D, P, scale, bptr,
                                                         bent, (int)m, alpha_v, SA, ld, Yout, ldy,
                                                         nullptr);

@@ -359,6 +359,25 @@ __global__ void k_hash_keys(const unsigned* __restrict__ hidx, int64_t nk, int k
     }
 }
 
+// Every hashed row must lie in [0, m): the bucket build and the sketch use
+// them as addresses.  Flags bit 16 of *status otherwise.
+__global__ void k_check_hash_rows(const unsigned* __restrict__ hidx, int64_t nk, unsigned m,
+                                  unsigned* __restrict__ status)
+{
+    bool bad = false;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nk;
+         q += (int64_t)gridDim.x * blockDim.x)
+        bad = bad || (hidx[q] & 0x7fffffffu) >= m;
+    if (bad) atomicOr(status, 16u);
+}
+
+void check_hash_rows(const unsigned* hidx, int64_t nk, int64_t m, unsigned* status, cudaStream_t st)
+{
+    if (nk <= 0) return;
+    k_check_hash_rows<<<grid_for(nk, 256), 256, 0, st>>>(hidx, nk, (unsigned)m, status);
+    SKL_LAUNCHED();
+}
+
 size_t build_buckets_scratch_ints(int64_t m, int64_t nk)
 {
     size_t s = (size_t)(m + 1) + 4 * (size_t)nk;

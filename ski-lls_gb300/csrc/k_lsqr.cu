@@ -668,7 +668,7 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     if (stage) rpb = (int)std::max<int64_t>(kRowsPerBlock, (P.n + 152 * 4 - 1) / (152 * 4));
     const unsigned g = (unsigned)((P.n + rpb - 1) / rpb);
 #define SPMV_N(LL) do { \
-        if (smem > 48 * 1024) SKL_CUDA(cudaFuncSetAttribute(k_spmv_n_csr<MIXED, LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_spmv_n_csr<MIXED, LL>); \
         k_spmv_n_csr<MIXED, LL><<<g, kLThreads, smem, st>>>(P.rp, P.ci, (const V*)P.cx, (int)P.n, rpb, (const V*)B.z, stage, B.uh, (V*)B.us, B.S, B.partials); \
     } while (0)
     if (L == 32) SPMV_N(32);

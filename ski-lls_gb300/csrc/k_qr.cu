@@ -851,7 +851,8 @@ template <typename T>
 static void launch_cluster(const void* fn, dim3 block, size_t smem, cudaStream_t st, void** args)
 {
     SKL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    SKL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem(fn);
+    (void)smem;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kCluster, 1, 1);
     cfg.blockDim = block;

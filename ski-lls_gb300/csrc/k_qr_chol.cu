@@ -393,13 +393,8 @@ void chol_panel(T* P, int64_t ld, int M, int b, int j0, T* A, T* cg, T* cr1, T* 
                 cudaStream_t st)
 {
     const size_t ssm = chol_small_smem_bytes<T>(b);
-    static bool attr_set = false;
-    if (!attr_set) {
-        const size_t mx = chol_small_smem_bytes<T>(kMaxSmall);
-        SKL_CUDA(cudaFuncSetAttribute(k_chol_small1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-        SKL_CUDA(cudaFuncSetAttribute(k_chol_small2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-        attr_set = true;
-    }
+    allow_max_dynamic_smem((const void*)k_chol_small1<T>);
+    allow_max_dynamic_smem((const void*)k_chol_small2<T>);
     gemm<T>(true, false, b, b, M, T(1), P, ld, P, ld, T(0), cg, b, part, part_cap, st);
     k_chol_small1<T><<<1, kSmallThreads, ssm, st>>>(cg, b, cr1, cx1, fail);
     SKL_CUDA(cudaGetLastError());

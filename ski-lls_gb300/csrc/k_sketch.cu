@@ -147,8 +147,7 @@ void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, in
     const double isk = 1.0 / std::sqrt((double)k);
     size_t smem = (size_t)m * sizeof(unsigned long long);
     if (smem + 1024 <= smem_optin()) {
-        SKL_CUDA(cudaFuncSetAttribute(k_sketch_sparse_smem<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_dynamic_smem((const void*)k_sketch_sparse_smem<T>);
         k_sketch_sparse_smem<T><<<(unsigned)d, kSketchThreads, smem, st>>>(
             cp, ri, Ax, hidx, k, (int)m, SA, ld, equilibrate, isk, colnorm, colscale);
         SKL_LAUNCHED();

@@ -20,6 +20,7 @@
 #include <ctime>
 #include <mutex>
 #include <thread>
+#include <atomic>
 #include <type_traits>
 #include <vector>
 
@@ -53,8 +54,23 @@ static int trace_enabled()
     return v;
 }
 
+void allow_max_dynamic_smem(const void* fn)
+{
+    int dev = 0, optin = 0;
+    SKL_CUDA(cudaGetDevice(&dev));
+    SKL_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    SKL_CUDA(cudaFuncGetAttributes(&fa, fn));
+    SKL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin - (int)fa.sharedSizeBytes));
+}
+
+// Phase boundary: a launch that failed (bad configuration) is reported here
+// instead of letting later phases run on unwritten buffers.  With
+// SKILLS_TRACE=1 also synchronises and prints the phase.
 void trace_phase(cudaStream_t st, const char* name)
 {
+    SKL_CUDA(cudaPeekAtLastError());
     if (!trace_enabled()) return;
     static auto t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamSynchronize(st);
@@ -125,9 +141,9 @@ void Arena::release()
 
 // ------------------------------------------------------------ contexts ----
 static std::mutex g_ctx_mu;
-static std::vector<Context*> g_ctx;
+static std::vector<std::vector<Context*>> g_ctx;   // [device][slot]
 
-Context& context(int device)
+Context& context(int device, int slot)
 {
     std::lock_guard<std::mutex> lk(g_ctx_mu);
     int ndev = 0;
@@ -136,9 +152,10 @@ Context& context(int device)
         fail(SKL_ERR_NO_DEVICE, "no CUDA device available");
     }
     if (device < 0 || device >= ndev) fail(SKL_ERR_INVALID, "device ordinal out of range");
-    if ((int)g_ctx.size() < ndev) g_ctx.resize(ndev, nullptr);
+    if ((int)g_ctx.size() < ndev) g_ctx.resize(ndev);
+    if ((int)g_ctx[device].size() <= slot) g_ctx[device].resize(slot + 1, nullptr);
     SKL_CUDA(cudaSetDevice(device));
-    if (!g_ctx[device]) {
+    if (!g_ctx[device][slot]) {
         cudaDeviceProp prop;
         SKL_CUDA(cudaGetDeviceProperties(&prop, device));
         if (prop.major != 10)
@@ -151,27 +168,28 @@ Context& context(int device)
         SKL_CUDA(cudaMemset(c->dev_status, 0, 256));
         c->host_pinned_bytes = 4096;
         SKL_CUDA(cudaMallocHost(&c->host_pinned, c->host_pinned_bytes));
-        g_ctx[device] = c;
+        g_ctx[device][slot] = c;
     }
-    return *g_ctx[device];
+    return *g_ctx[device][slot];
 }
 
 void release_all_contexts()
 {
     std::lock_guard<std::mutex> lk(g_ctx_mu);
     for (size_t d = 0; d < g_ctx.size(); ++d) {
-        Context* c = g_ctx[d];
-        if (!c) continue;
-        cudaSetDevice((int)d);
-        cudaStreamSynchronize(c->stream);
-        c->arena.release();
-        c->staging.release();
-        for (auto& e : c->ev) cudaEventDestroy(e);
-        cudaFree(c->dev_status);
-        cudaFreeHost(c->host_pinned);
-        cudaStreamDestroy(c->stream);
-        delete c;
-        g_ctx[d] = nullptr;
+        for (Context*& c : g_ctx[d]) {
+            if (!c) continue;
+            cudaSetDevice((int)d);
+            cudaStreamSynchronize(c->stream);
+            c->arena.release();
+            c->staging.release();
+            for (auto& e : c->ev) cudaEventDestroy(e);
+            cudaFree(c->dev_status);
+            cudaFreeHost(c->host_pinned);
+            cudaStreamDestroy(c->stream);
+            delete c;
+            c = nullptr;
+        }
     }
 }
 
@@ -291,15 +309,17 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
         split_values(in.Ax, nnz, rx2, st);
     }
     // ---- hash stream (host) -> device buckets ----
-    if (hash_thread) {
-        hash_thread->join();
-        SKL_CUDA(cudaMemcpyAsync(hidx, host_hidx->data(), n * k * sizeof(unsigned),
-                                 cudaMemcpyHostToDevice, st));
-    }
+    if (hash_thread) hash_thread->join();
+    if (!host_hidx || (int64_t)host_hidx->size() != n * k)
+        fail(SKL_ERR_INVALID, "hash stream missing for the sparse sketch");
+    SKL_CUDA(cudaMemcpyAsync(hidx, host_hidx->data(), n * k * sizeof(unsigned),
+                             cudaMemcpyHostToDevice, st));
+    check_hash_rows(hidx, n * k, m, C.dev_status, st);
     unsigned bad = read_status(C, st);
     if (bad & 1u) fail(SKL_ERR_INVALID, "CSC column pointers are not a valid structure");
     if (bad & 2u) fail(SKL_ERR_INVALID, "CSC row index out of range");
     if (bad & 4u) fail(SKL_ERR_NONFINITE, "A contains NaN or Inf");
+    if (bad & 16u) fail(SKL_ERR_INVALID, "hash row index out of range");
     trace_phase(st, "csr+validate");
     build_buckets(hidx, n, (int)k, m, bptr, bent, (int*)work, st);
     trace_phase(st, "buckets");
@@ -472,42 +492,14 @@ static void validate_csc_header(const skl_csc* A)
     if (A->m < A->n) fail(SKL_ERR_NOT_OVERDETERMINED, "Matrix is not overdetermined.");
 }
 
-static void sparse_solve_common(const skl_csc* A, const double* b, double* x, const skl_opts* opts,
-                                skl_info* info, bool host)
+// One sparse solve on context C and stream st.  The hash stream arrives
+// either from a worker thread still filling hh (single solves overlap it with
+// the upload and validation) or already filled (th = nullptr).
+static void sparse_solve_core(Context& C, cudaStream_t st, const skl_csc* A, const double* b,
+                              double* x, const skl_opts& o, skl_info& inf, bool host,
+                              std::thread* th, std::vector<uint32_t>* hh)
 {
-    skl_opts o;
-    if (opts) o = *opts;
-    else fill_default(&o);
-    check_opts(o);
-    validate_csc_header(A);
-    if (!b || !x) fail(SKL_ERR_INVALID, "b or x is null");
-    skl_info inf;
-    std::memset(&inf, 0, sizeof inf);
     const int64_t n = A->m, d = A->n;
-    if (d == 0) {
-        if (info) *info = inf;
-        return;
-    }
-    Context& C = context(o.device);
-    reset_launch_count();
-    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : C.stream;
-    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
-    if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
-    // host hash stream in a worker thread (serial Fisher-Yates)
-    std::vector<uint32_t> hh((size_t)(n * o.k));
-    double hash_ms = 0.0;
-    std::thread th([&]() {
-        auto t0 = std::chrono::steady_clock::now();
-        if (o.seed_mode) rng_srand(o.seed);
-        rng_lock();
-        gen_hash_packed(m, n, o.k, hh.data());
-        rng_unlock();
-        hash_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    });
-    struct Joiner {
-        std::thread& t;
-        ~Joiner() { if (t.joinable()) t.join(); }
-    } joiner{th};
     SparseDev in;
     in.n = n;
     in.d = d;
@@ -536,9 +528,9 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
         SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
         in.Ap = Ap; in.Ai = Ai; in.Ax = Ax; in.b = bd; in.nnz = nnz;
         if (o.precision == SKL_PREC_MIXED)
-            sparse_pipeline<float>(C, st, in, xd, o, inf, true, &th, &hh);
+            sparse_pipeline<float>(C, st, in, xd, o, inf, true, th, hh);
         else
-            sparse_pipeline<double>(C, st, in, xd, o, inf, true, &th, &hh);
+            sparse_pipeline<double>(C, st, in, xd, o, inf, true, th, hh);
         SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
     } else {
@@ -547,15 +539,137 @@ static void sparse_solve_common(const skl_csc* A, const double* b, double* x, co
         nnz = *(int64_t*)C.host_pinned;
         in.Ap = A->p; in.Ai = A->i; in.Ax = A->x; in.b = b; in.nnz = nnz;
         if (o.precision == SKL_PREC_MIXED)
-            sparse_pipeline<float>(C, st, in, x, o, inf, false, &th, &hh);
+            sparse_pipeline<float>(C, st, in, x, o, inf, false, th, hh);
         else
-            sparse_pipeline<double>(C, st, in, x, o, inf, false, &th, &hh);
+            sparse_pipeline<double>(C, st, in, x, o, inf, false, th, hh);
     }
+}
+
+static void sparse_solve_common(const skl_csc* A, const double* b, double* x, const skl_opts* opts,
+                                skl_info* info, bool host)
+{
+    skl_opts o;
+    if (opts) o = *opts;
+    else fill_default(&o);
+    check_opts(o);
+    validate_csc_header(A);
+    if (!b || !x) fail(SKL_ERR_INVALID, "b or x is null");
+    skl_info inf;
+    std::memset(&inf, 0, sizeof inf);
+    const int64_t n = A->m, d = A->n;
+    if (d == 0) {
+        if (info) *info = inf;
+        return;
+    }
+    Context& C = context(o.device, 0);
+    reset_launch_count();
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : C.stream;
+    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+    if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
+    // host hash stream in a worker thread (serial Fisher-Yates)
+    std::vector<uint32_t> hh((size_t)(n * o.k));
+    double hash_ms = 0.0;
+    std::thread th([&]() {
+        auto t0 = std::chrono::steady_clock::now();
+        if (o.seed_mode) rng_srand(o.seed);
+        rng_lock();
+        gen_hash_packed(m, n, o.k, hh.data());
+        rng_unlock();
+        hash_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    });
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() { if (t.joinable()) t.join(); }
+    } joiner{th};
+    sparse_solve_core(C, st, A, b, x, o, inf, host, &th, &hh);
     inf.t_host_hash_ms = hash_ms;
     inf.kernel_launches = launches_since_reset();
     if (info) *info = inf;
 }
 
+// Batched sparse solves (host buffers): hashing drawn here in problem order,
+// exactly as a loop of skl_sparse_solve calls with the same options would draw
+// it, then the problems spread over worker threads, each with its own device
+// context and stream.
+static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double* const* b,
+                                  double* const* x, const skl_opts* opts, skl_info* info,
+                                  skl_status* status)
+{
+    if (nprob < 0) fail(SKL_ERR_INVALID, "nprob < 0");
+    if (nprob == 0) return;
+    if (!A || !b || !x) fail(SKL_ERR_INVALID, "skl_batched_sparse_solve: null array");
+    skl_opts o;
+    if (opts) o = *opts;
+    else fill_default(&o);
+    check_opts(o);
+    for (int64_t p = 0; p < nprob; ++p) {
+        validate_csc_header(&A[p]);
+        if (!b[p] || !x[p]) fail(SKL_ERR_INVALID, "skl_batched_sparse_solve: b or x is null");
+        if (A[p].n > 0 && o.k > (int64_t)std::ceil((double)A[p].n * o.gamma))
+            fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
+    }
+    // hash streams, in problem order
+    std::vector<std::vector<uint32_t>> hh((size_t)nprob);
+    std::vector<double> hash_ms((size_t)nprob, 0.0);
+    for (int64_t p = 0; p < nprob; ++p) {
+        const int64_t n = A[p].m, d = A[p].n;
+        if (d == 0) continue;
+        const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+        hh[(size_t)p].resize((size_t)(n * o.k));
+        auto t0 = std::chrono::steady_clock::now();
+        if (o.seed_mode) rng_srand(o.seed);
+        rng_lock();
+        gen_hash_packed(m, n, o.k, hh[(size_t)p].data());
+        rng_unlock();
+        hash_ms[(size_t)p] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    int workers = 8;
+    if (const char* e = std::getenv("SKILLS_BATCH_STREAMS")) workers = std::max(1, std::atoi(e));
+    workers = (int)std::min<int64_t>(workers, nprob);
+    std::atomic<int64_t> next{0};
+    std::mutex err_mu;
+    skl_status first_status = SKL_OK;
+    std::string first_msg;
+    auto work = [&](int slot) {
+        for (;;) {
+            const int64_t p = next.fetch_add(1);
+            if (p >= nprob) break;
+            skl_info inf;
+            std::memset(&inf, 0, sizeof inf);
+            skl_status rc = SKL_OK;
+            std::string msg;
+            try {
+                if (A[p].n > 0) {
+                    Context& C = context(o.device, 1 + slot);
+                    reset_launch_count();
+                    sparse_solve_core(C, C.stream, &A[p], b[p], x[p], o, inf, true, nullptr,
+                                      &hh[(size_t)p]);
+                    inf.t_host_hash_ms = hash_ms[(size_t)p];
+                    inf.kernel_launches = launches_since_reset();
+                }
+            } catch (const Error& e) {
+                rc = e.status;
+                msg = e.what();
+            } catch (const std::exception& e) {
+                rc = SKL_ERR_CUDA;
+                msg = e.what();
+            }
+            if (info) info[p] = inf;
+            if (status) status[p] = rc;
+            if (rc != SKL_OK) {
+                std::lock_guard<std::mutex> lk(err_mu);
+                if (first_status == SKL_OK) {
+                    first_status = rc;
+                    first_msg = "problem " + std::to_string(p) + ": " + msg;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 0; w < workers; ++w) pool.emplace_back(work, w);
+    for (auto& t : pool) t.join();
+    if (first_status != SKL_OK) fail(first_status, first_msg);
+}
 
 // --------------------------------------------------------- dense solve ---
 // ls_dense_hashing_blendenpik (src/ls_dense_hashing_blendenpik.cpp:23-149) and,
@@ -860,6 +974,13 @@ skl_status skl_sparse_solve_device(const skl_csc* A, const double* b, double* x,
                                    const skl_opts* opts, skl_info* info)
 {
     return guarded([&] { sparse_solve_common(A, b, x, opts, info, false); });
+}
+
+skl_status skl_batched_sparse_solve(int64_t nprob, const skl_csc* A, const double* const* b,
+                                    double* const* x, const skl_opts* opts, skl_info* info,
+                                    skl_status* status)
+{
+    return guarded([&] { batched_sparse_common(nprob, A, b, x, opts, info, status); });
 }
 
 skl_status skl_dense_solve(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,

@@ -26,6 +26,12 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line);
 // prints the phase name and the elapsed host time to stderr.
 void trace_phase(cudaStream_t st, const char* name);
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum (less
+// its static shared memory).  Always the same value, so concurrent solves on
+// several host threads can call it before any launch without lowering the
+// limit under one another.
+void allow_max_dynamic_smem(const void* fn);
+
 // Kernel launch accounting (counted per solve, reported in skl_info).
 void note_launch();
 int64_t launches_since_reset();
@@ -73,7 +79,8 @@ struct Context {
     size_t host_pinned_bytes = 0;
 };
 
-Context& context(int device);
+// Device context `slot` of a device (slot 0: single solves; 1..: batched workers).
+Context& context(int device, int slot = 0);
 // Runs fn and converts exceptions into an skl_status (C ABI guard).
 skl_status run_guarded(void (*fn)(void*), void* arg);
 void release_all_contexts();
@@ -90,6 +97,8 @@ void csc_narrow(const int64_t* Ap, const int64_t* Ai, const double* Ax, int64_t 
 size_t build_csr_scratch_ints(int64_t nrow, int64_t nnz);
 void build_csr(const int* cp, const int* ri, const double* Ax, int64_t nrow, int64_t ncol,
                int64_t nnz, int* rp, int* ci, double* cx, int* scratch, cudaStream_t st);
+// Flags bit 16 of *status if a hashed row index is outside [0, m).
+void check_hash_rows(const unsigned* hidx, int64_t nk, int64_t m, unsigned* status, cudaStream_t st);
 size_t build_buckets_scratch_ints(int64_t m, int64_t nk);
 void build_buckets(const unsigned* hidx, int64_t n, int k, int64_t m, int* bptr, unsigned* bent,
                    int* scratch, cudaStream_t st);

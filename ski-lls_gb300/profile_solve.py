@@ -23,9 +23,20 @@ def main():
     reps = int(sys.argv[3]) if len(sys.argv) > 3 else 1
     w = synthetic.WORKLOADS[name]
     A, b = w["gen"]()
+    dev = torch.device("cuda", 0)
+    if w["kind"] == "dense":
+        n, d = A.shape
+        Ad = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).to(dev)
+        bd = torch.from_numpy(b).to(dev)
+        xd = torch.zeros(d, dtype=torch.float64, device=dev)
+        for _ in range(reps):
+            info = skl.dense_solve_device(n, d, Ad.data_ptr(), n, bd.data_ptr(), xd.data_ptr(),
+                                          w["gamma"], w["k"], precision=prec, seed=1,
+                                          it_tol=1e-10, profile=1)
+        print(json.dumps(info.as_dict()))
+        return
     A = A.tocsc()
     n, d = A.shape
-    dev = torch.device("cuda", 0)
     Ap = torch.from_numpy(A.indptr.astype(np.int64)).to(dev)
     Ai = torch.from_numpy(A.indices.astype(np.int64)).to(dev)
     Ax = torch.from_numpy(A.data).to(dev)

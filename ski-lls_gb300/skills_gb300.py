@@ -106,6 +106,9 @@ def lib():
             f.argtypes = [ctypes.POINTER(SklCsc), vp, vp, ctypes.POINTER(SklOpts),
                           ctypes.POINTER(SklInfo)]
             f.restype = ctypes.c_int
+        L.skl_batched_sparse_solve.argtypes = [i64, ctypes.POINTER(SklCsc), vp, vp,
+                                               ctypes.POINTER(SklOpts), ctypes.POINTER(SklInfo), vp]
+        L.skl_batched_sparse_solve.restype = ctypes.c_int
         for name in ("skl_dense_solve", "skl_dense_solve_device"):
             f = getattr(L, name)
             f.argtypes = [vp, i64, i64, i64, vp, vp, ctypes.POINTER(SklOpts),
@@ -228,6 +231,60 @@ def sparse_solve_device(n, d, p_ptr, i_ptr, x_ptr, b_ptr, xout_ptr, nnz, gamma, 
                                          ctypes.c_void_p(xout_ptr), ctypes.byref(o),
                                          ctypes.byref(info)))
     return info
+
+
+def dense_solve_device(n, d, a_ptr, lda, b_ptr, xout_ptr, gamma, k, *, precision="mixed",
+                       seed=1, rcond=1e-10, it_tol=IT_TOL, max_it=MAX_IT, abs_tol=ABS_TOL,
+                       use_cpqr=1, stream=None, profile=0, device=0) -> SklInfo:
+    """skl_dense_solve_device on device pointers (column-major A, lda >= n)."""
+    o = default_opts()
+    o.gamma, o.k, o.abs_tol, o.it_tol, o.max_it, o.rcond = gamma, k, abs_tol, it_tol, max_it, rcond
+    o.precision = PREC[precision]
+    o.seed_mode, o.seed = 1, int(seed) & 0xFFFFFFFF
+    o.use_cpqr, o.device, o.stream, o.profile = use_cpqr, device, stream, profile
+    info = SklInfo()
+    _check(lib().skl_dense_solve_device(ctypes.c_void_p(a_ptr), lda, n, d, ctypes.c_void_p(b_ptr),
+                                        ctypes.c_void_p(xout_ptr), ctypes.byref(o),
+                                        ctypes.byref(info)))
+    return info
+
+
+def batched_sparse_spqr(problems, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, *,
+                        abs_tol=ABS_TOL, it_tol=IT_TOL, max_it=MAX_IT, precision="mixed",
+                        seed=None, device=0):
+    """skl_batched_sparse_solve over [(A, b), ...] (scipy CSC, host arrays).
+    Returns (list of x, list of SklInfo, list of status codes)."""
+    nprob = len(problems)
+    keep = []
+    cscs = (SklCsc * max(nprob, 1))()
+    bptr = (ctypes.c_void_p * max(nprob, 1))()
+    xptr = (ctypes.c_void_p * max(nprob, 1))()
+    xs = []
+    for p, (A, b) in enumerate(problems):
+        A = A.tocsc()
+        ip = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        ii = np.ascontiguousarray(A.indices, dtype=np.int64)
+        xx = np.ascontiguousarray(A.data, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(A.shape[1], dtype=np.float64)
+        keep += [ip, ii, xx, bb]
+        xs.append(x)
+        cscs[p] = SklCsc(A.shape[0], A.shape[1], int(A.nnz), _ptr(ip).value, _ptr(ii).value,
+                         _ptr(xx).value)
+        bptr[p] = _ptr(bb).value
+        xptr[p] = _ptr(x).value
+    o = default_opts()
+    o.gamma, o.k, o.abs_tol, o.it_tol, o.max_it = gamma, k, abs_tol, it_tol, max_it
+    o.precision = PREC[precision]
+    o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    o.device = device
+    infos = (SklInfo * max(nprob, 1))()
+    status = (ctypes.c_int * max(nprob, 1))()
+    rc = lib().skl_batched_sparse_solve(nprob, cscs, ctypes.cast(bptr, ctypes.c_void_p),
+                                        ctypes.cast(xptr, ctypes.c_void_p), ctypes.byref(o),
+                                        infos, ctypes.cast(status, ctypes.c_void_p))
+    _check(rc)
+    return xs, [infos[p] for p in range(nprob)], [status[p] for p in range(nprob)]
 
 
 def ls_dense_hashing_blendenpik(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN,
