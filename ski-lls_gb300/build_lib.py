@@ -52,5 +52,28 @@ def build(verbose=False, jobs=None):
     return LIB
 
 
+CLI_DIR = os.path.join(HERE, "cli")
+CLI_TOOLS = ("ls_qr", "ls_blendenpik_hashing")
+
+
+def build_cli():
+    """Command-line drivers (cli/*.cpp) over the C++ drop-in header, linked
+    against the library; binaries next to it in lib/."""
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(NVCC)), "include")
+    out = []
+    for tool in CLI_TOOLS:
+        exe = os.path.join(OUT_DIR, tool)
+        cmd = ["g++", "-std=c++17", "-O2", "-I", inc, "-I", CLI_DIR, "-I", cuda_inc,
+               os.path.join(CLI_DIR, tool + ".cpp"), "-o", exe, "-L", OUT_DIR, "-lskills_gb300",
+               "-Wl,-rpath," + OUT_DIR]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed for {tool}:\n" + r.stdout + r.stderr)
+        out.append(exe)
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
+    print(build_cli())
