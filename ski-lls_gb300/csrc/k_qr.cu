@@ -794,6 +794,7 @@ struct QrBuffers {
     T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *tmp;
     int *sel, *plan_src, *plan_dst, *plan_n, *chol_fail;
     T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
+    T* R12;                   // b x (d-j): rows j..j+b of the updated trailing matrix
     double *qw;
     int64_t part_cap, tmp_rows;
 };
@@ -833,6 +834,7 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.cr1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.cx1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.cw = (T*)take((size_t)p.nb * p.nb * sizeof(T));
+    B.R12 = (T*)take((size_t)p.nb * d * sizeof(T));
     B.qw = (double*)take(kMaxNb * sizeof(double));
     if (total) *total = off;
     return B;
@@ -939,23 +941,65 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
     // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
     const bool use_chol = pivoting && nb <= 64 && std::is_same<T, float>::value && qr_chol_enabled<T>();
+
+    // Two streams.  After W and Z of panel j the sample work (Y downdate, the
+    // sample QRP of panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs
+    // on a high-priority side stream while the main stream applies the big
+    // trailing update and Q^T c; panel j+1's permutation waits for the side
+    // stream's event.  (R12 is formed separately because the update rewrites
+    // A12 concurrently.)
+    cudaStream_t side = nullptr;
+    cudaEvent_t evR = nullptr, evY = nullptr, evG = nullptr;
+    if (pivoting) {
+        int lo = 0, hi = 0;
+        SKL_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        SKL_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+        SKL_CUDA(cudaEventCreateWithFlags(&evR, cudaEventDisableTiming));
+        SKL_CUDA(cudaEventCreateWithFlags(&evY, cudaEventDisableTiming));
+        SKL_CUDA(cudaEventCreateWithFlags(&evG, cudaEventDisableTiming));
+    }
+    struct StreamGuard {
+        cudaStream_t s;
+        cudaEvent_t a, b, c;
+        ~StreamGuard()
+        {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+            if (c) cudaEventDestroy(c);
+            if (s) cudaStreamDestroy(s);
+        }
+    } guard{side, evR, evY, evG};
+    QrTimer tms{qr_prof, {}, {}, 0, side};
+    bool side_pending = false;
+
+    auto launch_yqrp = [&](int64_t j, int b, int N, cudaStream_t s, QrTimer& t) {
+        int jj = (int)j;
+        int ldy = nbp;
+        const T* Yc = B.Y;
+        int* sel = B.sel;
+        int nbv = nbp;
+        void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel};
+        cudaEvent_t t0 = t.begin();
+        launch_cluster<T>((const void*)k_yqrp<T>, dim3(kQrThreads), ysm_max, s, args);
+        t.end(0, t0);
+    };
+
     for (int64_t j = 0; j < mn; j += nb) {
         const int b = (int)std::min<int64_t>(nb, std::min<int64_t>(d - j, m - j));
         const bool last = (j + nb >= m) || (j + nb >= d);
         const int M = (int)(m - j);
         const int N = (int)(d - j);
         trace_phase(st, "qr: panel start");
+        if (side_pending) {
+            // the sample QRP of this panel (evY) before the permutation; the
+            // side stream's last use of V (evG) before the panel rewrites it
+            SKL_CUDA(cudaStreamWaitEvent(st, evY, 0));
+        }
         if (pivoting && !last) {
             int jj = (int)j;
-            int ldy = nbp;
-            const T* Yc = B.Y;
-            int* sel = B.sel;
-            void* args[] = {(void*)&Yc, &ldy, (void*)&nbp, &jj, (void*)&N, (void*)&b, &sel};
-            cudaEvent_t t0 = tm.begin();
-            launch_cluster<T>((const void*)k_yqrp<T>, dim3(kQrThreads), ysm_max, st, args);
-            tm.end(0, t0);
+            if (j == 0) launch_yqrp(j, b, N, st, tm);
             trace_phase(st, "qr: yqrp");
-            t0 = tm.begin();
+            cudaEvent_t t0 = tm.begin();
             k_perm_plan<<<1, 32, 0, st>>>(B.sel, b, N, B.plan_src, B.plan_dst, B.plan_n, status);
             SKL_LAUNCHED();
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
@@ -978,6 +1022,10 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             T* Yp = pivoting ? B.Y : nullptr;
             int ldy = nbp;
             int pp = pivoting ? 1 : 0;
+            if (side_pending) {
+                SKL_CUDA(cudaStreamWaitEvent(st, evG, 0));
+                side_pending = false;
+            }
             cudaEvent_t t0 = tm.begin();
             const int* cf = nullptr;
             if (use_chol && !last) {
@@ -991,6 +1039,64 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             tm.end(2, t0);
             trace_phase(st, "qr: panel");
         }
+        const int N2 = N - b;
+        T* Atr = A + j + (j + b) * ld;
+        if (N2 > 0) {
+            // W = V^T A_trail ; Z = T^T W
+            cudaEvent_t t0 = tm.begin();
+            gemm<T>(true, false, b, N2, M, T(1), B.V, m, Atr, ld, T(0), B.W, b, B.part,
+                    B.part_cap, st);
+            tm.end(4, t0);
+            t0 = tm.begin();
+            gemm<T>(true, false, b, N2, b, T(1), B.Tm, nb, B.W, b, T(0), B.Z, b, nullptr, 0, st);
+            tm.end(5, t0);
+        }
+        if (pivoting && !last) {
+            // R12 = A12 - V1 Z (rows j..j+b of the updated trailing matrix)
+            if (N2 > 0) {
+                k_copy_block<T><<<64, 256, 0, st>>>(Atr, ld, B.R12, b, b, N2);
+                SKL_LAUNCHED();
+                gemm<T>(false, false, b, N2, b, T(-1), B.V, m, B.Z, b, T(1), B.R12, b, nullptr, 0, st);
+            }
+            SKL_CUDA(cudaEventRecord(evR, st));
+            SKL_CUDA(cudaStreamWaitEvent(side, evR, 0));
+            // side: GU = G(:, j:m) V ; GUT = GU T ; B = G1 - GUT U11^T ;
+            // Y2 -= B R12 ; the next sample QRP (evY) ; G(:, j:m) -= GUT V^T,
+            // which only the next downdate needs (evG)
+            cudaEvent_t t0 = tms.begin();
+            T* Gj = B.G + j * nbp;
+            gemm<T>(false, false, nbp, b, M, T(1), Gj, nbp, B.V, m, T(0), B.GU, nbp, B.part,
+                    B.part_cap, side);
+            gemm<T>(false, false, nbp, b, b, T(1), B.GU, nbp, B.Tm, nb, T(0), B.GUT, nbp, nullptr,
+                    0, side);
+            k_copy_block<T><<<16, 256, 0, side>>>(Gj, nbp, B.Bm, nbp, nbp, b);
+            SKL_LAUNCHED();
+            gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
+                    side);
+            if (N2 > 0)
+                gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, B.R12, b, T(1),
+                        B.Y + (j + b) * nbp, nbp, nullptr, 0, side);
+            tms.end(7, t0);
+            const int64_t jn = j + nb;
+            const bool next_last = (jn + nb >= m) || (jn + nb >= d);
+            if (jn < mn && !next_last) {
+                const int bn = (int)std::min<int64_t>(nb, std::min<int64_t>(d - jn, m - jn));
+                launch_yqrp(jn, bn, (int)(d - jn), side, tms);
+            }
+            SKL_CUDA(cudaEventRecord(evY, side));
+            t0 = tms.begin();
+            gemm<T>(false, true, nbp, M, b, T(-1), B.GUT, nbp, B.V, m, T(1), Gj, nbp, nullptr, 0,
+                    side);
+            tms.end(7, t0);
+            SKL_CUDA(cudaEventRecord(evG, side));
+            side_pending = true;
+        }
+        if (N2 > 0) {
+            // A_trail -= V Z
+            cudaEvent_t t0 = tm.begin();
+            gemm<T>(false, false, M, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
+            tm.end(6, t0);
+        }
         if (c) {
             cudaEvent_t t0 = tm.begin();
             k_qt_w<T><<<b, 256, 0, st>>>(B.V, m, M, b, c + j, B.qw);
@@ -1000,41 +1106,9 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             SKL_LAUNCHED();
             tm.end(3, t0);
         }
-        const int N2 = N - b;
-        if (N2 > 0) {
-            T* Atr = A + j + (j + b) * ld;
-            // W = V^T A_trail ; Z = T^T W ; A_trail -= V Z
-            cudaEvent_t t0 = tm.begin();
-            gemm<T>(true, false, b, N2, M, T(1), B.V, m, Atr, ld, T(0), B.W, b, B.part,
-                    B.part_cap, st);
-            tm.end(4, t0);
-            t0 = tm.begin();
-            gemm<T>(true, false, b, N2, b, T(1), B.Tm, nb, B.W, b, T(0), B.Z, b, nullptr, 0, st);
-            tm.end(5, t0);
-            t0 = tm.begin();
-            gemm<T>(false, false, M, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
-            tm.end(6, t0);
-        }
-        if (pivoting && !last) {
-            cudaEvent_t t0 = tm.begin();
-            T* Gj = B.G + j * nbp;
-            // GU = G(:, j:m) V ; GUT = GU T ; B = G1 - GUT U11^T ; Y2 -= B R12 ; G(:, j:m) -= GUT V^T
-            gemm<T>(false, false, nbp, b, M, T(1), Gj, nbp, B.V, m, T(0), B.GU, nbp, B.part,
-                    B.part_cap, st);
-            gemm<T>(false, false, nbp, b, b, T(1), B.GU, nbp, B.Tm, nb, T(0), B.GUT, nbp, nullptr,
-                    0, st);
-            k_copy_block<T><<<16, 256, 0, st>>>(Gj, nbp, B.Bm, nbp, nbp, b);
-            SKL_LAUNCHED();
-            gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
-                    st);
-            if (N2 > 0)
-                gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, A + j + (j + b) * ld, ld, T(1),
-                        B.Y + (j + b) * nbp, nbp, nullptr, 0, st);
-            gemm<T>(false, true, nbp, M, b, T(-1), B.GUT, nbp, B.V, m, T(1), Gj, nbp, nullptr, 0,
-                    st);
-            tm.end(7, t0);
-        }
     }
+    if (side_pending) SKL_CUDA(cudaStreamWaitEvent(st, evG, 0));
+    tms.finish();
     tm.finish();
 }
 
