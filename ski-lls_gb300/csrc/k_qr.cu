@@ -42,6 +42,8 @@
 namespace skl {
 
 constexpr int kQrThreads = 512;
+constexpr int kYThreads = 512;    // sample QRP block
+constexpr int kYWarps = kYThreads / 32;
 constexpr int kQrWarps = kQrThreads / 32;
 constexpr int kCluster = 16;
 constexpr int kPP = 16;          // over-sampling rows of the sample Y
@@ -114,7 +116,7 @@ struct YqrpSmem {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kQrThreads)
+__global__ void __launch_bounds__(kYThreads)
 k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -129,24 +131,22 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     size_t off = ((size_t)ldp * cn * sizeof(T) + cn * sizeof(T) + cn + 16 + 15) & ~(size_t)15;
     T* cand_col = (T*)(smem_raw + off);          // [2][nbp]
     T* allc = cand_col + 2 * nbp;                 // [16][nbp]
-    T* v = allc + kCluster * nbp;                 // [nbp]
-    T* cand_val = v + nbp;                        // [2]
+    T* cand_val = allc + kCluster * nbp + nbp;    // [2]
     int* cand_idx = (int*)(cand_val + 2);         // [2]
-    __shared__ T s_red_v[kQrWarps];
-    __shared__ int s_red_i[kQrWarps];
+    __shared__ T s_red_v[kYWarps];
+    __shared__ int s_red_i[kYWarps];
     __shared__ T s_cv[kCluster];
     __shared__ int s_ci[kCluster];
-    __shared__ T s_tau;
-    __shared__ int s_win_idx, s_local;
+    __shared__ int s_local;
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int e = tid; e < nbp * ncols; e += kQrThreads) {
+    for (int e = tid; e < nbp * ncols; e += kYThreads) {
         int r = e % nbp, c = e / nbp;
         Ys[r + (size_t)c * ldp] = Y[r + (int64_t)(j0 + c0 + c) * ldy];
     }
-    for (int c = tid; c < cn; c += kQrThreads) taken[c] = (c < ncols) ? 0 : 1;
+    for (int c = tid; c < cn; c += kYThreads) taken[c] = (c < ncols) ? 0 : 1;
     __syncthreads();
-    for (int c = tid; c < ncols; c += kQrThreads) {
+    for (int c = tid; c < ncols; c += kYThreads) {
         const T* col = Ys + (size_t)c * ldp;
         T ss = T(0);
         for (int r = 0; r < nbp; ++r) ss += col[r] * col[r];
@@ -159,7 +159,7 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         // (a) local argmax (largest norm; ties -> smallest index)
         T bv = T(-1);
         int bi = -1;
-        for (int c = tid; c < ncols; c += kQrThreads) {
+        for (int c = tid; c < ncols; c += kYThreads) {
             // a NaN norm ranks below every real one but stays selectable, so
             // a winner always exists while untaken columns remain
             const T nv = nrm[c] == nrm[c] ? nrm[c] : T(-0.5);
@@ -174,8 +174,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
         __syncthreads();
         if (wid == 0) {
-            T ov = lane < kQrWarps ? s_red_v[lane] : T(-1);
-            int oi = lane < kQrWarps ? s_red_i[lane] : -1;
+            T ov = lane < kYWarps ? s_red_v[lane] : T(-1);
+            int oi = lane < kYWarps ? s_red_i[lane] : -1;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 T xv = __shfl_xor_sync(0xffffffffu, ov, o);
@@ -191,7 +191,7 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         __syncthreads();
         {
             const int li = s_local;
-            for (int r = s + tid; r < nbp; r += kQrThreads)
+            for (int r = s + tid; r < nbp; r += kYThreads)
                 cand_col[p * nbp + r] = (li >= 0) ? Ys[r + (size_t)li * ldp] : T(0);
         }
         cluster_sync();
@@ -201,59 +201,54 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
             s_ci[tid] = dsmem_ld_s32(&cand_idx[p], tid);
         }
         const int rows_left = nbp - s;
-        for (int e = tid; e < kCluster * rows_left; e += kQrThreads) {
+        for (int e = tid; e < kCluster * rows_left; e += kYThreads) {
             int q = e / rows_left, r = s + e % rows_left;
             allc[q * nbp + r] = dsmem_ld(&cand_col[p * nbp + r], q);
         }
         __syncthreads();
-        if (wid == 0) {
-            T ov = lane < kCluster ? s_cv[lane] : T(-1);
-            int oi = lane < kCluster ? s_ci[lane] : -1;
-            int orank = lane;
+        // winner and Householder vector, in every warp (no broadcast barrier)
+        T ov = lane < kCluster ? s_cv[lane] : T(-1);
+        int oi = lane < kCluster ? s_ci[lane] : -1;
+        int orank = lane;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                T xv = __shfl_xor_sync(0xffffffffu, ov, o);
-                int xi = __shfl_xor_sync(0xffffffffu, oi, o);
-                int xr = __shfl_xor_sync(0xffffffffu, orank, o);
-                if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; orank = xr; }
-            }
-            const T* wc = allc + orank * nbp;
-            T sg = T(0);
-            for (int r = s + 1 + lane; r < nbp; r += 32) sg += wc[r] * wc[r];
-            sg = warp_sum(sg);
-            T beta, tau, scale;
-            householder(wc[s], sg, beta, tau, scale);
-            for (int r = s + 1 + lane; r < nbp; r += 32) v[r] = wc[r] * scale;
-            if (lane == 0) {
-                v[s] = T(1);
-                s_tau = tau;
-                s_win_idx = oi;
-                if (crank == 0) sel[s] = oi;
-                if (oi >= c0 && oi < c0 + ncols) taken[oi - c0] = 1;
-            }
+        for (int o = 16; o > 0; o >>= 1) {
+            const T xv = __shfl_xor_sync(0xffffffffu, ov, o);
+            const int xi = __shfl_xor_sync(0xffffffffu, oi, o);
+            const int xr = __shfl_xor_sync(0xffffffffu, orank, o);
+            if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; orank = xr; }
         }
-        __syncthreads();
-        const T tau = s_tau;
+        const T* wc = allc + orank * nbp;
+        T sg = T(0);
+        for (int r = s + 1 + lane; r < nbp; r += 32) sg += wc[r] * wc[r];
+        sg = warp_sum(sg);
+        T beta, tau, scale;
+        householder(wc[s], sg, beta, tau, scale);
+        const int win_local = (oi >= c0 && oi < c0 + ncols) ? oi - c0 : -1;
+        if (tid == 0) {
+            if (crank == 0) sel[s] = oi;
+            if (win_local >= 0) taken[win_local] = 1;   // read again only after the next barrier
+        }
         // (c) H = I - tau v v^T on the untaken local columns, new norms (rows > s):
-        // 4 lanes per column, passes uniform across the CTA (quad shuffles)
+        // 4 lanes per column, passes uniform across the CTA (quad shuffles);
+        // v_r = 1 at r = s, wc[r] * scale below
         {
             const int q4 = tid & 3;
             const int gcol = tid >> 2;
-            const int per_pass = kQrThreads / 4;
+            const int per_pass = kYThreads / 4;
             for (int base = 0; base < ncols; base += per_pass) {
                 const int c = base + gcol;
-                const bool act = c < ncols && !taken[c];
+                const bool act = c < ncols && !taken[c] && c != win_local;
                 T* col = Ys + (size_t)(act ? c : 0) * ldp;
                 T w = T(0);
                 if (act)
-                    for (int r = s + q4; r < nbp; r += 4) w += v[r] * col[r];
+                    for (int r = s + q4; r < nbp; r += 4) w += (r == s ? T(1) : wc[r] * scale) * col[r];
                 w += __shfl_xor_sync(0xffffffffu, w, 1);
                 w += __shfl_xor_sync(0xffffffffu, w, 2);
                 w *= tau;
                 T ss = T(0);
                 if (act) {
                     for (int r = s + q4; r < nbp; r += 4) {
-                        T y = col[r] - w * v[r];
+                        T y = col[r] - w * (r == s ? T(1) : wc[r] * scale);
                         col[r] = y;
                         if (r > s) ss += y * y;
                     }
@@ -980,7 +975,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         int nbv = nbp;
         void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel};
         cudaEvent_t t0 = t.begin();
-        launch_cluster<T>((const void*)k_yqrp<T>, dim3(kQrThreads), ysm_max, s, args);
+        launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
         t.end(0, t0);
     };
 

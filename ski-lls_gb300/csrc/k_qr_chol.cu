@@ -25,6 +25,29 @@ constexpr int kMaxSmall = 64;
 // The reciprocal of the next pivot is formed by the thread that finishes that
 // pivot, one step ahead, so no division sits on the per-step critical path.
 
+// Thread layout of the eliminations: thread t owns row t >> 4 and the four
+// columns 4 (t & 15) .. +3 (one float4 of a row; ld = b + 4 keeps rows
+// 16-byte aligned), so 1024 threads cover a 64 x 64 block and every step is
+// one vector read-modify-write per thread plus one barrier.
+template <typename T> struct Quad;
+template <> struct Quad<float> { using type = float4; };
+template <> struct Quad<double> { using type = double4; };
+
+template <typename T>
+SKL_DEV typename Quad<T>::type ld4(const T* p) { return *reinterpret_cast<const typename Quad<T>::type*>(p); }
+template <typename T>
+SKL_DEV void st4(T* p, typename Quad<T>::type v) { *reinterpret_cast<typename Quad<T>::type*>(p) = v; }
+template <typename T, typename V>
+SKL_DEV T q_at(const V& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+template <typename T, typename V>
+SKL_DEV void q_set(V& v, int e, T x)
+{
+    if (e == 0) v.x = x;
+    else if (e == 1) v.y = x;
+    else if (e == 2) v.z = x;
+    else v.w = x;
+}
+
 // In-place Cholesky G = R^T R of the symmetric b x b block G: R (upper,
 // zeros below) over G.  Rows stay unnormalised during the elimination and
 // are scaled by 1/sqrt(d_i) at the end.  inv: b scratch entries (1/d_k).
@@ -32,7 +55,8 @@ constexpr int kMaxSmall = 64;
 template <typename T>
 SKL_DEV void chol_smem(T* G, int ld, int b, const T* __restrict__ mass, T eps, T* inv, int* bad)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+    const bool own = i < b && c0 < b;
     if (threadIdx.x == 0) {
         const T d = G[0];
         const bool ok = d > T(32) * eps * mass[0] && mass[0] > T(0);
@@ -41,25 +65,34 @@ SKL_DEV void chol_smem(T* G, int ld, int b, const T* __restrict__ mass, T eps, T
     }
     __syncthreads();
     for (int k = 0; k < b - 1; ++k) {
-        const T ik = inv[k];
-        for (int i = k + 1 + wid; i < b; i += kSmallWarps) {
-            const T gki = G[k * ld + i] * ik;
-            for (int c = i + lane; c < b; c += 32) {
-                const T v = G[i * ld + c] - gki * G[k * ld + c];
-                G[i * ld + c] = v;
-                if (c == k + 1) {                       // next pivot, finished now
-                    const bool ok = v > T(32) * eps * mass[c] && mass[c] > T(0);
-                    if (!ok) *bad = 1;
-                    inv[c] = ok ? T(1) / v : T(0);
-                }
+        if (own && i > k && c0 + 3 >= i) {
+            const T gki = G[k * ld + i] * inv[k];
+            auto row = ld4<T>(G + i * ld + c0);
+            const auto piv = ld4<T>(G + k * ld + c0);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = c0 + e;
+                if (c >= i && c < b) q_set<T>(row, e, q_at<T>(row, e) - gki * q_at<T>(piv, e));
+            }
+            st4<T>(G + i * ld + c0, row);
+            if (i == k + 1 && c0 <= i && i < c0 + 4) {   // next pivot, finished now
+                const T v = q_at<T>(row, i - c0);
+                const bool ok = v > T(32) * eps * mass[i] && mass[i] > T(0);
+                if (!ok) *bad = 1;
+                inv[i] = ok ? T(1) / v : T(0);
             }
         }
         __syncthreads();
     }
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e / b, c = e - i * b;
+    if (own) {
         const T s = inv[i] > T(0) ? t_sqrt(inv[i]) : T(0);
-        G[i * ld + c] = (c >= i) ? G[i * ld + c] * s : T(0);
+        auto row = ld4<T>(G + i * ld + c0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = c0 + e;
+            q_set<T>(row, e, (c >= i) ? q_at<T>(row, e) * s : T(0));
+        }
+        st4<T>(G + i * ld + c0, row);
     }
     __syncthreads();
 }
@@ -68,29 +101,41 @@ SKL_DEV void chol_smem(T* G, int ld, int b, const T* __restrict__ mass, T eps, T
 // diagonal never read).  Back substitution over all columns at once: step k
 // removes row k's contribution from rows i < k (columns c >= k), and row i
 // is final (scaled by 1/U_ii) after step i + 1.  Writes X's upper triangle,
-// and zeros below it when zero_lower.  inv: b scratch entries.
+// and zeros below it when zero_lower (otherwise only the upper triangle is
+// written, so X may hold another triangle below).  inv: b scratch entries.
 template <typename T>
 SKL_DEV void inv_upper_smem(const T* U, int ldu, int b, T* X, int ldx, bool zero_lower, T* inv)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+    const bool own = i < b && c0 < b;
     for (int k = threadIdx.x; k < b; k += kSmallThreads) inv[k] = T(1) / U[k * ldu + k];
     __syncthreads();
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e / b, c = e - i * b;
-        if (c >= i) X[i * ldx + c] = (i == c) ? (i == b - 1 ? inv[i] : T(1)) : T(0);
-        else if (zero_lower) X[i * ldx + c] = T(0);
+    if (own) {
+        auto row = ld4<T>(X + i * ldx + c0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = c0 + e;
+            if (c >= i) q_set<T>(row, e, (c == i) ? (i == b - 1 ? inv[i] : T(1)) : T(0));
+            else if (zero_lower) q_set<T>(row, e, T(0));
+        }
+        st4<T>(X + i * ldx + c0, row);
     }
     __syncthreads();
     for (int k = b - 1; k >= 1; --k) {
         // X[i][c] -= U[i][k] X[k][c] for i < k <= c; row k - 1 is then final
-        for (int i = wid; i < k; i += kSmallWarps) {
+        const bool has_diag = (i == k - 1) && c0 <= i && i < c0 + 4;
+        if (own && i < k && (c0 + 3 >= k || has_diag)) {
             const T uik = U[i * ldu + k];
-            for (int c = k + lane; c < b; c += 32) {
-                T v = X[i * ldx + c] - uik * X[k * ldx + c];
-                if (i == k - 1) v *= inv[i];
-                X[i * ldx + c] = v;
+            const T sc = (i == k - 1) ? inv[i] : T(1);
+            auto row = ld4<T>(X + i * ldx + c0);
+            const auto xk = ld4<T>(X + k * ldx + c0);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = c0 + e;
+                if (c >= k && c < b) q_set<T>(row, e, (q_at<T>(row, e) - uik * q_at<T>(xk, e)) * sc);
+                else if (c == i && i == k - 1) q_set<T>(row, e, inv[i]);
             }
-            if (i == k - 1 && lane == 0) X[i * ldx + i] = inv[i];   // column i's own entry
+            st4<T>(X + i * ldx + c0, row);
         }
         __syncthreads();
     }
@@ -102,21 +147,28 @@ SKL_DEV void inv_upper_smem(const T* U, int ldu, int b, T* X, int ldx, bool zero
 template <typename T>
 SKL_DEV void inv_unit_lower_smem(const T* L, int ldl, int b, T* Y, int ldy)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    // Y starts as the identity's strict lower part (zeros); row k of Y is
-    // final before step k, with Y[k][k] = 1 implied
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e / b, c = e - i * b;
-        if (c < i) Y[i * ldy + c] = T(0);
+    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+    const bool own = i < b && c0 < b;
+    // Y's strict lower part starts at zero; row k of Y is final before step k
+    if (own) {
+        auto row = ld4<T>(Y + i * ldy + c0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (c0 + e < i) q_set<T>(row, e, T(0));
+        st4<T>(Y + i * ldy + c0, row);
     }
     __syncthreads();
     for (int k = 0; k < b - 1; ++k) {
-        for (int i = k + 1 + wid; i < b; i += kSmallWarps) {
+        if (own && i > k && c0 <= k) {
             const T lik = L[i * ldl + k];
-            for (int c = lane; c <= k; c += 32) {
-                const T ykc = (c == k) ? T(1) : Y[k * ldy + c];
-                Y[i * ldy + c] -= lik * ykc;
+            auto row = ld4<T>(Y + i * ldy + c0);
+            const auto yk = ld4<T>(Y + k * ldy + c0);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = c0 + e;
+                if (c <= k) q_set<T>(row, e, q_at<T>(row, e) - lik * (c == k ? T(1) : q_at<T>(yk, e)));
             }
+            st4<T>(Y + i * ldy + c0, row);
         }
         __syncthreads();
     }
@@ -130,7 +182,8 @@ SKL_DEV void inv_unit_lower_smem(const T* L, int ldl, int b, T* Y, int ldy)
 template <typename T>
 SKL_DEV void mlu_smem(T* A, int ld, int b, T* sg, T* iu)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+    const bool own = i < b && c0 < b;
     if (threadIdx.x == 0) {
         const T p = A[0];
         const T sk = p >= T(0) ? T(-1) : T(1);
@@ -139,25 +192,32 @@ SKL_DEV void mlu_smem(T* A, int ld, int b, T* sg, T* iu)
     }
     __syncthreads();
     for (int k = 0; k < b; ++k) {
-        const T ik = iu[k];
-        if (k > 0) {
-            // finish column k - 1: multipliers and the pivot U_{k-1,k-1}
-            for (int i = k - 1 + threadIdx.x; i < b; i += kSmallThreads) {
-                if (i == k - 1) A[i * ld + i] = T(1) / iu[i];
-                else A[i * ld + (k - 1)] *= iu[k - 1];
+        if (own) {
+            auto row = ld4<T>(A + i * ld + c0);
+            bool dirty = false;
+            if (k > 0 && i >= k - 1 && c0 <= k - 1 && k - 1 < c0 + 4) {
+                // finish column k - 1: multiplier (i > k-1) or pivot U_{k-1,k-1}
+                const int e = k - 1 - c0;
+                q_set<T>(row, e, (i == k - 1) ? T(1) / iu[k - 1] : q_at<T>(row, e) * iu[k - 1]);
+                dirty = true;
             }
-        }
-        for (int i = k + 1 + wid; i < b; i += kSmallWarps) {
-            const T lik = A[i * ld + k] * ik;
-            for (int c = k + 1 + lane; c < b; c += 32) {
-                const T v = A[i * ld + c] - lik * A[k * ld + c];
-                A[i * ld + c] = v;
-                if (i == k + 1 && c == k + 1) {           // next pivot, finished now
+            if (i > k && c0 + 3 > k) {
+                const T lik = A[i * ld + k] * iu[k];
+                const auto uk = ld4<T>(A + k * ld + c0);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int c = c0 + e;
+                    if (c > k && c < b) q_set<T>(row, e, q_at<T>(row, e) - lik * q_at<T>(uk, e));
+                }
+                dirty = true;
+                if (i == k + 1 && c0 <= i && i < c0 + 4) {   // next pivot, finished now
+                    const T v = q_at<T>(row, i - c0);
                     const T sk = v >= T(0) ? T(-1) : T(1);
-                    sg[c] = sk;
-                    iu[c] = T(1) / (v - sk);
+                    sg[i] = sk;
+                    iu[i] = T(1) / (v - sk);
                 }
             }
+            if (dirty) st4<T>(A + i * ld + c0, row);
         }
         __syncthreads();
     }
