@@ -112,6 +112,9 @@ typedef struct {
        1 column moves, 2 panel, 3 Q^T c, 4 W = V^T A, 5 Z = T^T W,
        6 A -= V Z, 7 sample downdate, 8 initial sample Y = G A */
     double qr_prof_ms[9];
+    /* mixed path: refinement steps of the explicit sketch solution against
+       the FP64 residual (each ||b - A xs|| at least halved) */
+    int64_t sketch_refine_steps;
 } skl_info;
 
 /* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,

@@ -124,28 +124,39 @@ SKL_DEV Acc<MIXED> thread_dot_seg(const MatT<MIXED>* __restrict__ M, const ValT<
     if (t < jb - j0) a0.fma_f(M[j0 + t], v[j0 + t]);
     const int nch = (j1 - jb) >> 2;
     const int je = jb + (nch << 2);
+    // Chunks c, c + nthr, ... in order; two chunks per pass so that two
+    // 16-byte matrix loads per thread are in flight.
     if constexpr (MIXED) {
         const float4* M4 = reinterpret_cast<const float4*>(M + jb);
         const float4* v4 = reinterpret_cast<const float4*>(v + jb);   // 2 elements per float4
-        for (int c = t; c < nch; c += nthr) {
-            const float4 m0 = M4[c];
-            const float4 x0 = v4[2 * c], x1 = v4[2 * c + 1];
+        auto chunk = [&](const float4& m0, const float4& x0, const float4& x1) {
             a0.fma_f(m0.x, make_float2(x0.x, x0.y));
             a1.fma_f(m0.y, make_float2(x0.z, x0.w));
             a0.fma_f(m0.z, make_float2(x1.x, x1.y));
             a1.fma_f(m0.w, make_float2(x1.z, x1.w));
+        };
+        int c = t;
+        for (; c + nthr < nch; c += 2 * nthr) {
+            const int c2 = c + nthr;
+            const float4 m0 = M4[c], m1 = M4[c2];
+            const float4 x0 = v4[2 * c], x1 = v4[2 * c + 1];
+            const float4 y0 = v4[2 * c2], y1 = v4[2 * c2 + 1];
+            chunk(m0, x0, x1);
+            chunk(m1, y0, y1);
         }
+        if (c < nch) chunk(M4[c], v4[2 * c], v4[2 * c + 1]);
     } else {
         const double2* M2 = reinterpret_cast<const double2*>(M + jb);
         const double2* v2 = reinterpret_cast<const double2*>(v + jb);
-        for (int c = t; c < nch; c += nthr) {
+        auto chunk = [&](int c) {
             const double2 m0 = M2[2 * c], m1 = M2[2 * c + 1];
             const double2 x0 = v2[2 * c], x1 = v2[2 * c + 1];
             a0.fma_f(m0.x, x0.x);
             a1.fma_f(m0.y, x0.y);
             a0.fma_f(m1.x, x1.x);
             a1.fma_f(m1.y, x1.y);
-        }
+        };
+        for (int c = t; c < nch; c += nthr) chunk(c);
     }
     if (t < j1 - je) a1.fma_f(M[je + t], v[je + t]);
     a0.add(a1);
@@ -228,16 +239,23 @@ k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED
     double ss = 0.0;
     for (int pidx = blockIdx.x; pidx < npairs; pidx += gridDim.x) {
         const int j1 = pidx, j2 = r - 1 - pidx;
+        // the old vh of both columns, loaded before the dots so the epilogue
+        // does not wait on memory
+        double o1 = 0.0, o2 = 0.0;
+        if (threadIdx.x == 0) {
+            o1 = vh[j1];
+            if (j2 != j1) o2 = vh[j2];
+        }
         Acc<MIXED> a = thread_dot_seg<MIXED>(Mc + (int64_t)j1 * ldm, t, 0, j1 + 1, threadIdx.x, kTriThreads);
         Acc<MIXED> b;
         if (j2 != j1) b = thread_dot_seg<MIXED>(Mc + (int64_t)j2 * ldm, t, 0, j2 + 1, threadIdx.x, kTriThreads);
         block_reduce2<MIXED>(a, b, sm);
         if (threadIdx.x == 0) {
-            double nv = a.value() - coef * vh[j1];
+            double nv = a.value() - coef * o1;
             vh[j1] = nv;
             ss += nv * nv;
             if (j2 != j1) {
-                nv = b.value() - coef * vh[j2];
+                nv = b.value() - coef * o2;
                 vh[j2] = nv;
                 ss += nv * nv;
             }
@@ -254,9 +272,27 @@ k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED
     }
 }
 
+// Loads of four (index, value) entries p, p+L, p+2L, p+3L of one row or
+// column, predicated on p < p1 (index 0 and value 0 past the end, so the
+// matching gather reads a valid element and contributes nothing).
+template <bool MIXED, int L>
+SKL_DEV void load_group4(const int* __restrict__ idx, const ValT<MIXED>* __restrict__ val, int p,
+                         int p1, int (&ii)[4], ValT<MIXED> (&aa)[4])
+{
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int q = p + k * L;
+        const bool ok = q < p1;
+        ii[k] = ok ? idx[q] : 0;
+        aa[k] = ok ? val[q] : ValT<MIXED>{};
+    }
+}
+
 // ---------------------------------------------------------- spmv_n (CSR) --
 // uh[i] = sum_j A[i][j] z[j] - coef * uh[i], coef = alpha/beta (0 at init with
 // z = 0 replaced by rhs b);  usplit = split(uh);  beta' = ||uh||.
+constexpr int kRowTile = 512;   // rows whose pointers a block stages at a time
+
 template <bool MIXED, int L>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<MIXED>* __restrict__ cv,
@@ -264,20 +300,25 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
              double* __restrict__ uh, ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S,
              double* __restrict__ partials)
 {
+    using V = ValT<MIXED>;
     if (S->done) return;
     __shared__ double wsum[kLThreads / 32];
+    __shared__ int rps[kRowTile + 1];
     // z is gathered at random columns: stage it in shared memory when it fits
     extern __shared__ __align__(16) unsigned char zsm_raw[];
-    const ValT<MIXED>* z = zg;
+    const V* z = zg;
     if (d_stage > 0) {
-        ValT<MIXED>* zs = reinterpret_cast<ValT<MIXED>*>(zsm_raw);
+        V* zs = reinterpret_cast<V*>(zsm_raw);
         for (int j = threadIdx.x; j < d_stage; j += blockDim.x) zs[j] = zg[j];
-        __syncthreads();
         z = zs;
     }
     // Each warp owns 32/L consecutive row slots per pass; the pass count is
     // uniform across the warp so the full-mask shuffles below always see all
-    // 32 lanes (groups past the last row contribute zero).
+    // 32 lanes (groups past the last row contribute zero).  Rows are software
+    // pipelined: the first four (index, value) loads per lane and the old
+    // uh of the next pass's row are issued before the current row's gathers
+    // and arithmetic, and the row pointers come from shared memory, so a pass
+    // waits on one memory round trip instead of three.
     const int lane = threadIdx.x % L;
     const int grp = threadIdx.x / L;
     const int ngrp = kLThreads / L;
@@ -286,25 +327,39 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
     const int r1 = min(n, r0 + rows_per_block);
     const int warp_grp0 = (threadIdx.x >> 5) * (32 / L);
     double ss = 0.0;
-    for (int base = r0 + warp_grp0; base < r1; base += ngrp) {
-        const int i = base + (grp - warp_grp0);
-        const bool active = i < r1;
-        Acc<MIXED> acc, acc2;
-        if (active) {
-            const int p1 = rp[i + 1];
-            // predicated groups of four: every lane issues its (index, value)
-            // loads and gathers before any arithmetic, also on short rows
-            for (int pb = rp[i] + lane; pb < p1; pb += 4 * L) {
-                int cc[4];
-                ValT<MIXED> aa[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int p = pb + k * L;
-                    const bool ok = p < p1;
-                    cc[k] = ok ? ci[p] : 0;
-                    aa[k] = ok ? cv[p] : ValT<MIXED>{};
-                }
-                ValT<MIXED> zz[4];
+    for (int t0 = r0; t0 < r1; t0 += kRowTile) {
+        const int t1 = min(r1, t0 + kRowTile);
+        __syncthreads();   // z staged; the previous tile's pointers are no longer read
+        for (int q = threadIdx.x; q <= t1 - t0; q += blockDim.x) rps[q] = rp[t0 + q];
+        __syncthreads();
+        int i = t0 + grp;
+        bool act = i < t1;
+        int pb = 0, p1 = 0;
+        int cc[4];
+        V aa[4];
+        double uo = 0.0;
+        if (act) {
+            pb = rps[i - t0] + lane;
+            p1 = rps[i - t0 + 1];
+            if (lane == 0) uo = uh[i];
+        }
+        load_group4<MIXED, L>(ci, cv, pb, p1, cc, aa);
+        for (int base = t0 + warp_grp0; base < t1; base += ngrp) {
+            const int ni = i + ngrp;
+            const bool nact = ni < t1;
+            int npb = 0, np1 = 0;
+            int nc[4];
+            V na[4];
+            double nuo = 0.0;
+            if (nact) {
+                npb = rps[ni - t0] + lane;
+                np1 = rps[ni - t0 + 1];
+                if (lane == 0) nuo = uh[ni];
+            }
+            load_group4<MIXED, L>(ci, cv, npb, np1, nc, na);
+            Acc<MIXED> acc, acc2;
+            {
+                V zz[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) zz[k] = z[cc[k]];
                 acc.fma_mv(aa[0], zz[0]);
@@ -312,15 +367,38 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
                 acc.fma_mv(aa[2], zz[2]);
                 acc2.fma_mv(aa[3], zz[3]);
             }
-        }
-        acc.add(acc2);
+            // rows longer than 4L: the remaining groups of four, unpipelined
+            for (int p = pb + 4 * L; p < p1; p += 4 * L) {
+                int c2[4];
+                V a2[4];
+                load_group4<MIXED, L>(ci, cv, p, p1, c2, a2);
+                V zz[4];
 #pragma unroll
-        for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
-        if (active && lane == 0) {
-            double nv = acc.value() - coef * uh[i];
-            uh[i] = nv;
-            us[i] = store_val<MIXED>(nv);
-            ss += nv * nv;
+                for (int k = 0; k < 4; ++k) zz[k] = z[c2[k]];
+                acc.fma_mv(a2[0], zz[0]);
+                acc2.fma_mv(a2[1], zz[1]);
+                acc.fma_mv(a2[2], zz[2]);
+                acc2.fma_mv(a2[3], zz[3]);
+            }
+            acc.add(acc2);
+#pragma unroll
+            for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
+            if (act && lane == 0) {
+                double nv = acc.value() - coef * uo;
+                uh[i] = nv;
+                us[i] = store_val<MIXED>(nv);
+                ss += nv * nv;
+            }
+            i = ni;
+            act = nact;
+            pb = npb;
+            p1 = np1;
+            uo = nuo;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                cc[k] = nc[k];
+                aa[k] = na[k];
+            }
         }
     }
     ss = warp_sum(ss);
@@ -342,6 +420,9 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
 
 // --------------------------------------------------------- spmv_t (CSC) --
 // t[i] = colscale[c] * (sum_{p in col c} A[p] u[row p]) / beta,  c = cols[i]
+// L lanes per column; the (index, value) loads of the next group of four per
+// lane are issued before the gathers of the current group are consumed, so
+// the HBM stream of A overlaps the L2 gathers of u.
 template <bool MIXED, int L>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<MIXED>* __restrict__ cv,
@@ -349,6 +430,7 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
              const ValT<MIXED>* __restrict__ us, ValT<MIXED>* __restrict__ t,
              const LsqrState* __restrict__ S)
 {
+    using V = ValT<MIXED>;
     if (S->done) return;
     const int lane = threadIdx.x % L;
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L;
@@ -364,23 +446,28 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
         if (active) {
             c = cols[i];
             const int p1 = cp[c + 1];
-            for (int pb = cp[c] + lane; pb < p1; pb += 4 * L) {
-                int rr[4];
-                ValT<MIXED> aa[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int p = pb + k * L;
-                    const bool ok = p < p1;
-                    rr[k] = ok ? ri[p] : 0;
-                    aa[k] = ok ? cv[p] : ValT<MIXED>{};
-                }
-                ValT<MIXED> uu[4];
+            int pb = cp[c] + lane;
+            int rr[4];
+            V aa[4];
+            load_group4<MIXED, L>(ri, cv, pb, p1, rr, aa);
+            while (pb < p1) {
+                V uu[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) uu[k] = us[rr[k]];
+                const int pn = pb + 4 * L;
+                int rn[4];
+                V an[4];
+                load_group4<MIXED, L>(ri, cv, pn, p1, rn, an);
                 acc.fma_mv(aa[0], uu[0]);
                 acc2.fma_mv(aa[1], uu[1]);
                 acc.fma_mv(aa[2], uu[2]);
                 acc2.fma_mv(aa[3], uu[3]);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    rr[k] = rn[k];
+                    aa[k] = an[k];
+                }
+                pb = pn;
             }
         }
         acc.add(acc2);
@@ -891,6 +978,107 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
     else
         k_tri_n_f64acc<double><<<g, kTriThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv,
                                                           P.cols, P.colscale, xfull);
+    SKL_LAUNCHED();
+}
+
+// ------------------------------------- refinement of the sketch solution --
+// One step of iterative refinement of the sketched least-squares solution
+// c* = argmin || S (A D P1 M c - b) || (the explicit solution x_s = D P1 M c
+// of ls_sparse_spqr, src/ls_sparse_spqr.cpp:144-151, which the reference forms
+// from an FP64 factorization):
+//     r  = b - A x            (FP64, by the caller / the previous step)
+//     g  = D P1^T A^T S^T S r
+//     c += M^T g,  x = D P1 M c,  r = b - A x.
+// With M from an FP32 factorization of S A D P1 (= Q R + E, ||E|| ~ eps32 ||S A D||)
+// each step contracts the error of c by ~eps32 * cond(R), so two or three
+// steps bring x_s to FP64 quality; the LSQR that follows then starts from the
+// residual the reference starts from.
+
+// h[i] = sum_t sign(i, t) / sqrt(k) * g[row(i, t)]   (S^T g; hidx[i*k+t] = row | sign bit)
+__global__ void k_hash_t(const unsigned* __restrict__ hidx, int n, int k, double v,
+                         const double* __restrict__ g, double* __restrict__ h)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int t = 0; t < k; ++t) {
+            const unsigned e = hidx[(int64_t)i * k + t];
+            const double sv = (e & 0x80000000u) ? -v : v;
+            acc = fma(sv, g[e & 0x7fffffffu], acc);
+        }
+        h[i] = acc;
+    }
+}
+
+// t[i] = colscale[c] * sum_{p in column c} A[p] h[row p],  c = cols[i]  (FP64, warp per column)
+__global__ void __launch_bounds__(kLThreads)
+k_atr_sel(const int* __restrict__ cp, const int* __restrict__ ri, const double* __restrict__ rx,
+          const int* __restrict__ cols, const double* __restrict__ colscale, int r,
+          const double* __restrict__ h, double* __restrict__ t)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < r; i += nw) {
+        const int c = cols[i];
+        double a0 = 0.0, a1 = 0.0;
+        const int p1 = cp[c + 1];
+        int p = cp[c] + lane;
+        for (; p + 32 < p1; p += 64) {
+            a0 = fma(rx[p], h[ri[p]], a0);
+            a1 = fma(rx[p + 32], h[ri[p + 32]], a1);
+        }
+        if (p < p1) a0 = fma(rx[p], h[ri[p]], a0);
+        const double acc = warp_sum(a0 + a1);
+        if (lane == 0) t[i] = colscale[c] * acc;
+    }
+}
+
+// c[j] += sum_{i <= j} M[i][j] t[i]  (Mc column-major, FP64 accumulation)
+template <typename MT>
+__global__ void __launch_bounds__(kTriThreads)
+k_tri_t_acc(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restrict__ t,
+            double* __restrict__ c)
+{
+    __shared__ double red[kTriThreads / 32];
+    for (int j = blockIdx.x; j < r; j += gridDim.x) {
+        const MT* col = Mc + (int64_t)j * ldm;
+        double acc = 0.0;
+        for (int i = threadIdx.x; i <= j; i += blockDim.x) acc = fma((double)col[i], t[i], acc);
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) c[j] += acc;
+    }
+}
+
+__global__ void __launch_bounds__(kLThreads)
+k_residual_csr(const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ cx,
+               int n, const double* __restrict__ x, const double* __restrict__ b,
+               double* __restrict__ r, double* __restrict__ part);
+__global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out);
+
+void sketch_refine_step(const LsqrProblem& P, const int* bptr, const unsigned* bent,
+                        const unsigned* hidx, int k, int64_t m, const double* b, double* rs,
+                        double* gm, double* t, double* c, double* x, double* part,
+                        double* rnorm, cudaStream_t st)
+{
+    if (P.r <= 0 || P.Ad64 || P.Ad) fail(SKL_ERR_INVALID, "sketch refinement: sparse problems only");
+    sketch_rhs(bptr, bent, m, k, rs, gm, st);
+    const double v = 1.0 / std::sqrt((double)k);
+    k_hash_t<<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 152 * 16), 256, 0, st>>>(
+        hidx, (int)P.n, k, v, gm, rs);
+    k_atr_sel<<<(unsigned)std::min<int64_t>((P.r * 32 + kLThreads - 1) / kLThreads, 152 * 32),
+                kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, P.cols, P.colscale, (int)P.r, rs, t);
+    const unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
+    if (P.precision == SKL_PREC_MIXED)
+        k_tri_t_acc<float><<<g, kTriThreads, 0, st>>>((const float*)P.M, P.ldm, (int)P.r, t, c);
+    else
+        k_tri_t_acc<double><<<g, kTriThreads, 0, st>>>((const double*)P.M, P.ldm, (int)P.r, t, c);
+    for (int q = 0; q < 3; ++q) SKL_LAUNCHED();
+    SKL_CUDA(cudaMemsetAsync(x, 0, P.d * sizeof(double), st));
+    precond_apply(P, c, x, nullptr, st);
+    const int np = 512;
+    k_residual_csr<<<np, kLThreads, 0, st>>>(P.rp, P.ci, P.cx64, (int)P.n, x, b, rs, part);
+    k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, rnorm);
+    SKL_LAUNCHED();
     SKL_LAUNCHED();
 }
 

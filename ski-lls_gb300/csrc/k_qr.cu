@@ -786,12 +786,12 @@ static QrPlan qr_plan(int64_t m, int64_t d)
 
 template <typename T>
 struct QrBuffers {
-    T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *tmp;
+    T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *part2, *tmp;
     int *sel, *plan_src, *plan_dst, *plan_n, *chol_fail;
     T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
     T* R12;                   // b x (d-j): rows j..j+b of the updated trailing matrix
     double *qw;
-    int64_t part_cap, tmp_rows;
+    int64_t part_cap, part2_cap, tmp_rows;   // part2: split-K partials of the side stream
 };
 
 template <typename T>
@@ -818,6 +818,8 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     if (cap < (int64_t)1 << 20) cap = (int64_t)1 << 20;
     B.part_cap = cap;
     B.part = (T*)take((size_t)cap * sizeof(T));
+    B.part2_cap = (int64_t)32 * p.nbp * p.nb;
+    B.part2 = (T*)take((size_t)B.part2_cap * sizeof(T));
     B.tmp_rows = m > p.nbp ? m : p.nbp;
     B.tmp = (T*)take((size_t)B.tmp_rows * 2 * p.nb * sizeof(T));
     B.sel = (int*)take(kMaxNb * sizeof(int));
@@ -937,33 +939,33 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
     const bool use_chol = pivoting && nb <= 64 && std::is_same<T, float>::value && qr_chol_enabled<T>();
 
-    // Two streams.  After W and Z of panel j the sample work (Y downdate, the
-    // sample QRP of panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs
-    // on a high-priority side stream while the main stream applies the big
-    // trailing update and Q^T c; panel j+1's permutation waits for the side
-    // stream's event.  (R12 is formed separately because the update rewrites
-    // A12 concurrently.)
+    // Two streams.  The sample work of panel j (Y downdate, the sample QRP of
+    // panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs on a
+    // high-priority side stream: the part that needs V and T alone (GU, GUT, B)
+    // overlaps W and R12, the rest overlaps the big trailing update and Q^T c;
+    // panel j+1's permutation waits for the side stream's event.  (R12 is
+    // formed separately because the update rewrites A12 concurrently.)
     cudaStream_t side = nullptr;
-    cudaEvent_t evR = nullptr, evY = nullptr, evG = nullptr;
+    cudaEvent_t evV = nullptr, evR = nullptr, evY = nullptr, evG = nullptr;
     if (pivoting) {
         int lo = 0, hi = 0;
         SKL_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         SKL_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+        SKL_CUDA(cudaEventCreateWithFlags(&evV, cudaEventDisableTiming));
         SKL_CUDA(cudaEventCreateWithFlags(&evR, cudaEventDisableTiming));
         SKL_CUDA(cudaEventCreateWithFlags(&evY, cudaEventDisableTiming));
         SKL_CUDA(cudaEventCreateWithFlags(&evG, cudaEventDisableTiming));
     }
     struct StreamGuard {
         cudaStream_t s;
-        cudaEvent_t a, b, c;
+        cudaEvent_t ev[4];
         ~StreamGuard()
         {
-            if (a) cudaEventDestroy(a);
-            if (b) cudaEventDestroy(b);
-            if (c) cudaEventDestroy(c);
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
             if (s) cudaStreamDestroy(s);
         }
-    } guard{side, evR, evY, evG};
+    } guard{side, {evV, evR, evY, evG}};
     QrTimer tms{qr_prof, {}, {}, 0, side};
     bool side_pending = false;
 
@@ -1034,6 +1036,22 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             tm.end(2, t0);
             trace_phase(st, "qr: panel");
         }
+        T* Gj = B.G + j * nbp;
+        if (pivoting && !last) {
+            // side: GU = G(:, j:m) V ; GUT = GU T ; B = G1 - GUT V1^T
+            SKL_CUDA(cudaEventRecord(evV, st));
+            SKL_CUDA(cudaStreamWaitEvent(side, evV, 0));
+            cudaEvent_t t0 = tms.begin();
+            gemm<T>(false, false, nbp, b, M, T(1), Gj, nbp, B.V, m, T(0), B.GU, nbp, B.part2,
+                    B.part2_cap, side);
+            gemm<T>(false, false, nbp, b, b, T(1), B.GU, nbp, B.Tm, nb, T(0), B.GUT, nbp, nullptr,
+                    0, side);
+            k_copy_block<T><<<16, 256, 0, side>>>(Gj, nbp, B.Bm, nbp, nbp, b);
+            SKL_LAUNCHED();
+            gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
+                    side);
+            tms.end(7, t0);
+        }
         const int N2 = N - b;
         T* Atr = A + j + (j + b) * ld;
         if (N2 > 0) {
@@ -1055,19 +1073,9 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             }
             SKL_CUDA(cudaEventRecord(evR, st));
             SKL_CUDA(cudaStreamWaitEvent(side, evR, 0));
-            // side: GU = G(:, j:m) V ; GUT = GU T ; B = G1 - GUT U11^T ;
-            // Y2 -= B R12 ; the next sample QRP (evY) ; G(:, j:m) -= GUT V^T,
+            // side: Y2 -= B R12 ; the next sample QRP (evY) ; G(:, j:m) -= GUT V^T,
             // which only the next downdate needs (evG)
             cudaEvent_t t0 = tms.begin();
-            T* Gj = B.G + j * nbp;
-            gemm<T>(false, false, nbp, b, M, T(1), Gj, nbp, B.V, m, T(0), B.GU, nbp, B.part,
-                    B.part_cap, side);
-            gemm<T>(false, false, nbp, b, b, T(1), B.GU, nbp, B.Tm, nb, T(0), B.GUT, nbp, nullptr,
-                    0, side);
-            k_copy_block<T><<<16, 256, 0, side>>>(Gj, nbp, B.Bm, nbp, nbp, b);
-            SKL_LAUNCHED();
-            gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
-                    side);
             if (N2 > 0)
                 gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, B.R12, b, T(1),
                         B.Y + (j + b) * nbp, nbp, nullptr, 0, side);

@@ -28,6 +28,17 @@
 
 namespace skl {
 
+// Upper bound on the refinement steps of the mixed path's sketch solution
+// (SKILLS_SKETCH_REFINE=<n>; 0 disables).
+static int sketch_refine_max_steps()
+{
+    static const int v = [] {
+        const char* e = std::getenv("SKILLS_SKETCH_REFINE");
+        return e ? std::max(0, std::atoi(e)) : 6;
+    }();
+    return v;
+}
+
 // ------------------------------------------------------------- errors ----
 static thread_local std::string t_last_error;
 static thread_local int64_t t_launches = 0;
@@ -267,6 +278,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     S.add<double>(d); S.add<double>(n); S.add<double>(d); S.add<double>(1024); S.add<double>(8);
     S.add<char>((int64_t)std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
     S.add<float2>(d);
+    S.add<double>(m);
     C.arena.reserve(S.bytes());
     C.arena.reset();
     Arena& Ar = C.arena;
@@ -297,6 +309,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     double* scal = Ar.alloc<double>(8);
     void* work = Ar.take(std::max({qr_ws, inv_ws, lsqr_ws, csr_scr, bkt_scr}));
     float2* ysplit = Ar.alloc<float2>(d);
+    double* gm = Ar.alloc<double>(m);   // S r_s during the sketch-solution refinement
 
     cudaEvent_t* ev = C.ev;
     SKL_CUDA(cudaEventRecord(ev[1], st));
@@ -366,10 +379,48 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     precond_apply(P, cvec, x_dev, ysplit, st);
     residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
     trace_phase(st, "explicit solution");
-    SKL_CUDA(cudaEventRecord(ev[5], st));
     SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     SKL_CUDA(cudaStreamSynchronize(st));
     double rnorm = ((double*)C.host_pinned)[0];
+    if (mixed && !(rnorm < o.abs_tol)) {
+        // The reference forms x_s from an FP64 factorization; an FP32 one leaves
+        // x_s ~eps32*cond(R) off the sketched solution, and LSQR would spend
+        // iterations removing that consistent part of r_s.  Refine c against
+        // the FP64 residual until ||r_s|| stops halving (not merely until it
+        // drops below abs_tol: the early exit must see an x_s as good as the
+        // reference's).
+        const int steps = sketch_refine_max_steps();
+        double prev = rnorm;
+        bool refined = false;
+        for (int s = 0; s < steps; ++s) {
+            SKL_CUDA(cudaMemcpyAsync(yv, cvec, rank * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            sketch_refine_step(P, bptr, bent, hidx, (int)k, m, in.b, rs, gm, xacc, cvec, x_dev, part,
+                               scal, st);
+            SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            const double rn = ((double*)C.host_pinned)[0];
+            refined = true;
+            if (!(rn < prev)) {
+                // no progress (cond(R) too large for the FP32 factor): keep the previous c
+                SKL_CUDA(cudaMemcpyAsync(cvec, yv, rank * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
+                precond_apply(P, cvec, x_dev, ysplit, st);
+                break;
+            }
+            const bool slow = rn > 0.5 * prev;
+            prev = rn;
+            ++info.sketch_refine_steps;
+            if (slow) break;   // at the floor: further steps cannot lower ||r_s||
+        }
+        if (refined) {
+            residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
+            SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            rnorm = ((double*)C.host_pinned)[0];
+        }
+        trace_phase(st, "sketch refinement");
+    }
+    SKL_CUDA(cudaEventRecord(ev[5], st));
     info.explicit_residual = rnorm;
     info.it = 0;
     info.flag = 0;

@@ -76,7 +76,8 @@ class SklInfo(ctypes.Structure):
                 ("t_qr_ms", ctypes.c_double), ("t_precond_ms", ctypes.c_double),
                 ("t_lsqr_ms", ctypes.c_double), ("t_host_hash_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("prof_ms", ctypes.c_double * 4),
-                ("prof_launches", ctypes.c_int64 * 4), ("qr_prof_ms", ctypes.c_double * 9)]
+                ("prof_launches", ctypes.c_int64 * 4), ("qr_prof_ms", ctypes.c_double * 9),
+                ("sketch_refine_steps", ctypes.c_int64)]
 
     def as_dict(self):
         out = {}

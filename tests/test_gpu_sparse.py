@@ -72,6 +72,28 @@ def test_column_scaled_rank_deficient():
     assert abs(r_gpu - r_ref) <= 1e-9 * r_ref
 
 
+def test_mixed_sketch_solution_matches_fp64():
+    # Column scales up to 1e8 and planted dependent columns leave the FP32
+    # sketch solution ~1e-6 off; the mixed path refines it against the FP64
+    # residual, so its explicit residual and LSQR iteration count match the
+    # FP64 path's (the reference forms x_s from an FP64 factorization).
+    import synthetic
+    A, b, _ = synthetic.sparse_illcond(seed=11, n=24000, d=1000, per_col=240, n_dep=10)
+    out = {}
+    for precision in ("mixed", "fp64"):
+        out[precision] = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-10, seed=1,
+                                            precision=precision)
+    mixed, fp64 = out["mixed"], out["fp64"]
+    assert mixed.info["sketch_refine_steps"] >= 1
+    assert fp64.info["sketch_refine_steps"] == 0
+    xr_m, xr_d = mixed.info["explicit_residual"], fp64.info["explicit_residual"]
+    # the two factorizations keep different (equally valid) column sets, so the
+    # sketched optima differ slightly; unrefined, xr_m would be ~1e-6 ||b|| larger
+    assert abs(xr_m - xr_d) <= 1e-2 * xr_d, (xr_m, xr_d)
+    assert mixed.it <= fp64.it + 5, (mixed.it, fp64.it)
+    assert mixed.rank == fp64.rank == 990
+
+
 @pytest.mark.parametrize("name", RANK_DEF_NAMES)
 def test_rank_deficient_fixture_residuals(fixtures, name):
     n, d, p, i, x = fixture_csc(fixtures, name)
