@@ -1033,11 +1033,11 @@ k_atr_sel(const int* __restrict__ cp, const int* __restrict__ ri, const double* 
     }
 }
 
-// c[j] += sum_{i <= j} M[i][j] t[i]  (Mc column-major, FP64 accumulation)
+// dc[j] = sum_{i <= j} M[i][j] t[i]  (Mc column-major, FP64 accumulation)
 template <typename MT>
 __global__ void __launch_bounds__(kTriThreads)
-k_tri_t_acc(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restrict__ t,
-            double* __restrict__ c)
+k_tri_t_f64(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restrict__ t,
+            double* __restrict__ dc)
 {
     __shared__ double red[kTriThreads / 32];
     for (int j = blockIdx.x; j < r; j += gridDim.x) {
@@ -1045,8 +1045,28 @@ k_tri_t_acc(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restr
         double acc = 0.0;
         for (int i = threadIdx.x; i <= j; i += blockDim.x) acc = fma((double)col[i], t[i], acc);
         acc = block_sum(acc, red);
-        if (threadIdx.x == 0) c[j] += acc;
+        if (threadIdx.x == 0) dc[j] = acc;
     }
+}
+
+// partial sums of squares of x[0..n) per block (fixed order)
+__global__ void __launch_bounds__(kLThreads)
+k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ part)
+{
+    __shared__ double red[kLThreads / 32];
+    double ss = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        ss += x[i] * x[i];
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+// c[i] += sgn * dc[i]
+__global__ void k_axpy_sign(int n, double sgn, const double* __restrict__ dc, double* __restrict__ c)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c[i] = fma(sgn, dc[i], c[i]);
 }
 
 __global__ void __launch_bounds__(kLThreads)
@@ -1055,24 +1075,44 @@ k_residual_csr(const int* __restrict__ rp, const int* __restrict__ ci, const dou
                double* __restrict__ r, double* __restrict__ part);
 __global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out);
 
-void sketch_refine_step(const LsqrProblem& P, const int* bptr, const unsigned* bent,
-                        const unsigned* hidx, int k, int64_t m, const double* b, double* rs,
-                        double* gm, double* t, double* c, double* x, double* part,
-                        double* rnorm, cudaStream_t st)
+static void vec_norm(const double* x, int64_t n, double* part, double* out, cudaStream_t st)
+{
+    const int np = 256;
+    k_sumsq<<<np, kLThreads, 0, st>>>(x, n, part);
+    k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
+    SKL_LAUNCHED();
+    SKL_LAUNCHED();
+}
+
+void sketch_refine_direction(const LsqrProblem& P, const int* bptr, const unsigned* bent,
+                             const unsigned* hidx, int k, int64_t m, const double* rs, double* gm,
+                             double* h, double* t, double* dc, double* part, double* norms,
+                             cudaStream_t st)
 {
     if (P.r <= 0 || P.Ad64 || P.Ad) fail(SKL_ERR_INVALID, "sketch refinement: sparse problems only");
     sketch_rhs(bptr, bent, m, k, rs, gm, st);
     const double v = 1.0 / std::sqrt((double)k);
     k_hash_t<<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 152 * 16), 256, 0, st>>>(
-        hidx, (int)P.n, k, v, gm, rs);
+        hidx, (int)P.n, k, v, gm, h);
     k_atr_sel<<<(unsigned)std::min<int64_t>((P.r * 32 + kLThreads - 1) / kLThreads, 152 * 32),
-                kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, P.cols, P.colscale, (int)P.r, rs, t);
+                kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, P.cols, P.colscale, (int)P.r, h, t);
     const unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
     if (P.precision == SKL_PREC_MIXED)
-        k_tri_t_acc<float><<<g, kTriThreads, 0, st>>>((const float*)P.M, P.ldm, (int)P.r, t, c);
+        k_tri_t_f64<float><<<g, kTriThreads, 0, st>>>((const float*)P.M, P.ldm, (int)P.r, t, dc);
     else
-        k_tri_t_acc<double><<<g, kTriThreads, 0, st>>>((const double*)P.M, P.ldm, (int)P.r, t, c);
+        k_tri_t_f64<double><<<g, kTriThreads, 0, st>>>((const double*)P.M, P.ldm, (int)P.r, t, dc);
     for (int q = 0; q < 3; ++q) SKL_LAUNCHED();
+    vec_norm(gm, m, part, norms, st);
+    vec_norm(dc, P.r, part + 256, norms + 1, st);
+}
+
+void sketch_refine_apply(const LsqrProblem& P, double sgn, const double* dc, double* c,
+                         const double* b, double* x, double* rs, double* part, double* rnorm,
+                         cudaStream_t st)
+{
+    k_axpy_sign<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152)), 256,
+                  0, st>>>((int)P.r, sgn, dc, c);
+    SKL_LAUNCHED();
     SKL_CUDA(cudaMemsetAsync(x, 0, P.d * sizeof(double), st));
     precond_apply(P, c, x, nullptr, st);
     const int np = 512;

@@ -386,38 +386,40 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
         // The reference forms x_s from an FP64 factorization; an FP32 one leaves
         // x_s ~eps32*cond(R) off the sketched solution, and LSQR would spend
         // iterations removing that consistent part of r_s.  Refine c against
-        // the FP64 residual until ||r_s|| stops halving (not merely until it
-        // drops below abs_tol: the early exit must see an x_s as good as the
-        // reference's).
+        // the FP64 residual while a step is predicted to shrink ||r_s|| by at
+        // least 13 %: the correction dc = Q1^T S r_s removes the part of the
+        // sketched residual in range(S A), so ||r_s'|| ~ ||S r_s|| *
+        // sqrt(1 - (||dc|| / ||S r_s||)^2).  Refinement is not stopped merely by
+        // ||r_s|| < abs_tol: the early exit must see an x_s as good as the
+        // reference's.
         const int steps = sketch_refine_max_steps();
-        double prev = rnorm;
+        double* h = (double*)work;   // n doubles; the workspace is idle here
+        double* hp = (double*)C.host_pinned;
         bool refined = false;
         for (int s = 0; s < steps; ++s) {
-            SKL_CUDA(cudaMemcpyAsync(yv, cvec, rank * sizeof(double), cudaMemcpyDeviceToDevice, st));
-            sketch_refine_step(P, bptr, bent, hidx, (int)k, m, in.b, rs, gm, xacc, cvec, x_dev, part,
-                               scal, st);
-            SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, sizeof(double), cudaMemcpyDeviceToHost, st));
+            sketch_refine_direction(P, bptr, bent, hidx, (int)k, m, rs, gm, h, xacc, yv, part,
+                                    scal + 2, st);
+            SKL_CUDA(cudaMemcpyAsync(hp, scal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
             SKL_CUDA(cudaStreamSynchronize(st));
-            const double rn = ((double*)C.host_pinned)[0];
-            refined = true;
-            if (!(rn < prev)) {
-                // no progress (cond(R) too large for the FP32 factor): keep the previous c
-                SKL_CUDA(cudaMemcpyAsync(cvec, yv, rank * sizeof(double), cudaMemcpyDeviceToDevice, st));
-                SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
-                precond_apply(P, cvec, x_dev, ysplit, st);
+            if (!(hp[1] >= 0.5 * hp[0])) break;
+            sketch_refine_apply(P, 1.0, yv, cvec, in.b, x_dev, rs, part, scal + 4, st);
+            SKL_CUDA(cudaMemcpyAsync(hp, scal + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
+            SKL_CUDA(cudaStreamSynchronize(st));
+            const double rn = hp[0];
+            if (!(rn < rnorm)) {
+                // no progress (cond(R) too large for the FP32 factor): undo the step
+                sketch_refine_apply(P, -1.0, yv, cvec, in.b, x_dev, rs, part, scal + 4, st);
                 break;
             }
-            const bool slow = rn > 0.5 * prev;
-            prev = rn;
+            rnorm = rn;
+            refined = true;
             ++info.sketch_refine_steps;
-            if (slow) break;   // at the floor: further steps cannot lower ||r_s||
         }
-        if (refined) {
-            residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
-            SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaStreamSynchronize(st));
-            rnorm = ((double*)C.host_pinned)[0];
-        }
+        if (refined) residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
+        // host_pinned[0..1] = ||r_s||, ||A^T r_s|| again for the checks below
+        SKL_CUDA(cudaMemcpyAsync(hp, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        rnorm = hp[0];
         trace_phase(st, "sketch refinement");
     }
     SKL_CUDA(cudaEventRecord(ev[5], st));

@@ -210,14 +210,18 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
 // (512 doubles) are scratch.
 void residual_and_backward(const LsqrProblem& P, const double* x, const double* b, double* r,
                            double* part, double* out, cudaStream_t st);
-// One refinement step of the explicit sketch solution (sparse path): with
-// rs = b - A x on entry, c += M^T D P1^T A^T S^T S rs, x = D P1 M c (all d
-// entries written), rs = b - A x and *rnorm = ||rs||.  gm (m) and t (r) are
-// scratch.
-void sketch_refine_step(const LsqrProblem& P, const int* bptr, const unsigned* bent,
-                        const unsigned* hidx, int k, int64_t m, const double* b, double* rs,
-                        double* gm, double* t, double* c, double* x, double* part,
-                        double* rnorm, cudaStream_t st);
+// Refinement of the explicit sketch solution (sparse path).  Direction: with
+// rs = b - A x, gm = S rs, dc = M^T D P1^T A^T S^T gm (= Q1^T S rs up to the
+// FP32 factor's error), norms[0] = ||gm||, norms[1] = ||dc||; h (n), t (r)
+// and part (512) are scratch.  Apply: c += sgn * dc, x = D P1 M c (all d
+// entries written), rs = b - A x, *rnorm = ||rs||.
+void sketch_refine_direction(const LsqrProblem& P, const int* bptr, const unsigned* bent,
+                             const unsigned* hidx, int k, int64_t m, const double* rs, double* gm,
+                             double* h, double* t, double* dc, double* part, double* norms,
+                             cudaStream_t st);
+void sketch_refine_apply(const LsqrProblem& P, double sgn, const double* dc, double* c,
+                         const double* b, double* x, double* rs, double* part, double* rnorm,
+                         cudaStream_t st);
 void split_values(const double* x, int64_t n, float2* out, cudaStream_t st);
 void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out, cudaStream_t st);
 template <typename T>
