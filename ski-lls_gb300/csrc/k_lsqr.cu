@@ -32,15 +32,63 @@
 
 namespace skl {
 
+// Scalars every thread of a product kernel needs (ratios, reciprocals, the
+// Givens update's coefficients) are formed once by the thread that finalises
+// the norm they depend on, not per thread: GB300 issues FP64 at 1/64 of the
+// FP32 rate, and a division repeated by every warp of a grid cost several us
+// per kernel.
 struct LsqrState {
     double alpha, beta, alpha_new, rhobar, phibar, nrm_a, nrm_ar, tol;
     long long it, max_it;
     int done, flag;
     unsigned cnt[4];
+    double coef_n;      // alpha / beta: spmv_n's uh = A z - coef_n uh
+    double ib;          // 1 / beta:     spmv_t's t = A^T uh / beta
+    double coef_t;      // beta / alpha: tri_t's vh = M^T t - coef_t vh
+    double up_t1, up_t2, up_ia;   // update: y += t1 w, w = v + t2 w, v = vh / alpha
+    float2 coef_n_ff;   // coef_n as a (hi, lo) float pair
 };
 
+// beta is final: the ratios spmv_t and tri_t use (one thread)
+SKL_DEV void state_after_beta(LsqrState* S, double beta)
+{
+    S->beta = beta;
+    S->ib = beta > 0.0 ? 1.0 / beta : 0.0;
+    S->coef_t = S->alpha > 0.0 ? beta / S->alpha : 0.0;
+}
+
+// alpha (S->alpha) and beta final for the next spmv_n (one thread)
+SKL_DEV void state_coef_n(LsqrState* S)
+{
+    const double c = S->beta > 0.0 ? S->alpha / S->beta : 0.0;
+    S->coef_n = c;
+    ff f = ff_from_double(c);
+    S->coef_n_ff = make_float2(f.hi, f.lo);
+}
+
+// alpha' is final: the Givens rotation and the update's coefficients (one thread)
+SKL_DEV void state_update_coefs(LsqrState* S)
+{
+    const double alpha_old = S->alpha;
+    const double beta = S->beta;
+    // the reference skips the A^T u step when beta == 0 (IterSolver.cpp:242)
+    const double alpha = beta > 0.0 ? S->alpha_new : alpha_old;
+    const double rho = sqrt(S->rhobar * S->rhobar + beta * beta);
+    const double cs = S->rhobar / rho, sn = beta / rho;
+    const double theta = sn * alpha;
+    const double phi = cs * S->phibar;
+    S->up_t1 = phi / rho;
+    S->up_t2 = -theta / rho;
+    S->up_ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+}
+
 constexpr int kLThreads = 256;
-constexpr int kTriThreads = 128;   // threads per row pair of the triangular products
+// Threads per row pair of the triangular products.  r = 4,950 gives 2,475
+// pairs of equal length: 17 blocks per SM must be co-resident (16.3 on
+// average) for one wave, which 96-thread blocks at <= 40 registers allow;
+// 128-thread blocks left a second wave on part of the GPU.
+constexpr int kTriThreads = 96;
+constexpr int kTriMinBlocks = 17;
 
 // Fixed-order reduction of partials[0..np) by one block; result to *out.
 SKL_DEV double block_reduce_partials(const double* partials, int np)
@@ -194,7 +242,7 @@ SKL_DEV void block_reduce2(Acc<MIXED>& a, Acc<MIXED>& b, Acc<MIXED>* sm)
 // z[cols[i]] = colscale[cols[i]] * sum_{j>=i} M[i][j] v[j]   (Mr row-major)
 // One block per row pair (i, r-1-i): every block reads ~r+1 entries.
 template <bool MIXED>
-__global__ void __launch_bounds__(kTriThreads)
+__global__ void __launch_bounds__(kTriThreads, MIXED ? kTriMinBlocks : 1)
 k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED>* __restrict__ v,
         const int* __restrict__ cols, const double* __restrict__ colscale,
         ValT<MIXED>* __restrict__ z, const LsqrState* __restrict__ S, int plain_out,
@@ -228,13 +276,13 @@ k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED
 // ------------------------------------------------------------- tri_t -----
 // vh[j] = sum_{i<=j} M[i][j] t[i] - coef * vh[j], coef = beta'/alpha (0 at init)
 template <bool MIXED>
-__global__ void __launch_bounds__(kTriThreads)
+__global__ void __launch_bounds__(kTriThreads, MIXED ? kTriMinBlocks : 1)
 k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED>* __restrict__ t,
         double* __restrict__ vh, LsqrState* __restrict__ S, int init, double* __restrict__ partials)
 {
     if (S->done) return;
     __shared__ Acc<MIXED> sm[2 * kTriThreads / 32];
-    const double coef = init ? 0.0 : (S->alpha > 0.0 ? S->beta / S->alpha : 0.0);
+    const double coef = init ? 0.0 : S->coef_t;
     const int npairs = (r + 1) / 2;
     double ss = 0.0;
     for (int pidx = blockIdx.x; pidx < npairs; pidx += gridDim.x) {
@@ -267,26 +315,58 @@ k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
             S->alpha_new = sqrt(tot);
+            if (!init) state_update_coefs(S);
             S->cnt[1] = 0;
         }
     }
 }
 
-// Loads of four (index, value) entries p, p+L, p+2L, p+3L of one row or
-// column, predicated on p < p1 (index 0 and value 0 past the end, so the
+// Loads of U (index, value) entries p, p+L, ..., p+(U-1)L of one row or
+// column, predicated on q < p1 (index 0 and value 0 past the end, so the
 // matching gather reads a valid element and contributes nothing).
-template <bool MIXED, int L>
-SKL_DEV void load_group4(const int* __restrict__ idx, const ValT<MIXED>* __restrict__ val, int p,
-                         int p1, int (&ii)[4], ValT<MIXED> (&aa)[4])
+template <bool MIXED, int L, int U>
+SKL_DEV void load_group(const int* __restrict__ idx, const ValT<MIXED>* __restrict__ val, int p,
+                        int p1, int (&ii)[U], ValT<MIXED> (&aa)[U])
 {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < U; ++k) {
         const int q = p + k * L;
         const bool ok = q < p1;
         ii[k] = ok ? idx[q] : 0;
         aa[k] = ok ? val[q] : ValT<MIXED>{};
     }
 }
+
+template <bool MIXED, int L>
+SKL_DEV void load_group4(const int* __restrict__ idx, const ValT<MIXED>* __restrict__ val, int p,
+                         int p1, int (&ii)[4], ValT<MIXED> (&aa)[4])
+{
+    load_group<MIXED, L, 4>(idx, val, p, p1, ii, aa);
+}
+
+// The old u of one row for spmv_n's recurrence: a float pair read from us
+// on the mixed path (uh is not kept there), the FP64 uh otherwise.
+template <bool MIXED>
+struct UOld {
+    ff v{0.f, 0.f};
+    SKL_DEV static UOld load(const double*, const float2* us, int i)
+    {
+        UOld o;
+        const float2 t = us[i];
+        o.v = ff{t.x, t.y};
+        return o;
+    }
+};
+template <>
+struct UOld<false> {
+    double v = 0.0;
+    SKL_DEV static UOld load(const double* uh, const double*, int i)
+    {
+        UOld o;
+        o.v = uh[i];
+        return o;
+    }
+};
 
 // ---------------------------------------------------------- spmv_n (CSR) --
 // uh[i] = sum_j A[i][j] z[j] - coef * uh[i], coef = alpha/beta (0 at init with
@@ -322,11 +402,13 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
     const int lane = threadIdx.x % L;
     const int grp = threadIdx.x / L;
     const int ngrp = kLThreads / L;
-    const double coef = S->beta > 0.0 ? S->alpha / S->beta : 0.0;
+    const double coef = S->coef_n;
+    const ff coef_ff{S->coef_n_ff.x, S->coef_n_ff.y};
     const int r0 = blockIdx.x * rows_per_block;
     const int r1 = min(n, r0 + rows_per_block);
     const int warp_grp0 = (threadIdx.x >> 5) * (32 / L);
     double ss = 0.0;
+    ff ssf{0.f, 0.f};
     for (int t0 = r0; t0 < r1; t0 += kRowTile) {
         const int t1 = min(r1, t0 + kRowTile);
         __syncthreads();   // z staged; the previous tile's pointers are no longer read
@@ -337,11 +419,11 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
         int pb = 0, p1 = 0;
         int cc[4];
         V aa[4];
-        double uo = 0.0;
+        UOld<MIXED> uo;
         if (act) {
             pb = rps[i - t0] + lane;
             p1 = rps[i - t0 + 1];
-            if (lane == 0) uo = uh[i];
+            if (lane == 0) uo = UOld<MIXED>::load(uh, us, i);
         }
         load_group4<MIXED, L>(ci, cv, pb, p1, cc, aa);
         for (int base = t0 + warp_grp0; base < t1; base += ngrp) {
@@ -350,11 +432,11 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
             int npb = 0, np1 = 0;
             int nc[4];
             V na[4];
-            double nuo = 0.0;
+            UOld<MIXED> nuo;
             if (nact) {
                 npb = rps[ni - t0] + lane;
                 np1 = rps[ni - t0 + 1];
-                if (lane == 0) nuo = uh[ni];
+                if (lane == 0) nuo = UOld<MIXED>::load(uh, us, ni);
             }
             load_group4<MIXED, L>(ci, cv, npb, np1, nc, na);
             Acc<MIXED> acc, acc2;
@@ -384,10 +466,18 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
 #pragma unroll
             for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
             if (act && lane == 0) {
-                double nv = acc.value() - coef * uo;
-                uh[i] = nv;
-                us[i] = store_val<MIXED>(nv);
-                ss += nv * nv;
+                if constexpr (MIXED) {
+                    // float-float throughout: uh lives only as the pair us
+                    ff nv = acc.a;
+                    ff_fma(nv, ff{-coef_ff.hi, -coef_ff.lo}, uo.v);
+                    us[i] = make_float2(nv.hi, nv.lo);
+                    ff_fma(ssf, nv, nv);
+                } else {
+                    double nv = acc.value() - coef * uo.v;
+                    uh[i] = nv;
+                    us[i] = store_val<MIXED>(nv);
+                    ss += nv * nv;
+                }
             }
             i = ni;
             act = nact;
@@ -401,6 +491,7 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
             }
         }
     }
+    if constexpr (MIXED) ss = ff_to_double(ssf);
     ss = warp_sum(ss);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = ss;
     __syncthreads();
@@ -412,7 +503,7 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
     if (arrive_last(&S->cnt[0])) {
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
-            S->beta = sqrt(tot);
+            state_after_beta(S, sqrt(tot));
             S->cnt[0] = 0;
         }
     }
@@ -420,9 +511,14 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
 
 // --------------------------------------------------------- spmv_t (CSC) --
 // t[i] = colscale[c] * (sum_{p in col c} A[p] u[row p]) / beta,  c = cols[i]
-// L lanes per column; the (index, value) loads of the next group of four per
-// lane are issued before the gathers of the current group are consumed, so
-// the HBM stream of A overlaps the L2 gathers of u.
+// L lanes per column, kTU entries per lane per step; the (index, value) loads
+// of the next step are issued before the gathers of the current step are
+// consumed, so the HBM stream of A overlaps the L2 gathers of u.  Each warp
+// walks one long column, so the kernel is bound by how many bytes each warp
+// keeps in flight: 8 entries per lane per step (12 B each) halves the
+// dependent steps per column against 4.
+constexpr int kTU = 8;
+
 template <bool MIXED, int L>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<MIXED>* __restrict__ cv,
@@ -436,7 +532,7 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L;
     const int ng = (gridDim.x * blockDim.x) / L;
     const int gw0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 / L);  // first group of this warp
-    const double ib = S->beta > 0.0 ? 1.0 / S->beta : 0.0;
+    const double ib = S->ib;
     // warp-uniform trip count (see k_spmv_n_csr)
     for (int base = gw0; base < r; base += ng) {
         const int i = base + (g - gw0);
@@ -447,23 +543,24 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
             c = cols[i];
             const int p1 = cp[c + 1];
             int pb = cp[c] + lane;
-            int rr[4];
-            V aa[4];
-            load_group4<MIXED, L>(ri, cv, pb, p1, rr, aa);
+            int rr[kTU];
+            V aa[kTU];
+            load_group<MIXED, L, kTU>(ri, cv, pb, p1, rr, aa);
             while (pb < p1) {
-                V uu[4];
+                V uu[kTU];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) uu[k] = us[rr[k]];
-                const int pn = pb + 4 * L;
-                int rn[4];
-                V an[4];
-                load_group4<MIXED, L>(ri, cv, pn, p1, rn, an);
-                acc.fma_mv(aa[0], uu[0]);
-                acc2.fma_mv(aa[1], uu[1]);
-                acc.fma_mv(aa[2], uu[2]);
-                acc2.fma_mv(aa[3], uu[3]);
+                for (int k = 0; k < kTU; ++k) uu[k] = us[rr[k]];
+                const int pn = pb + kTU * L;
+                int rn[kTU];
+                V an[kTU];
+                load_group<MIXED, L, kTU>(ri, cv, pn, p1, rn, an);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
+                for (int k = 0; k < kTU; k += 2) {
+                    acc.fma_mv(aa[k], uu[k]);
+                    acc2.fma_mv(aa[k + 1], uu[k + 1]);
+                }
+#pragma unroll
+                for (int k = 0; k < kTU; ++k) {
                     rr[k] = rn[k];
                     aa[k] = an[k];
                 }
@@ -506,7 +603,7 @@ k_spmv_n_dense_reduce(const double* __restrict__ part, int nchunks, int n, doubl
 {
     if (S->done) return;
     __shared__ double red[kLThreads / 32];
-    const double coef = S->beta > 0.0 ? S->alpha / S->beta : 0.0;
+    const double coef = S->coef_n;
     double ss = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double s = 0.0;
@@ -521,7 +618,7 @@ k_spmv_n_dense_reduce(const double* __restrict__ part, int nchunks, int n, doubl
     if (arrive_last(&S->cnt[0])) {
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
-            S->beta = sqrt(tot);
+            state_after_beta(S, sqrt(tot));
             S->cnt[0] = 0;
         }
     }
@@ -536,7 +633,7 @@ k_spmv_t_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int*
 {
     if (S->done) return;
     __shared__ Acc<MIXED> red[kLThreads / 32];
-    const double ib = S->beta > 0.0 ? 1.0 / S->beta : 0.0;
+    const double ib = S->ib;
     for (int i = blockIdx.x; i < r; i += gridDim.x) {
         const int c = cols[i];
         const ValT<MIXED>* col = A + (int64_t)c * lda;
@@ -575,7 +672,7 @@ k_lsqr_init_u(const double* __restrict__ b, int n, double* __restrict__ uh,
     if (arrive_last(&S->cnt[0])) {
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
-            S->beta = sqrt(tot);
+            state_after_beta(S, sqrt(tot));
             S->cnt[0] = 0;
         }
     }
@@ -606,6 +703,7 @@ k_lsqr_init_v(int r, double* __restrict__ vh, ValT<MIXED>* __restrict__ vs, doub
             S->flag = 1;
             S->done = (alpha * beta == 0.0) ? 1 : 0;
             if (S->done) S->flag = 0;
+            state_coef_n(S);
             S->cnt[2] = 0;
         }
     }
@@ -618,16 +716,8 @@ k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs
               double* __restrict__ w, double* __restrict__ y, LsqrState* __restrict__ S)
 {
     if (S->done) return;
-    const double alpha_old = S->alpha;
     const double beta = S->beta;
-    // the reference skips the A^T u step when beta == 0 (IterSolver.cpp:242)
-    const double alpha = beta > 0.0 ? S->alpha_new : alpha_old;
-    const double rho = sqrt(S->rhobar * S->rhobar + beta * beta);
-    const double cs = S->rhobar / rho, sn = beta / rho;
-    const double theta = sn * alpha;
-    const double phi = cs * S->phibar;
-    const double t1 = phi / rho, t2 = -theta / rho;
-    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    const double t1 = S->up_t1, t2 = S->up_t2, ia = S->up_ia;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
         double v = (beta > 0.0) ? vh[i] * ia : 0.0;
         if (beta > 0.0) vs[i] = store_val<MIXED>(v);
@@ -637,6 +727,10 @@ k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs
     }
     if (arrive_last(&S->cnt[3])) {
         if (threadIdx.x == 0) {
+            const double alpha_old = S->alpha;
+            const double alpha = beta > 0.0 ? S->alpha_new : alpha_old;
+            const double rho = sqrt(S->rhobar * S->rhobar + beta * beta);
+            const double cs = S->rhobar / rho, sn = beta / rho;
             double nrm_a = S->nrm_a;
             if (beta > 0.0) nrm_a = sqrt(nrm_a * nrm_a + alpha_old * alpha_old + beta * beta);
             const double phibar = sn * S->phibar;
@@ -644,6 +738,7 @@ k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs
             S->phibar = phibar;
             S->nrm_a = nrm_a;
             S->alpha = alpha;
+            state_coef_n(S);
             S->it += 1;
             const double nrm_ar = phibar * alpha * fabs(cs);
             S->nrm_ar = nrm_ar;
