@@ -347,12 +347,16 @@ __global__ void k_splitk_reduce(int M, int N, int splits, T alpha, const T* __re
 }
 
 // Picks a split-K factor so that the grid covers the GPU when the output is
-// small and K is long.  partial must hold splits*M*N entries when splits > 1.
+// small and K is long (down to 64 rows of K per split, up to 128 splits: a
+// 64 x 64 Gram over 8,000 rows then runs on 64 CTAs instead of 16).  partial
+// must hold splits*M*N entries when splits > 1.
+constexpr int kSplitMinK = 64;
+constexpr int kSplitMax = 128;
 inline int gemm_splits(int M, int N, int K)
 {
     int tiles = ((M + kGBM - 1) / kGBM) * ((N + kGBN - 1) / kGBN);
     int s = 1;
-    while (tiles * s < 2 * 152 && K / (s * 2) >= 256 && s < 32) s *= 2;
+    while (tiles * s < 2 * 152 && K / (s * 2) >= kSplitMinK && s < kSplitMax) s *= 2;
     return s;
 }
 
@@ -372,7 +376,7 @@ inline int sgemm_splits(int M, int N, int K, int bm)
 {
     int tiles = ((M + bm - 1) / bm) * ((N + kSBN - 1) / kSBN);
     int s = 1;
-    while (tiles * s < 2 * 152 && K / (s * 2) >= 256 && s < 32) s *= 2;
+    while (tiles * s < 2 * 152 && K / (s * 2) >= kSplitMinK && s < kSplitMax) s *= 2;
     return s;
 }
 

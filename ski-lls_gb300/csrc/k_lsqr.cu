@@ -91,11 +91,23 @@ constexpr int kTriThreads = 96;
 constexpr int kTriMinBlocks = 17;
 
 // Fixed-order reduction of partials[0..np) by one block; result to *out.
+// Eight loads per thread are issued before their (ordered) adds: with 2,475
+// partials and 96 threads a load-add-load chain was ~9 us of L2 latency in
+// the grid's last block.
 SKL_DEV double block_reduce_partials(const double* partials, int np)
 {
     __shared__ double red[kLThreads / 32];
     double s = 0.0;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+    const int nt = blockDim.x;
+    int i = threadIdx.x;
+    for (; i + 7 * nt < np; i += 8 * nt) {
+        double v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = partials[i + k * nt];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s += v[k];
+    }
+    for (; i < np; i += nt) s += partials[i];
     return block_sum(s, red);
 }
 

@@ -98,6 +98,71 @@ SKL_DEV void householder(T alpha, T sigma2, T& beta, T& tau, T& scale)
 //   local argmax -> publish candidate (norm, index, column) -> cluster barrier
 //   -> every CTA reads all 16 candidates in one batched DSMEM round trip ->
 //   same winner and Householder vector everywhere -> thread-per-column update.
+// Column moves for a panel from its b selections (b <= 64): selected columns
+// go to the front in selection order; the displaced low positions (not
+// selected), in increasing order, fill the vacated high positions (selected
+// with index >= b) in increasing order.  plan_src/plan_dst hold b + (number of
+// high selections) moves.  A selection outside [0, N) or a repeated one (only
+// possible after non-finite values) flags status and plans no move.  Called
+// by every thread of one block (a multiple of 32 threads); s_sel, in_low and
+// lowpos (kMaxNb each) are shared.  Warp ballots replace the O(b^2) loops.
+SKL_DEV void perm_plan_block(const int* s_sel, int* in_low, int* lowpos, int b, int N,
+                             int* __restrict__ plan_src, int* __restrict__ plan_dst,
+                             int* __restrict__ plan_n, unsigned* __restrict__ status)
+{
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+    const unsigned full = 0xffffffffu;
+    // warp wid checks selections wid, wid + nw, ...: range and repeats
+    bool bad = false;
+    for (int tt = wid; tt < b; tt += nw) {
+        const int v = s_sel[tt];
+        const bool dup = (lane < tt && s_sel[lane] == v) || (lane + 32 < tt && s_sel[lane + 32] == v);
+        bad = bad || __any_sync(full, dup) || v < 0 || v >= N;
+    }
+    if (t < kMaxNb) in_low[t] = 0;
+    if (__syncthreads_or(bad)) {
+        if (t == 0) {
+            *plan_n = 0;
+            dev_flag(status, kDevErrQrSelect);
+        }
+        return;
+    }
+    if (t < b && s_sel[t] < b) in_low[s_sel[t]] = 1;
+    __syncthreads();
+    if (wid == 0) {
+        // displaced low positions, increasing
+        int base = 0;
+        for (int c = 0; c < b; c += 32) {
+            const int pos = c + lane;
+            const bool z = pos < b && !in_low[pos];
+            const unsigned m = __ballot_sync(full, z);
+            if (z) lowpos[base + __popc(m & ((1u << lane) - 1u))] = pos;
+            base += __popc(m);
+        }
+    }
+    __syncthreads();
+    for (int tt = wid; tt < b; tt += nw) {
+        const int hs = s_sel[tt];
+        if (lane == 0) {
+            plan_src[tt] = hs;
+            plan_dst[tt] = tt;
+        }
+        if (hs >= b) {
+            // rank of hs among the high selections
+            const int u0 = lane < b ? s_sel[lane] : -1;
+            const int u1 = lane + 32 < b ? s_sel[lane + 32] : -1;
+            const int rk = __popc(__ballot_sync(full, u0 >= b && u0 < hs)) +
+                           __popc(__ballot_sync(full, u1 >= b && u1 < hs));
+            if (lane == 0) {
+                plan_src[b + rk] = lowpos[rk];
+                plan_dst[b + rk] = hs;
+            }
+        }
+    }
+    const int n_extra = __syncthreads_count(t < b && s_sel[t] >= b);
+    if (t == 0) *plan_n = b + n_extra;
+}
+
 template <typename T>
 struct YqrpSmem {
     __host__ __device__ static int ldp(int nbp) { return nbp | 1; }
@@ -117,7 +182,9 @@ struct YqrpSmem {
 
 template <typename T>
 __global__ void __launch_bounds__(kYThreads)
-k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel)
+k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel,
+       int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
+       unsigned* __restrict__ status)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned crank = cluster_ctarank();
@@ -138,6 +205,9 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     __shared__ T s_cv[kCluster];
     __shared__ int s_ci[kCluster];
     __shared__ int s_local;
+    __shared__ int s_sel[kMaxNb];   // CTA 0: the selections, for the move plan
+    __shared__ int s_inlow[kMaxNb];
+    __shared__ int s_lowpos[kMaxNb];
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int e = tid; e < nbp * ncols; e += kYThreads) {
@@ -225,7 +295,10 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         householder(wc[s], sg, beta, tau, scale);
         const int win_local = (oi >= c0 && oi < c0 + ncols) ? oi - c0 : -1;
         if (tid == 0) {
-            if (crank == 0) sel[s] = oi;
+            if (crank == 0) {
+                sel[s] = oi;
+                s_sel[s] = oi;
+            }
             if (win_local >= 0) taken[win_local] = 1;   // read again only after the next barrier
         }
         // (c) H = I - tau v v^T on the untaken local columns, new norms (rows > s):
@@ -260,6 +333,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         }
         __syncthreads();
     }
+    // CTA 0 plans the panel's column moves while the cluster drains
+    if (crank == 0) perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
     cluster_sync();   // keep shared memory alive until every CTA finished reading it
 }
 
@@ -267,103 +342,47 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
 // Moves the selected columns (sel, relative to j0) to positions j0..j0+b-1;
 // the columns they displace fill the vacated positions in increasing order.
 // plan: src[t] for t in [0, 2b): dest position dst[t] (relative) <- src.
-__global__ void k_perm_plan(const int* __restrict__ sel, int b, int N, int* __restrict__ plan_src,
-                            int* __restrict__ plan_dst, int* __restrict__ plan_n,
-                            unsigned* __restrict__ status)
-{
-    // one warp: lanes own positions t and t+32 (b <= 64)
-    __shared__ int s_sel[kMaxNb];
-    __shared__ int in_low[kMaxNb];
-    const int lane = threadIdx.x;
-    for (int t = lane; t < kMaxNb; t += 32) {
-        s_sel[t] = t < b ? sel[t] : -1;
-        in_low[t] = 0;
-    }
-    __syncwarp();
-    // a selection outside [0, N) or a repeated one (only possible after
-    // non-finite values): flag it and leave the columns where they are
-    bool badsel = false;
-    for (int t = lane; t < b; t += 32) {
-        const int v = s_sel[t];
-        bool bad = v < 0 || v >= N;
-        for (int u = 0; u < t; ++u) bad = bad || s_sel[u] == v;
-        badsel = badsel || bad;
-    }
-    if (__any_sync(0xffffffffu, badsel)) {
-        if (lane == 0) {
-            *plan_n = 0;
-            dev_flag(status, kDevErrQrSelect);
-        }
-        return;
-    }
-    for (int t = lane; t < b; t += 32)
-        if (s_sel[t] < b) in_low[s_sel[t]] = 1;
-    __syncwarp();
-    // selected columns go to the front in selection order
-    for (int t = lane; t < b; t += 32) {
-        plan_src[t] = s_sel[t];
-        plan_dst[t] = t;
-    }
-    // displaced low positions (not selected), in increasing order, fill the
-    // vacated high positions (selected with index >= b) in increasing order
-    int n_extra = 0;
-    for (int t = lane; t < b; t += 32) {
-        const int hs = s_sel[t];
-        if (hs >= b) {
-            // rank of hs among the high selections
-            int rk = 0;
-            for (int u = 0; u < b; ++u) rk += (s_sel[u] >= b && s_sel[u] < hs) ? 1 : 0;
-            // the rk-th displaced low position
-            int cnt = -1, pos = 0;
-            for (pos = 0; pos < b; ++pos) {
-                if (!in_low[pos]) ++cnt;
-                if (cnt == rk) break;
-            }
-            plan_src[b + rk] = pos;
-            plan_dst[b + rk] = hs;
-        }
-        n_extra += (hs >= b) ? 1 : 0;
-    }
-    for (int o = 16; o > 0; o >>= 1) n_extra += __shfl_xor_sync(0xffffffffu, n_extra, o);
-    if (lane == 0) *plan_n = b + n_extra;
-}
-
-// Copy the planned source columns of X (rows x cols, ld) into tmp, then
-// write them to their destinations.  Also permutes jpvt.
+// Planned column moves of A (rows m, ld), the sample Y (nbp rows, ldy) and
+// jpvt: gather every source column into scratch, then (next launch, after all
+// gathers) write them to their destinations.  Grid (x over rows of A, one y
+// per planned move); the x == 0 blocks also move Y's column and jpvt.
 template <typename T>
-__global__ void k_perm_gather(const T* __restrict__ X, int64_t ld, int rows, int j0,
+__global__ void k_perm_gather(const T* __restrict__ A, int64_t ld, int m, const T* __restrict__ Y,
+                              int ldy, int nbp, const int* __restrict__ jpvt, int j0,
                               const int* __restrict__ plan_src, const int* __restrict__ plan_n,
-                              T* __restrict__ tmp)
+                              T* __restrict__ tmpA, T* __restrict__ tmpY, int* __restrict__ tmpI)
 {
     const int q = blockIdx.y;
     if (q >= *plan_n) return;
-    const T* src = X + (int64_t)(j0 + plan_src[q]) * ld;
-    T* dst = tmp + (int64_t)q * rows;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    const int64_t c = j0 + plan_src[q];
+    const T* src = A + c * ld;
+    T* dst = tmpA + (int64_t)q * m;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
         dst[r] = src[r];
+    if (blockIdx.x == 0) {
+        for (int r = threadIdx.x; r < nbp; r += blockDim.x) tmpY[q * nbp + r] = Y[c * ldy + r];
+        if (threadIdx.x == 0) tmpI[q] = jpvt[c];
+    }
 }
 
 template <typename T>
-__global__ void k_perm_scatter(T* __restrict__ X, int64_t ld, int rows, int j0,
+__global__ void k_perm_scatter(T* __restrict__ A, int64_t ld, int m, T* __restrict__ Y, int ldy,
+                               int nbp, int* __restrict__ jpvt, int j0,
                                const int* __restrict__ plan_dst, const int* __restrict__ plan_n,
-                               const T* __restrict__ tmp)
+                               const T* __restrict__ tmpA, const T* __restrict__ tmpY,
+                               const int* __restrict__ tmpI)
 {
     const int q = blockIdx.y;
     if (q >= *plan_n) return;
-    T* dst = X + (int64_t)(j0 + plan_dst[q]) * ld;
-    const T* src = tmp + (int64_t)q * rows;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    const int64_t c = j0 + plan_dst[q];
+    T* dst = A + c * ld;
+    const T* src = tmpA + (int64_t)q * m;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
         dst[r] = src[r];
-}
-
-__global__ void k_perm_ints(int* __restrict__ jpvt, int j0, const int* __restrict__ plan_src,
-                            const int* __restrict__ plan_dst, const int* __restrict__ plan_n)
-{
-    __shared__ int vals[2 * kMaxNb];
-    const int n = *plan_n;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) vals[q] = jpvt[j0 + plan_src[q]];
-    __syncthreads();
-    for (int q = threadIdx.x; q < n; q += blockDim.x) jpvt[j0 + plan_dst[q]] = vals[q];
+    if (blockIdx.x == 0) {
+        for (int r = threadIdx.x; r < nbp; r += blockDim.x) Y[c * ldy + r] = tmpY[q * nbp + r];
+        if (threadIdx.x == 0) jpvt[c] = tmpI[q];
+    }
 }
 
 // ------------------------------------------------------------- panel ----
@@ -788,6 +807,8 @@ template <typename T>
 struct QrBuffers {
     T *G, *Y, *V, *Tm, *W, *Z, *GU, *GUT, *Bm, *part, *part2, *tmp;
     int *sel, *plan_src, *plan_dst, *plan_n, *chol_fail;
+    T* tmpY;      // 2 nb sample columns being moved
+    int* tmpI;    // 2 nb pivot indices being moved
     T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
     T* R12;                   // b x (d-j): rows j..j+b of the updated trailing matrix
     double *qw;
@@ -818,10 +839,12 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     if (cap < (int64_t)1 << 20) cap = (int64_t)1 << 20;
     B.part_cap = cap;
     B.part = (T*)take((size_t)cap * sizeof(T));
-    B.part2_cap = (int64_t)32 * p.nbp * p.nb;
+    B.part2_cap = (int64_t)kSplitMax * p.nbp * p.nb;
     B.part2 = (T*)take((size_t)B.part2_cap * sizeof(T));
     B.tmp_rows = m > p.nbp ? m : p.nbp;
     B.tmp = (T*)take((size_t)B.tmp_rows * 2 * p.nb * sizeof(T));
+    B.tmpY = (T*)take((size_t)p.nbp * 2 * p.nb * sizeof(T));
+    B.tmpI = (int*)take(2 * kMaxNb * sizeof(int));
     B.sel = (int*)take(kMaxNb * sizeof(int));
     B.plan_src = (int*)take(2 * kMaxNb * sizeof(int));
     B.plan_dst = (int*)take(2 * kMaxNb * sizeof(int));
@@ -975,7 +998,12 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         const T* Yc = B.Y;
         int* sel = B.sel;
         int nbv = nbp;
-        void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel};
+        int* psrc = B.plan_src;
+        int* pdst = B.plan_dst;
+        int* pn = B.plan_n;
+        unsigned* stp = status;
+        void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel, &psrc, &pdst,
+                        &pn, &stp};
         cudaEvent_t t0 = t.begin();
         launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
         t.end(0, t0);
@@ -997,16 +1025,14 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             if (j == 0) launch_yqrp(j, b, N, st, tm);
             trace_phase(st, "qr: yqrp");
             cudaEvent_t t0 = tm.begin();
-            k_perm_plan<<<1, 32, 0, st>>>(B.sel, b, N, B.plan_src, B.plan_dst, B.plan_n, status);
-            SKL_LAUNCHED();
+            // the sample QRP planned the moves (plan_src/plan_dst/plan_n)
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
-            k_perm_gather<T><<<gA, 256, 0, st>>>(A, ld, (int)m, jj, B.plan_src, B.plan_n, B.tmp);
-            k_perm_scatter<T><<<gA, 256, 0, st>>>(A, ld, (int)m, jj, B.plan_dst, B.plan_n, B.tmp);
-            dim3 gY(1, 2 * b);
-            k_perm_gather<T><<<gY, 128, 0, st>>>(B.Y, nbp, nbp, jj, B.plan_src, B.plan_n, B.tmp);
-            k_perm_scatter<T><<<gY, 128, 0, st>>>(B.Y, nbp, nbp, jj, B.plan_dst, B.plan_n, B.tmp);
-            k_perm_ints<<<1, 128, 0, st>>>(jpvt, jj, B.plan_src, B.plan_dst, B.plan_n);
-            for (int q = 0; q < 5; ++q) SKL_LAUNCHED();
+            k_perm_gather<T><<<gA, 256, 0, st>>>(A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_src,
+                                                 B.plan_n, B.tmp, B.tmpY, B.tmpI);
+            k_perm_scatter<T><<<gA, 256, 0, st>>>(A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_dst,
+                                                  B.plan_n, B.tmp, B.tmpY, B.tmpI);
+            SKL_LAUNCHED();
+            SKL_LAUNCHED();
             tm.end(1, t0);
         }
         {
