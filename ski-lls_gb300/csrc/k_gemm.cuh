@@ -335,8 +335,18 @@ __global__ void k_splitk_reduce(int M, int N, int splits, T alpha, const T* __re
     int64_t total = (int64_t)M * N;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
+        // splits summed in order, eight loads in flight (up to 128 splits of a
+        // small output: a load-add chain would wait on L2 once per split)
         T s = T(0);
-        for (int z = 0; z < splits; ++z) s += partial[(int64_t)z * total + e];
+        int z = 0;
+        for (; z + 8 <= splits; z += 8) {
+            T v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = partial[(int64_t)(z + q) * total + e];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s += v[q];
+        }
+        for (; z < splits; ++z) s += partial[(int64_t)z * total + e];
         int gm = (int)(e % M);
         int64_t gn = e / M;
         T* c = C + gm + gn * ldc;

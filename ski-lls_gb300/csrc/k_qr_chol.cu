@@ -14,215 +14,189 @@
 namespace skl {
 
 constexpr int kSmallThreads = 1024;
-constexpr int kSmallWarps = kSmallThreads / 32;
-constexpr int kMaxSmall = 64;
 
 // ---- small dense algebra on b x b (b <= 64) row-major shared-memory blocks --
-// Every routine is a rolled loop over elimination steps with one block
-// barrier per step; within a step, warps take rows and lanes take columns of
-// the block that changes.  (Fully unrolled register versions were tried:
-// their straight-line code, executed once, is bound by instruction fetch.)
-// The reciprocal of the next pivot is formed by the thread that finishes that
-// pivot, one step ahead, so no division sits on the per-step critical path.
+// The factorizations are blocked by 16: the 16 x 16 diagonal blocks are
+// factored and inverted by one warp (a step is a __syncwarp, not a block
+// barrier), and everything else is a block product over the whole CTA
+// (blk_mul).  A 64 x 64 Cholesky plus inverse is then 4 warp factorizations
+// and ~14 block barriers instead of 128 one-barrier elimination steps, each of
+// which had to wait for all 32 warps of the CTA.  Matrices are padded to
+// np = round_up(b, 16) rows/columns (identity for the Cholesky, zeros for the
+// LU input, which the modified LU turns into identity factors).
+constexpr int kDB = 16;   // diagonal block
 
-// Thread layout of the eliminations: thread t owns row t >> 4 and the four
-// columns 4 (t & 15) .. +3 (one float4 of a row; ld = b + 4 keeps rows
-// 16-byte aligned), so 1024 threads cover a 64 x 64 block and every step is
-// one vector read-modify-write per thread plus one barrier.
-template <typename T> struct Quad;
-template <> struct Quad<float> { using type = float4; };
-template <> struct Quad<double> { using type = double4; };
-
+// Warp-level 16 x 16 routines: lane l holds row l >> 1, columns 8 (l & 1) ..
+// +7 of the block in registers; row k reaches the other lanes by shuffles, so
+// a step is ~25 instructions with no shared-memory round trip.  The step
+// loops stay rolled (register elements picked by selects): a one-warp
+// straight-line version would wait on instruction fetch.
 template <typename T>
-SKL_DEV typename Quad<T>::type ld4(const T* p) { return *reinterpret_cast<const typename Quad<T>::type*>(p); }
-template <typename T>
-SKL_DEV void st4(T* p, typename Quad<T>::type v) { *reinterpret_cast<typename Quad<T>::type*>(p) = v; }
-template <typename T, typename V>
-SKL_DEV T q_at(const V& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
-template <typename T, typename V>
-SKL_DEV void q_set(V& v, int e, T x)
+SKL_DEV T sel8(const T (&a)[8], int i)
 {
-    if (e == 0) v.x = x;
-    else if (e == 1) v.y = x;
-    else if (e == 2) v.z = x;
-    else v.w = x;
+    T v = a[0];
+#pragma unroll
+    for (int e = 1; e < 8; ++e) v = (i == e) ? a[e] : v;
+    return v;
 }
 
-// In-place Cholesky G = R^T R of the symmetric b x b block G: R (upper,
-// zeros below) over G.  Rows stay unnormalised during the elimination and
-// are scaled by 1/sqrt(d_i) at the end.  inv: b scratch entries (1/d_k).
-// Sets *bad when a pivot is below 32 eps times its mass.
+// Element k of the lane's own row (k in either half of the row).
 template <typename T>
-SKL_DEV void chol_smem(T* G, int ld, int b, const T* __restrict__ mass, T eps, T* inv, int* bad)
+SKL_DEV T own_col(const T (&a)[8], int k, int lane)
 {
-    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-    const bool own = i < b && c0 < b;
-    if (threadIdx.x == 0) {
-        const T d = G[0];
-        const bool ok = d > T(32) * eps * mass[0] && mass[0] > T(0);
-        if (!ok) *bad = 1;
-        inv[0] = ok ? T(1) / d : T(0);
-    }
-    __syncthreads();
-    for (int k = 0; k < b - 1; ++k) {
-        if (own && i > k && c0 + 3 >= i) {
-            const T gki = G[k * ld + i] * inv[k];
-            auto row = ld4<T>(G + i * ld + c0);
-            const auto piv = ld4<T>(G + k * ld + c0);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int c = c0 + e;
-                if (c >= i && c < b) q_set<T>(row, e, q_at<T>(row, e) - gki * q_at<T>(piv, e));
-            }
-            st4<T>(G + i * ld + c0, row);
-            if (i == k + 1 && c0 <= i && i < c0 + 4) {   // next pivot, finished now
-                const T v = q_at<T>(row, i - c0);
-                const bool ok = v > T(32) * eps * mass[i] && mass[i] > T(0);
-                if (!ok) *bad = 1;
-                inv[i] = ok ? T(1) / v : T(0);
-            }
-        }
-        __syncthreads();
-    }
-    if (own) {
-        const T s = inv[i] > T(0) ? t_sqrt(inv[i]) : T(0);
-        auto row = ld4<T>(G + i * ld + c0);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int c = c0 + e;
-            q_set<T>(row, e, (c >= i) ? q_at<T>(row, e) * s : T(0));
-        }
-        st4<T>(G + i * ld + c0, row);
-    }
-    __syncthreads();
+    const T mine = sel8(a, k & 7);
+    const T other = __shfl_xor_sync(0xffffffffu, mine, 1);
+    return ((k >> 3) == (lane & 1)) ? mine : other;
 }
 
-// X = U^{-1} for the upper triangle of the b x b block U (entries below U's
-// diagonal never read).  Back substitution over all columns at once: step k
-// removes row k's contribution from rows i < k (columns c >= k), and row i
-// is final (scaled by 1/U_ii) after step i + 1.  Writes X's upper triangle,
-// and zeros below it when zero_lower (otherwise only the upper triangle is
-// written, so X may hold another triangle below).  inv: b scratch entries.
 template <typename T>
-SKL_DEV void inv_upper_smem(const T* U, int ldu, int b, T* X, int ldx, bool zero_lower, T* inv)
+SKL_DEV void row_load(const T* A, int ld, T (&a)[8])
 {
-    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-    const bool own = i < b && c0 < b;
-    for (int k = threadIdx.x; k < b; k += kSmallThreads) inv[k] = T(1) / U[k * ldu + k];
-    __syncthreads();
-    if (own) {
-        auto row = ld4<T>(X + i * ldx + c0);
+    const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int c = c0 + e;
-            if (c >= i) q_set<T>(row, e, (c == i) ? (i == b - 1 ? inv[i] : T(1)) : T(0));
-            else if (zero_lower) q_set<T>(row, e, T(0));
-        }
-        st4<T>(X + i * ldx + c0, row);
-    }
-    __syncthreads();
-    for (int k = b - 1; k >= 1; --k) {
-        // X[i][c] -= U[i][k] X[k][c] for i < k <= c; row k - 1 is then final
-        const bool has_diag = (i == k - 1) && c0 <= i && i < c0 + 4;
-        if (own && i < k && (c0 + 3 >= k || has_diag)) {
-            const T uik = U[i * ldu + k];
-            const T sc = (i == k - 1) ? inv[i] : T(1);
-            auto row = ld4<T>(X + i * ldx + c0);
-            const auto xk = ld4<T>(X + k * ldx + c0);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int c = c0 + e;
-                if (c >= k && c < b) q_set<T>(row, e, (q_at<T>(row, e) - uik * q_at<T>(xk, e)) * sc);
-                else if (c == i && i == k - 1) q_set<T>(row, e, inv[i]);
-            }
-            st4<T>(X + i * ldx + c0, row);
-        }
-        __syncthreads();
-    }
+    for (int e = 0; e < 8; ++e) a[e] = A[r * ld + cb + e];
 }
 
-// Y = L^{-1} for the unit lower triangle of L (strict lower part read):
-// Y's strict lower part only (unit diagonal implied).  Forward substitution
-// over all columns at once: step k removes row k from rows i > k.
+// In-place Cholesky of the symmetric 16 x 16 block A (both triangles hold the
+// current values): R (upper, normalised, zeros below) over A.  Rows stay
+// unnormalised during the elimination and are scaled by 1/sqrt(d) at the end.
+// Sets *bad when a pivot is not above 32 eps times its mass.
 template <typename T>
-SKL_DEV void inv_unit_lower_smem(const T* L, int ldl, int b, T* Y, int ldy)
+SKL_DEV void warp16_chol(T* A, int ld, const T* __restrict__ mass, T eps, int* bad)
 {
-    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-    const bool own = i < b && c0 < b;
-    // Y's strict lower part starts at zero; row k of Y is final before step k
-    if (own) {
-        auto row = ld4<T>(Y + i * ldy + c0);
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
+    T a[8];
+    row_load(A, ld, a);
+    bool isbad = false;
+#pragma unroll 1
+    for (int k = 0; k < kDB; ++k) {
+        const T d = __shfl_sync(full, sel8(a, k & 7), 2 * k + (k >> 3));
+        const T ms = mass[k];
+        const bool ok = d > T(32) * eps * ms && ms > T(0);
+        isbad = isbad || !ok;
+        const T inv = ok ? T(1) / d : T(0);
+        T rk[8];
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
-            if (c0 + e < i) q_set<T>(row, e, T(0));
-        st4<T>(Y + i * ldy + c0, row);
-    }
-    __syncthreads();
-    for (int k = 0; k < b - 1; ++k) {
-        if (own && i > k && c0 <= k) {
-            const T lik = L[i * ldl + k];
-            auto row = ld4<T>(Y + i * ldy + c0);
-            const auto yk = ld4<T>(Y + k * ldy + c0);
+        for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
+        const T g = own_col(a, k, lane) * inv;   // A[r][k] = A[k][r]
+        if (r > k) {
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int c = c0 + e;
-                if (c <= k) q_set<T>(row, e, q_at<T>(row, e) - lik * (c == k ? T(1) : q_at<T>(yk, e)));
-            }
-            st4<T>(Y + i * ldy + c0, row);
+            for (int e = 0; e < 8; ++e)
+                if (cb + e > k) a[e] -= g * rk[e];
         }
-        __syncthreads();
     }
+    if (isbad && lane == 0) *bad = 1;
+    const T d = own_col(a, r, lane);
+    const T sc = d > T(0) ? T(1) / t_sqrt(d) : T(0);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) A[r * ld + cb + e] = (cb + e >= r) ? a[e] * sc : T(0);
+    __syncwarp();
 }
 
-// Modified LU without pivoting of the b x b block A in place: S_k =
+// X = U^{-1} for the upper 16 x 16 block U (entries below its diagonal never
+// read): X's upper triangle, and zeros below it when zero_lower.
+template <typename T>
+SKL_DEV void warp16_inv_upper(const T* U, int ldu, T* X, int ldx, bool zero_lower)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
+    const T iv = lane < kDB ? T(1) / U[lane * ldu + lane] : T(0);
+    T x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) x[e] = (cb + e == r) ? T(1) : T(0);
+#pragma unroll 1
+    for (int k = kDB - 1; k >= 0; --k) {
+        const T ik = __shfl_sync(full, iv, k);
+        const T u = U[r * ldu + k];
+        if (r == k) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) x[e] *= ik;
+        }
+        T xk[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) xk[e] = __shfl_sync(full, x[e], 2 * k + (lane & 1));
+        if (r < k) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) x[e] -= u * xk[e];
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int c = cb + e;
+        if (c >= r) X[r * ldx + c] = x[e];
+        else if (zero_lower) X[r * ldx + c] = T(0);
+    }
+    __syncwarp();
+}
+
+// Y = L^{-1} for the unit lower 16 x 16 block L (strict lower part read):
+// Y's strict lower part only (unit diagonal implied).
+template <typename T>
+SKL_DEV void warp16_inv_unit_lower(const T* L, int ldl, T* Y, int ldy)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
+    T y[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) y[e] = T(0);
+#pragma unroll 1
+    for (int k = 0; k < kDB - 1; ++k) {
+        const T l = L[r * ldl + k];
+        T yk[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) yk[e] = __shfl_sync(full, y[e], 2 * k + (lane & 1));
+        if (r > k) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int c = cb + e;
+                if (c < k) y[e] -= l * yk[e];
+                else if (c == k) y[e] -= l;
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (cb + e < r) Y[r * ldy + cb + e] = y[e];
+    __syncwarp();
+}
+
+// Modified LU without pivoting of the 16 x 16 block A in place: S_k =
 // -sign(pivot), U_kk = pivot - S_k (|U_kk| >= 1); L's multipliers below the
-// diagonal, U on and above; S to sg.  iu: b scratch entries (1/U_kk).
-// Column k is scaled into multipliers, and U_kk written, one step later, when
-// nothing reads them any more.
+// diagonal, U on and above; S to sg.
 template <typename T>
-SKL_DEV void mlu_smem(T* A, int ld, int b, T* sg, T* iu)
+SKL_DEV void warp16_mlu(T* A, int ld, T* sg)
 {
-    const int i = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-    const bool own = i < b && c0 < b;
-    if (threadIdx.x == 0) {
-        const T p = A[0];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
+    T a[8];
+    row_load(A, ld, a);
+#pragma unroll 1
+    for (int k = 0; k < kDB; ++k) {
+        const T p = __shfl_sync(full, sel8(a, k & 7), 2 * k + (k >> 3));
         const T sk = p >= T(0) ? T(-1) : T(1);
-        sg[0] = sk;
-        iu[0] = T(1) / (p - sk);
-    }
-    __syncthreads();
-    for (int k = 0; k < b; ++k) {
-        if (own) {
-            auto row = ld4<T>(A + i * ld + c0);
-            bool dirty = false;
-            if (k > 0 && i >= k - 1 && c0 <= k - 1 && k - 1 < c0 + 4) {
-                // finish column k - 1: multiplier (i > k-1) or pivot U_{k-1,k-1}
-                const int e = k - 1 - c0;
-                q_set<T>(row, e, (i == k - 1) ? T(1) / iu[k - 1] : q_at<T>(row, e) * iu[k - 1]);
-                dirty = true;
-            }
-            if (i > k && c0 + 3 > k) {
-                const T lik = A[i * ld + k] * iu[k];
-                const auto uk = ld4<T>(A + k * ld + c0);
+        const T ukk = p - sk;
+        T rk[8];
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int c = c0 + e;
-                    if (c > k && c < b) q_set<T>(row, e, q_at<T>(row, e) - lik * q_at<T>(uk, e));
-                }
-                dirty = true;
-                if (i == k + 1 && c0 <= i && i < c0 + 4) {   // next pivot, finished now
-                    const T v = q_at<T>(row, i - c0);
-                    const T sk = v >= T(0) ? T(-1) : T(1);
-                    sg[i] = sk;
-                    iu[i] = T(1) / (v - sk);
-                }
+        for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
+        const T l = own_col(a, k, lane) / ukk;
+        if (r > k) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int c = cb + e;
+                if (c > k) a[e] -= l * rk[e];
+                else if (c == k) a[e] = l;
             }
-            if (dirty) st4<T>(A + i * ld + c0, row);
+        } else if (r == k) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                if (cb + e == k) a[e] = ukk;
         }
-        __syncthreads();
+        if (lane == 0) sg[k] = sk;
     }
-    if (threadIdx.x == 0) A[(b - 1) * ld + (b - 1)] = T(1) / iu[b - 1];
-    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 8; ++e) A[r * ld + cb + e] = a[e];
+    __syncwarp();
 }
 
 // Operand views for blk_mul, in the coordinates (r, s) of op(X):
@@ -308,32 +282,120 @@ SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int 
     __syncthreads();
 }
 
-// Cholesky G = R^T R (b <= 64) with X = R^{-1}: R (upper, zeros below) over
-// G, X (upper, zeros below) to Xs.  buf: b scratch entries.
+// Off-diagonal blocks of X = U^{-1} (np x np upper, np a multiple of 16)
+// once X's 16 x 16 diagonal blocks hold the inverses of U's: recursive
+// doubling, [A B; 0 C]^{-1} = [A^{-1}, -A^{-1} B C^{-1}; 0, C^{-1}].  tmp holds
+// 32 x 32 (ldt).
 template <typename T>
-SKL_DEV void chol_inv_small(T* G, int ldx, int b, const T* __restrict__ mass, T eps, T* Xs, T* buf,
-                            int* bad)
+SKL_DEV void inv_upper_offdiag(const T* U, int ldu, T* X, int ldx, int np, T* tmp, int ldt)
 {
-    chol_smem<T>(G, ldx, b, mass, eps, buf, bad);
-    inv_upper_smem<T>(G, ldx, b, Xs, ldx, true, buf);
+    for (int w = kDB; w < np; w *= 2) {
+        for (int p0 = 0; p0 + w < np; p0 += 2 * w) {
+            const int n2 = min(w, np - p0 - w);
+            blk_mul<T, false, kMFull, false, kMUpper>(w, n2, n2, U + p0 * ldu + p0 + w, ldu,
+                                                     X + (p0 + w) * ldx + p0 + w, ldx, nullptr, T(1),
+                                                     tmp, ldt);
+            blk_mul<T, false, kMUpper, false, kMFull>(w, n2, w, X + p0 * ldx + p0, ldx, tmp, ldt,
+                                                     nullptr, T(-1), X + p0 * ldx + p0 + w, ldx);
+        }
+    }
 }
 
-// Modified LU of A (b <= 64) in place (L strict lower, U upper), signs to
+// Strict lower off-diagonal blocks of Y = L^{-1} (np x np unit lower) once
+// Y's diagonal blocks hold the inverses of L's:
+// [A 0; B C]^{-1} = [A^{-1}, 0; -C^{-1} B A^{-1}, C^{-1}].
+template <typename T>
+SKL_DEV void inv_unit_lower_offdiag(const T* L, int ldl, T* Y, int ldy, int np, T* tmp, int ldt)
+{
+    for (int w = kDB; w < np; w *= 2) {
+        for (int p0 = 0; p0 + w < np; p0 += 2 * w) {
+            const int n2 = min(w, np - p0 - w);
+            blk_mul<T, false, kMFull, false, kMLowerUnit>(n2, w, w, L + (p0 + w) * ldl + p0, ldl,
+                                                         Y + p0 * ldy + p0, ldy, nullptr, T(1), tmp,
+                                                         ldt);
+            blk_mul<T, false, kMLowerUnit, false, kMFull>(n2, w, n2, Y + (p0 + w) * ldy + p0 + w, ldy,
+                                                         tmp, ldt, nullptr, T(-1),
+                                                         Y + (p0 + w) * ldy + p0, ldy);
+        }
+    }
+}
+
+// Cholesky G = R^T R (np x np, np a multiple of 16) with X = R^{-1}: R (upper,
+// zeros below) over G, X (upper, zeros below) to Xs.  Blocked right-looking:
+// per 16-block, warp 0 factors the diagonal block and inverts it, then
+// R12 = R11^{-T} G12 and G22 -= R12^T R12 as block products.
+template <typename T>
+SKL_DEV void chol_inv_small(T* G, int ldx, int np, const T* __restrict__ mass, T eps, T* Xs, T* tmp,
+                            int ldt, int* bad)
+{
+    for (int e = threadIdx.x; e < np * np; e += kSmallThreads) Xs[(e / np) * ldx + e % np] = T(0);
+    __syncthreads();
+    for (int k0 = 0; k0 < np; k0 += kDB) {
+        const int rest = np - k0 - kDB;
+        T* G11 = G + k0 * ldx + k0;
+        if (threadIdx.x < 32) {
+            warp16_chol<T>(G11, ldx, mass + k0, eps, bad);
+            warp16_inv_upper<T>(G11, ldx, Xs + k0 * ldx + k0, ldx, true);
+        }
+        __syncthreads();
+        if (rest > 0) {
+            T* G12 = G11 + kDB;
+            blk_mul<T, true, kMFull, false, kMFull>(kDB, rest, kDB, Xs + k0 * ldx + k0, ldx, G12, ldx,
+                                                    nullptr, T(1), G12, ldx);
+            blk_mul<T, true, kMFull, false, kMFull, true>(rest, rest, kDB, G12, ldx, G12, ldx, nullptr,
+                                                          T(-1), G11 + kDB * ldx + kDB, ldx);
+        }
+    }
+    // R's strict lower part (the off-diagonal blocks kept G's values)
+    for (int e = threadIdx.x; e < np * np; e += kSmallThreads) {
+        const int i = e / np, c = e % np;
+        if (c < i) G[i * ldx + c] = T(0);
+    }
+    __syncthreads();
+    inv_upper_offdiag<T>(G, ldx, Xs, ldx, np, tmp, ldt);
+}
+
+// Modified LU of A (np x np) in place (L strict lower, U upper), signs to
 // sg, and in Z: L^{-1} (strict lower, unit diagonal implied) and U^{-1}
-// (upper).  buf: b scratch entries.
+// (upper).  Blocked right-looking by 16: warp 0 factors the diagonal block,
+// warps 0 and 1 invert its L and U factors into Z, then U12 = L11^{-1} A12,
+// L21 = A21 U11^{-1} and A22 -= L21 U12 as block products.
 template <typename T>
-SKL_DEV void mlu_inv_small(T* A, int ldx, int b, T* sg, T* Z, T* buf)
+SKL_DEV void mlu_inv_small(T* A, int ldx, int np, T* sg, T* Z, T* tmp, int ldt)
 {
-    mlu_smem<T>(A, ldx, b, sg, buf);
-    inv_unit_lower_smem<T>(A, ldx, b, Z, ldx);
-    inv_upper_smem<T>(A, ldx, b, Z, ldx, false, buf);
+    for (int k0 = 0; k0 < np; k0 += kDB) {
+        const int rest = np - k0 - kDB;
+        T* A11 = A + k0 * ldx + k0;
+        T* Z11 = Z + k0 * ldx + k0;
+        if (threadIdx.x < 32) warp16_mlu<T>(A11, ldx, sg + k0);
+        __syncthreads();
+        if (threadIdx.x < 32) warp16_inv_unit_lower<T>(A11, ldx, Z11, ldx);
+        else if (threadIdx.x < 64) warp16_inv_upper<T>(A11, ldx, Z11, ldx, false);
+        __syncthreads();
+        if (rest > 0) {
+            T* A12 = A11 + kDB;
+            T* A21 = A11 + kDB * ldx;
+            blk_mul<T, false, kMLowerUnit, false, kMFull>(kDB, rest, kDB, Z11, ldx, A12, ldx, nullptr,
+                                                         T(1), A12, ldx);
+            blk_mul<T, false, kMFull, false, kMUpper>(rest, kDB, kDB, A21, ldx, Z11, ldx, nullptr, T(1),
+                                                     A21, ldx);
+            blk_mul<T, false, kMFull, false, kMFull, true>(rest, rest, kDB, A21, ldx, A12, ldx, nullptr,
+                                                           T(-1), A11 + kDB * ldx + kDB, ldx);
+        }
+    }
+    inv_upper_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
+    inv_unit_lower_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
 }
 
-// b x b workspace layout of the small kernels (row-major, ld = b + 4).
+// Padded size of the b x b algebra and the workspace layout of the small
+// kernels: four np x np blocks (row-major, ld = np + 4), a 32 x 36 product
+// scratch, and 3 np entries.
+__host__ __device__ inline int small_np(int b) { return (b + kDB - 1) / kDB * kDB; }
 template <typename T>
 size_t chol_small_smem_bytes(int b)
 {
-    return (4 * (size_t)b * (b + 4) + 3 * (size_t)b) * sizeof(T) + 256;
+    const size_t np = (size_t)small_np(b);
+    return (4 * np * (np + 4) + 32 * 36 + 3 * np) * sizeof(T) + 256;
 }
 
 // Pass 1: R1 and X1 = R1^{-1} from G1 (column-major b x b, ldg = b).  Sets
@@ -344,21 +406,23 @@ k_chol_small1(const T* __restrict__ G, int b, T* __restrict__ R1, T* __restrict_
               int* __restrict__ fail)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int LDX = b + 4;
+    const int np = small_np(b);
+    const int LDX = np + 4;
     T* S0 = (T*)smem_raw;
-    T* S1 = S0 + (size_t)b * LDX;
-    T* mass = S1 + (size_t)b * LDX;
-    T* buf = mass + b;
+    T* S1 = S0 + (size_t)np * LDX;
+    T* tmp = S1 + (size_t)np * LDX;
+    T* mass = tmp + 32 * 36;
     __shared__ int s_bad;
     const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
     if (threadIdx.x == 0) s_bad = 0;
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e % b, c = e / b;
-        S0[i * LDX + c] = G[e];
+    // G padded with the identity beyond b
+    for (int e = threadIdx.x; e < np * np; e += kSmallThreads) {
+        const int i = e % np, c = e / np;
+        S0[i * LDX + c] = (i < b && c < b) ? G[i + c * b] : (i == c ? T(1) : T(0));
     }
-    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = G[k * b + k];
+    for (int k = threadIdx.x; k < np; k += kSmallThreads) mass[k] = k < b ? G[k * b + k] : T(1);
     __syncthreads();
-    chol_inv_small<T>(S0, LDX, b, mass, eps, S1, buf, &s_bad);
+    chol_inv_small<T>(S0, LDX, np, mass, eps, S1, tmp, 36, &s_bad);
     for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
         const int i = e / b, c = e % b;
         R1[e] = S0[i * LDX + c];     // row-major b x b
@@ -381,26 +445,28 @@ k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T
 {
     if (*fail) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int LDX = b + 4;
+    const int np = small_np(b);
+    const int LDX = np + 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T* S0 = (T*)smem_raw;                        // R1 -> R = R2 R1
-    T* S1 = S0 + (size_t)b * LDX;                // G2 -> R2 -> L^{-1} \ U^{-1}
-    T* S2 = S1 + (size_t)b * LDX;                // X2 -> W
-    T* S3 = S2 + (size_t)b * LDX;                // Q(0:b,:) -> Q1 -> L \ U
-    T* Sg = S3 + (size_t)b * LDX;
-    T* mass = Sg + b;
-    T* buf = mass + b;
+    T* S1 = S0 + (size_t)np * LDX;               // G2 -> R2 -> L^{-1} \ U^{-1}
+    T* S2 = S1 + (size_t)np * LDX;               // X2 -> W
+    T* S3 = S2 + (size_t)np * LDX;               // Q(0:b,:) -> Q1 -> L \ U
+    T* tmp = S3 + (size_t)np * LDX;              // 32 x 36 product scratch
+    T* Sg = tmp + 32 * 36;
+    T* mass = Sg + np;
     __shared__ int s_bad;
     const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
     if (threadIdx.x == 0) s_bad = 0;
-    for (int e = threadIdx.x; e < b * b; e += kSmallThreads) {
-        const int i = e % b, c = e / b;          // column-major sources
-        S1[i * LDX + c] = G[e];
-        S3[i * LDX + c] = Q[i + (int64_t)c * ldq];
-        const int r = e / b, q = e % b;          // row-major source
-        S0[r * LDX + q] = R1g[e];
+    // G2 padded with the identity, Q(0:b,:) with zeros, beyond b
+    for (int e = threadIdx.x; e < np * np; e += kSmallThreads) {
+        const int i = e % np, c = e / np;
+        const bool in = i < b && c < b;
+        S1[i * LDX + c] = in ? G[i + c * b] : (i == c ? T(1) : T(0));
+        S3[i * LDX + c] = in ? Q[i + (int64_t)c * ldq] : T(0);
+        S0[c * LDX + i] = in ? R1g[c * b + i] : (i == c ? T(1) : T(0));   // row-major source
     }
-    for (int k = threadIdx.x; k < b; k += kSmallThreads) mass[k] = T(1);
+    for (int k = threadIdx.x; k < np; k += kSmallThreads) mass[k] = T(1);
     __syncthreads();
     // Gershgorin distance of G2 from the identity
     for (int i = wid; i < b; i += kSmallThreads / 32) {
@@ -414,14 +480,14 @@ k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T
         if (threadIdx.x == 0) *fail = 1;
         return;
     }
-    chol_inv_small<T>(S1, LDX, b, mass, eps, S2, buf, &s_bad);  // R2 over S1, X2 -> S2
+    chol_inv_small<T>(S1, LDX, np, mass, eps, S2, tmp, 36, &s_bad);  // R2 over S1, X2 -> S2
     if (s_bad) {
         if (threadIdx.x == 0) *fail = 1;
         return;
     }
     blk_mul<T, false, kMFull, false, kMUpper>(b, b, b, S3, LDX, S2, LDX, nullptr, T(1), S3, LDX);   // Q1 = Q(0:b,:) X2
     blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S1, LDX, S0, LDX, nullptr, T(1), S0, LDX);  // R = R2 R1
-    mlu_inv_small<T>(S3, LDX, b, Sg, S1, buf);                   // Q1 - S = L U; S1 = L^{-1} \ U^{-1}
+    mlu_inv_small<T>(S3, LDX, np, Sg, S1, tmp, 36);              // Q1 - S = L U; S1 = L^{-1} \ U^{-1}
     blk_mul<T, false, kMUpper, false, kMUpper>(b, b, b, S2, LDX, S1, LDX, nullptr, T(1), S2, LDX);  // W = X2 U^{-1}
     blk_mul<T, false, kMUpper, true, kMUpperUnit>(b, b, b, S3, LDX, S1, LDX, Sg, T(-1), nullptr, 0,
                                                    Tout, ldt, tau_out + j0);   // T = -U S L^{-T}
