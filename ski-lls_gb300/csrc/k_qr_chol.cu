@@ -62,6 +62,13 @@ SKL_DEV void row_load(const T* A, int ld, T (&a)[8])
 // unnormalised during the elimination and are scaled by 1/sqrt(d) at the end.
 // Sets *bad when a pivot is not above 32 eps times its mass.
 template <typename T>
+SKL_DEV T t_rcp(T x);
+template <> SKL_DEV float t_rcp<float>(float x) { return __frcp_rn(x); }
+template <> SKL_DEV double t_rcp<double>(double x) { return __drcp_rn(x); }
+
+// Step k = 8 kh + kl: kl is a compile-time index (the inner loop is unrolled
+// by 8) so the pivot and the lane's own column k come from fixed registers.
+template <typename T>
 SKL_DEV void warp16_chol(T* A, int ld, const T* __restrict__ mass, T eps, int* bad)
 {
     const unsigned full = 0xffffffffu;
@@ -70,25 +77,30 @@ SKL_DEV void warp16_chol(T* A, int ld, const T* __restrict__ mass, T eps, int* b
     row_load(A, ld, a);
     bool isbad = false;
 #pragma unroll 1
-    for (int k = 0; k < kDB; ++k) {
-        const T d = __shfl_sync(full, sel8(a, k & 7), 2 * k + (k >> 3));
-        const T ms = mass[k];
-        const bool ok = d > T(32) * eps * ms && ms > T(0);
-        isbad = isbad || !ok;
-        const T inv = ok ? T(1) / d : T(0);
-        T rk[8];
+    for (int kh = 0; kh < 2; ++kh) {
 #pragma unroll
-        for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
-        const T g = own_col(a, k, lane) * inv;   // A[r][k] = A[k][r]
-        if (r > k) {
+        for (int kl = 0; kl < 8; ++kl) {
+            const int k = kh * 8 + kl;
+            const T d = __shfl_sync(full, a[kl], 2 * k + kh);
+            const T ms = mass[k];
+            const bool ok = d > T(32) * eps * ms && ms > T(0);
+            isbad = isbad || !ok;
+            const T inv = ok ? t_rcp(d) : T(0);
+            T rk[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e)
-                if (cb + e > k) a[e] -= g * rk[e];
+            for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
+            const T other = __shfl_xor_sync(full, a[kl], 1);
+            const T g = (kh == (lane & 1) ? a[kl] : other) * inv;   // A[r][k] = A[k][r]
+            if (r > k) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    if (cb + e > k) a[e] -= g * rk[e];
+            }
         }
     }
     if (isbad && lane == 0) *bad = 1;
     const T d = own_col(a, r, lane);
-    const T sc = d > T(0) ? T(1) / t_sqrt(d) : T(0);
+    const T sc = d > T(0) ? t_rcp(t_sqrt(d)) : T(0);
 #pragma unroll
     for (int e = 0; e < 8; ++e) A[r * ld + cb + e] = (cb + e >= r) ? a[e] * sc : T(0);
     __syncwarp();
@@ -101,7 +113,7 @@ SKL_DEV void warp16_inv_upper(const T* U, int ldu, T* X, int ldx, bool zero_lowe
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, r = lane >> 1, cb = (lane & 1) * 8;
-    const T iv = lane < kDB ? T(1) / U[lane * ldu + lane] : T(0);
+    const T iv = lane < kDB ? t_rcp(U[lane * ldu + lane]) : T(0);
     T x[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) x[e] = (cb + e == r) ? T(1) : T(0);
@@ -172,27 +184,31 @@ SKL_DEV void warp16_mlu(T* A, int ld, T* sg)
     T a[8];
     row_load(A, ld, a);
 #pragma unroll 1
-    for (int k = 0; k < kDB; ++k) {
-        const T p = __shfl_sync(full, sel8(a, k & 7), 2 * k + (k >> 3));
-        const T sk = p >= T(0) ? T(-1) : T(1);
-        const T ukk = p - sk;
-        T rk[8];
+    for (int kh = 0; kh < 2; ++kh) {
 #pragma unroll
-        for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
-        const T l = own_col(a, k, lane) / ukk;
-        if (r > k) {
+        for (int kl = 0; kl < 8; ++kl) {
+            const int k = kh * 8 + kl;
+            const T p = __shfl_sync(full, a[kl], 2 * k + kh);
+            const T sk = p >= T(0) ? T(-1) : T(1);
+            const T ukk = p - sk;
+            const T iu = t_rcp(ukk);
+            T rk[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int c = cb + e;
-                if (c > k) a[e] -= l * rk[e];
-                else if (c == k) a[e] = l;
+            for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
+            const T other = __shfl_xor_sync(full, a[kl], 1);
+            const T l = (kh == (lane & 1) ? a[kl] : other) * iu;
+            if (r > k) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int c = cb + e;
+                    if (c > k) a[e] -= l * rk[e];
+                    else if (c == k) a[e] = l;
+                }
+            } else if (r == k) {
+                if (kh == (lane & 1)) a[kl] = ukk;
             }
-        } else if (r == k) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e)
-                if (cb + e == k) a[e] = ukk;
+            if (lane == 0) sg[k] = sk;
         }
-        if (lane == 0) sg[k] = sk;
     }
 #pragma unroll
     for (int e = 0; e < 8; ++e) A[r * ld + cb + e] = a[e];
@@ -225,46 +241,50 @@ SKL_DEV void k_range(int i0, int c0, int tr, int tc, int kk, int& klo, int& khi)
 }
 
 // C (m x n) = alpha * op(A) (m x kk) * op(B) (kk x n) [* diag(sB) on B's
-// rows] (+ C when ACC), row-major shared memory; 2 x 2 register tiles, one
-// per thread (m * n <= 4 * kSmallThreads); k runs only over the range the
-// operand masks leave nonzero.  Results wait for a block barrier, so C may
+// rows] (+ C when ACC), row-major shared memory; TR x TR register tiles, one
+// per thread (m * n <= TR * TR * kSmallThreads); k runs only over the range
+// the operand masks leave nonzero.  Results wait for a block barrier, so C may
 // alias A or B.  With Cg set, C goes to global memory column-major (ldg)
 // instead and its diagonal also to tau.
-template <typename T, bool TA, int MA, bool TB, int MB, bool ACC = false>
-SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
-                     const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg = nullptr,
-                     int ldg = 0, T* __restrict__ tau = nullptr)
+template <typename T, bool TA, int MA, bool TB, int MB, bool ACC, int TR>
+SKL_DEV void blk_mul_t(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
+                       const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg, int ldg,
+                       T* __restrict__ tau)
 {
-    const int ntc = (n + 1) / 2;
+    const int ntc = (n + TR - 1) / TR;
     const int t = threadIdx.x;
-    const int i0 = (t / ntc) * 2, c0 = (t % ntc) * 2;
+    const int i0 = (t / ntc) * TR, c0 = (t % ntc) * TR;
     const bool act = i0 < m;
-    T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+    T acc[TR][TR];
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+        for (int q = 0; q < TR; ++q) acc[r][q] = T(0);
     if (act) {
         int klo, khi;
-        k_range<MA, MB>(i0, c0, 2, 2, kk, klo, khi);
+        k_range<MA, MB>(i0, c0, TR, TR, kk, klo, khi);
 #pragma unroll 4
         for (int k = klo; k < khi; ++k) {
-            T av[2], bv[2];
+            T av[TR], bv[TR];
 #pragma unroll
-            for (int r = 0; r < 2; ++r) av[r] = (i0 + r < m) ? op_at<T, TA, MA>(A, lda, i0 + r, k) : T(0);
+            for (int r = 0; r < TR; ++r) av[r] = (i0 + r < m) ? op_at<T, TA, MA>(A, lda, i0 + r, k) : T(0);
             const T sc = sB ? sB[k] : T(1);
 #pragma unroll
-            for (int q = 0; q < 2; ++q) bv[q] = (c0 + q < n) ? sc * op_at<T, TB, MB>(B, ldb, k, c0 + q) : T(0);
+            for (int q = 0; q < TR; ++q) bv[q] = (c0 + q < n) ? sc * op_at<T, TB, MB>(B, ldb, k, c0 + q) : T(0);
 #pragma unroll
-            for (int r = 0; r < 2; ++r)
+            for (int r = 0; r < TR; ++r)
 #pragma unroll
-                for (int q = 0; q < 2; ++q) acc[r][q] += av[r] * bv[q];
+                for (int q = 0; q < TR; ++q) acc[r][q] += av[r] * bv[q];
         }
     }
     __syncthreads();
     if (act) {
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
+        for (int r = 0; r < TR; ++r) {
             const int i = i0 + r;
             if (i >= m) continue;
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < TR; ++q) {
                 const int c = c0 + q;
                 if (c >= n) continue;
                 const T v = alpha * acc[r][q];
@@ -280,6 +300,16 @@ SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int 
         }
     }
     __syncthreads();
+}
+
+// 2 x 2 tiles: 4 x 4 tiles measured slower inside the small kernels (their
+// k ranges trim less under the triangular masks).
+template <typename T, bool TA, int MA, bool TB, int MB, bool ACC = false>
+SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
+                     const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg = nullptr,
+                     int ldg = 0, T* __restrict__ tau = nullptr)
+{
+    blk_mul_t<T, TA, MA, TB, MB, ACC, 2>(m, n, kk, A, lda, B, ldb, sB, alpha, C, ldc, Cg, ldg, tau);
 }
 
 // Off-diagonal blocks of X = U^{-1} (np x np upper, np a multiple of 16)
