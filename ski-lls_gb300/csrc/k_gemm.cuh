@@ -17,19 +17,27 @@ constexpr int kGBM = 64, kGBN = 64, kGBK = 16;
 // TRI = 0: general.  TRI = 1: op(A) is upper triangular (terms with k < row
 // vanish).  TRI = 2: op(B) is upper triangular (terms with k > col vanish).
 // Tiles skip the K range that is structurally zero.
-template <typename T, bool TA, bool TB, int TRI = 0>
+// BAT: blockIdx.z indexes a batch of equally shaped products whose operands
+// sit bsa / bsb / bsc elements apart (no split-K).
+template <typename T, bool TA, bool TB, int TRI = 0, bool BAT = false>
 __global__ void __launch_bounds__(256)
 k_gemm(int M, int N, int K, T alpha, const T* __restrict__ A, int64_t lda,
        const T* __restrict__ B, int64_t ldb, T beta, T* __restrict__ C, int64_t ldc, int kchunk,
-       T* __restrict__ partial)
+       T* __restrict__ partial, int64_t bsa = 0, int64_t bsb = 0, int64_t bsc = 0)
 {
     __shared__ T As[kGBK][kGBM + 1];
     __shared__ T Bs[kGBK][kGBN + 1];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;     // 16 x 16 threads
     const int m0 = blockIdx.x * kGBM, n0 = blockIdx.y * kGBN;
-    int k_begin = blockIdx.z * kchunk;
-    int k_end = min(K, k_begin + kchunk);
+    if (BAT) {
+        A += blockIdx.z * bsa;
+        B += blockIdx.z * bsb;
+        C += blockIdx.z * bsc;
+        partial = nullptr;
+    }
+    int k_begin = BAT ? 0 : blockIdx.z * kchunk;
+    int k_end = BAT ? K : min(K, k_begin + kchunk);
     if (TRI == 1) k_begin = max(k_begin, m0 / kGBK * kGBK);
     if (TRI == 2) k_end = min(k_end, n0 + kGBN);
     T acc[4][4];
@@ -119,7 +127,8 @@ SKL_DEV void sgemm_load_a(const float* __restrict__ A, int64_t lda, int M, int m
     if (!TA) {
         const int k = c / (BM / 4), m4 = (c % (BM / 4)) * 4;
         const int gm = m0 + m4, gk = k0 + k;
-        if (vec && gk < k_end && gm + 3 < M && TRI != 1) {
+        // a triangular operand still loads whole float4s away from its diagonal
+        if (vec && gk < k_end && gm + 3 < M && (TRI != 1 || gk >= gm + 3)) {
             ra[0] = *reinterpret_cast<const float4*>(A + gm + (int64_t)gk * lda);
             return;
         }
@@ -131,7 +140,7 @@ SKL_DEV void sgemm_load_a(const float* __restrict__ A, int64_t lda, int M, int m
     } else {
         const int m = c / (kSBK / 4), k4 = (c % (kSBK / 4)) * 4;
         const int gm = m0 + m, gk = k0 + k4;
-        if (vec && gm < M && gk + 3 < k_end && TRI != 1) {
+        if (vec && gm < M && gk + 3 < k_end && (TRI != 1 || gk >= gm)) {
             ra[0] = *reinterpret_cast<const float4*>(A + gk + (int64_t)gm * lda);
             return;
         }
@@ -172,7 +181,7 @@ SKL_DEV void sgemm_load_b(const float* __restrict__ B, int64_t ldb, int N, int n
     if (!TB) {
         const int n = c / (kSBK / 4), k4 = (c % (kSBK / 4)) * 4;
         const int gn = n0 + n, gk = k0 + k4;
-        if (vec && gn < N && gk + 3 < k_end && TRI != 2) {
+        if (vec && gn < N && gk + 3 < k_end && (TRI != 2 || gk + 3 <= gn)) {
             rb[0] = *reinterpret_cast<const float4*>(B + gk + (int64_t)gn * ldb);
             return;
         }
@@ -184,7 +193,7 @@ SKL_DEV void sgemm_load_b(const float* __restrict__ B, int64_t ldb, int N, int n
     } else {
         const int k = c / (kSBN / 4), n4 = (c % (kSBN / 4)) * 4;
         const int gn = n0 + n4, gk = k0 + k;
-        if (vec && gk < k_end && gn + 3 < N && TRI != 2) {
+        if (vec && gk < k_end && gn + 3 < N && (TRI != 2 || gk <= gn)) {
             rb[0] = *reinterpret_cast<const float4*>(B + gn + (int64_t)gk * ldb);
             return;
         }
@@ -496,6 +505,27 @@ void trmm(int tri, int M, int N, int K, T alpha, const T* A, int64_t lda, const 
           T beta, T* C, int64_t ldc, cudaStream_t st)
 {
     gemm_launch<T>(false, false, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nullptr, 0, tri, st);
+}
+
+// batch products C_z = alpha op(A_z) op(B_z) + beta C_z, z = 0..batch-1, with
+// A_z = A + z bsa etc. (one launch; tri as in trmm)
+template <typename T>
+void trmm_batched(int tri, int M, int N, int K, T alpha, const T* A, int64_t lda, int64_t bsa,
+                  const T* B, int64_t ldb, int64_t bsb, T beta, T* C, int64_t ldc, int64_t bsc,
+                  int batch, cudaStream_t st)
+{
+    if (M <= 0 || N <= 0 || batch <= 0) return;
+    dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, batch);
+    if (tri == 1)
+        k_gemm<T, false, false, 1, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                                                ldc, K, nullptr, bsa, bsb, bsc);
+    else if (tri == 2)
+        k_gemm<T, false, false, 2, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                                                ldc, K, nullptr, bsa, bsb, bsc);
+    else
+        k_gemm<T, false, false, 0, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                                                ldc, K, nullptr, bsa, bsb, bsc);
+    SKL_LAUNCHED();
 }
 
 }  // namespace skl

@@ -48,7 +48,6 @@ constexpr int kQrWarps = kQrThreads / 32;
 constexpr int kCluster = 16;
 constexpr int kPP = 16;          // over-sampling rows of the sample Y
 constexpr int kMaxNb = 64;
-constexpr int kYRows = (kMaxNb + kPP + 3) / 4;   // sample rows per lane of a column quad
 
 // ------------------------------------------------------------- Gaussian --
 SKL_DEV unsigned long long splitmix64(unsigned long long x)
@@ -309,38 +308,22 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
             const int q4 = tid & 3;
             const int gcol = tid >> 2;
             const int per_pass = kYThreads / 4;
-            // this lane's rows r = s + q4 + 4 t of v, formed once per step
-            T vr[kYRows];
-#pragma unroll
-            for (int t = 0; t < kYRows; ++t) {
-                const int r = s + q4 + 4 * t;
-                vr[t] = r < nbp ? (r == s ? T(1) : wc[r] * scale) : T(0);
-            }
             for (int base = 0; base < ncols; base += per_pass) {
                 const int c = base + gcol;
                 const bool act = c < ncols && !taken[c] && c != win_local;
                 T* col = Ys + (size_t)(act ? c : 0) * ldp;
                 T w = T(0);
-                if (act) {
-#pragma unroll
-                    for (int t = 0; t < kYRows; ++t) {
-                        const int r = s + q4 + 4 * t;
-                        if (r < nbp) w += vr[t] * col[r];
-                    }
-                }
+                if (act)
+                    for (int r = s + q4; r < nbp; r += 4) w += (r == s ? T(1) : wc[r] * scale) * col[r];
                 w += __shfl_xor_sync(0xffffffffu, w, 1);
                 w += __shfl_xor_sync(0xffffffffu, w, 2);
                 w *= tau;
                 T ss = T(0);
                 if (act) {
-#pragma unroll
-                    for (int t = 0; t < kYRows; ++t) {
-                        const int r = s + q4 + 4 * t;
-                        if (r < nbp) {
-                            const T y = col[r] - w * vr[t];
-                            col[r] = y;
-                            if (r > s) ss += y * y;
-                        }
+                    for (int r = s + q4; r < nbp; r += 4) {
+                        T y = col[r] - w * (r == s ? T(1) : wc[r] * scale);
+                        col[r] = y;
+                        if (r > s) ss += y * y;
                     }
                 }
                 ss += __shfl_xor_sync(0xffffffffu, ss, 1);

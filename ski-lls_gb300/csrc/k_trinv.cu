@@ -22,6 +22,7 @@
 namespace skl {
 
 constexpr int kTB = 64;   // diagonal block size
+constexpr int kBatchMaxBlock = 512;   // levels up to this block size run as one batched launch per product
 
 // Invert the 64x64 (or smaller, last) diagonal blocks of R (+ perturb*I):
 // one CTA per block, one thread per column of the inverse.
@@ -129,7 +130,20 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
     T* tmp = (T*)work;   // holds B * C^{-1} for one pair (s x s')
     // recursive doubling: blocks of size s are inverted; combine neighbours
     for (int64_t s = kTB; s < r; s *= 2) {
-        for (int64_t a0 = 0; a0 + s < r; a0 += 2 * s) {
+        int64_t a_first = 0;
+        if (s <= kBatchMaxBlock) {
+            // all full pairs of this level in two launches
+            const int64_t full = r / (2 * s);
+            if (full > 0) {
+                const int64_t step = 2 * s * (ldm + 1);
+                trmm_batched<T>(2, (int)s, (int)s, (int)s, T(1), R + s * ld, ld, 2 * s * (ld + 1),
+                                M + s + s * ldm, ldm, step, T(0), tmp, s, s * s, (int)full, st);
+                trmm_batched<T>(1, (int)s, (int)s, (int)s, T(-1), M, ldm, step, tmp, s, s * s, T(0),
+                                M + s * ldm, ldm, step, (int)full, st);
+                a_first = full * 2 * s;
+            }
+        }
+        for (int64_t a0 = a_first; a0 + s < r; a0 += 2 * s) {
             const int64_t c0 = a0 + s;
             const int64_t sa = s;
             const int64_t sc = std::min<int64_t>(s, r - c0);
