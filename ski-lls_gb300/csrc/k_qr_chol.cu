@@ -66,6 +66,19 @@ SKL_DEV T t_rcp(T x);
 template <> SKL_DEV float t_rcp<float>(float x) { return __frcp_rn(x); }
 template <> SKL_DEV double t_rcp<double>(double x) { return __drcp_rn(x); }
 
+// Pivot reciprocal on the elimination's dependency chain: the hardware
+// approximation (relative error ~2^-23, like one more rounding of the
+// pivot) instead of the correctly rounded multi-instruction sequence.
+template <typename T>
+SKL_DEV T t_rcp_chain(T x);
+template <> SKL_DEV float t_rcp_chain<float>(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+template <> SKL_DEV double t_rcp_chain<double>(double x) { return __drcp_rn(x); }
+
 // Step k = 8 kh + kl: kl is a compile-time index (the inner loop is unrolled
 // by 8) so the pivot and the lane's own column k come from fixed registers.
 template <typename T>
@@ -85,7 +98,7 @@ SKL_DEV void warp16_chol(T* A, int ld, const T* __restrict__ mass, T eps, int* b
             const T ms = mass[k];
             const bool ok = d > T(32) * eps * ms && ms > T(0);
             isbad = isbad || !ok;
-            const T inv = ok ? t_rcp(d) : T(0);
+            const T inv = ok ? t_rcp_chain(d) : T(0);
             T rk[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
@@ -191,7 +204,7 @@ SKL_DEV void warp16_mlu(T* A, int ld, T* sg)
             const T p = __shfl_sync(full, a[kl], 2 * k + kh);
             const T sk = p >= T(0) ? T(-1) : T(1);
             const T ukk = p - sk;
-            const T iu = t_rcp(ukk);
+            const T iu = t_rcp_chain(ukk);
             T rk[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) rk[e] = __shfl_sync(full, a[e], 2 * k + (lane & 1));
