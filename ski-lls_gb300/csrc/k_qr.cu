@@ -810,7 +810,6 @@ struct QrBuffers {
     T* tmpY;      // 2 nb sample columns being moved
     int* tmpI;    // 2 nb pivot indices being moved
     T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
-    T* R12;                   // b x (d-j): rows j..j+b of the updated trailing matrix
     double *qw;
     int64_t part_cap, part2_cap, tmp_rows;   // part2: split-K partials of the side stream
 };
@@ -854,7 +853,6 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.cr1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.cx1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.cw = (T*)take((size_t)p.nb * p.nb * sizeof(T));
-    B.R12 = (T*)take((size_t)p.nb * d * sizeof(T));
     B.qw = (double*)take(kMaxNb * sizeof(double));
     if (total) *total = off;
     return B;
@@ -966,8 +964,8 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     // panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs on a
     // high-priority side stream: the part that needs V and T alone (GU, GUT, B)
     // overlaps W and R12, the rest overlaps the big trailing update and Q^T c;
-    // panel j+1's permutation waits for the side stream's event.  (R12 is
-    // formed separately because the update rewrites A12 concurrently.)
+    // panel j+1's permutation waits for the side stream's event.  (R12 is the
+    // first b rows of the trailing update, done ahead of the other rows.)
     cudaStream_t side = nullptr;
     cudaEvent_t evV = nullptr, evR = nullptr, evY = nullptr, evG = nullptr;
     if (pivoting) {
@@ -1090,20 +1088,20 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             gemm<T>(true, false, b, N2, b, T(1), B.Tm, nb, B.W, b, T(0), B.Z, b, nullptr, 0, st);
             tm.end(5, t0);
         }
-        if (pivoting && !last) {
-            // R12 = A12 - V1 Z (rows j..j+b of the updated trailing matrix)
-            if (N2 > 0) {
-                k_copy_block<T><<<64, 256, 0, st>>>(Atr, ld, B.R12, b, b, N2);
-                SKL_LAUNCHED();
-                gemm<T>(false, false, b, N2, b, T(-1), B.V, m, B.Z, b, T(1), B.R12, b, nullptr, 0, st);
-            }
+        // with pivoting the first b rows of the trailing update (R12 = A12 - V1 Z)
+        // go first and alone: the side stream reads R12 in place while the
+        // main stream updates rows b.. of the trailing matrix
+        const bool split_update = pivoting && !last;
+        if (split_update) {
+            if (N2 > 0)
+                gemm<T>(false, false, b, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
             SKL_CUDA(cudaEventRecord(evR, st));
             SKL_CUDA(cudaStreamWaitEvent(side, evR, 0));
             // side: Y2 -= B R12 ; the next sample QRP (evY) ; G(:, j:m) -= GUT V^T,
             // which only the next downdate needs (evG)
             cudaEvent_t t0 = tms.begin();
             if (N2 > 0)
-                gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, B.R12, b, T(1),
+                gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, Atr, ld, T(1),
                         B.Y + (j + b) * nbp, nbp, nullptr, 0, side);
             tms.end(7, t0);
             const int64_t jn = j + nb;
@@ -1121,9 +1119,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             side_pending = true;
         }
         if (N2 > 0) {
-            // A_trail -= V Z
+            // A_trail -= V Z (rows b.. when the first b went ahead)
             cudaEvent_t t0 = tm.begin();
-            gemm<T>(false, false, M, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
+            const int r0 = split_update ? b : 0;
+            gemm<T>(false, false, M - r0, N2, b, T(-1), B.V + r0, m, B.Z, b, T(1), Atr + r0, ld, nullptr, 0,
+                    st);
             tm.end(6, t0);
         }
         if (c) {
