@@ -226,6 +226,23 @@ SKL_DEV int dsmem_ld_s32(const int* local, unsigned rank)
     return v;
 }
 
+// Remote stores (fire and forget; a later cluster barrier with release /
+// acquire semantics orders them for the destination CTA).
+SKL_DEV void dsmem_st_f32(float* local, unsigned rank, float v)
+{
+    asm volatile("st.shared::cluster.f32 [%0], %1;" :: "r"(dsmem_addr(local, rank)), "f"(v) : "memory");
+}
+SKL_DEV void dsmem_st_f64(double* local, unsigned rank, double v)
+{
+    asm volatile("st.shared::cluster.f64 [%0], %1;" :: "r"(dsmem_addr(local, rank)), "d"(v) : "memory");
+}
+SKL_DEV void dsmem_st_s32(int* local, unsigned rank, int v)
+{
+    asm volatile("st.shared::cluster.s32 [%0], %1;" :: "r"(dsmem_addr(local, rank)), "r"(v) : "memory");
+}
+SKL_DEV void dsmem_st(float* local, unsigned rank, float v) { dsmem_st_f32(local, rank, v); }
+SKL_DEV void dsmem_st(double* local, unsigned rank, double v) { dsmem_st_f64(local, rank, v); }
+
 template <typename T>
 SKL_DEV T dsmem_ld(const T* local, unsigned rank);
 template <>

@@ -172,10 +172,7 @@ struct YqrpSmem {
         s += (size_t)cn * sizeof(T);                        // nrm
         s += (size_t)cn + 16;                               // taken
         s = (s + 15) & ~(size_t)15;
-        s += 2 * (size_t)nbp * sizeof(T);                   // cand_col[2][nbp]
-        s += (size_t)kCluster * nbp * sizeof(T);            // all candidates' columns
-        s += (size_t)nbp * sizeof(T);                       // v
-        s += 2 * sizeof(T) + 2 * sizeof(int) + 64;          // cand val/idx
+        s += 2 * (size_t)kCluster * nbp * sizeof(T);        // all candidates' columns [2][16][nbp]
         return s + 256;
     }
 };
@@ -196,14 +193,13 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     T* nrm = Ys + (size_t)ldp * cn;
     unsigned char* taken = (unsigned char*)(nrm + cn);
     size_t off = ((size_t)ldp * cn * sizeof(T) + cn * sizeof(T) + cn + 16 + 15) & ~(size_t)15;
-    T* cand_col = (T*)(smem_raw + off);          // [2][nbp]
-    T* allc = cand_col + 2 * nbp;                 // [16][nbp]
-    T* cand_val = allc + kCluster * nbp + nbp;    // [2]
-    int* cand_idx = (int*)(cand_val + 2);         // [2]
+    // candidates pushed by every CTA of the cluster, double-buffered by step
+    // parity: [2][16][nbp] columns, [2][16] norms and indices
+    T* allc2 = (T*)(smem_raw + off);
     __shared__ T s_red_v[kYWarps];
     __shared__ int s_red_i[kYWarps];
-    __shared__ T s_cv[kCluster];
-    __shared__ int s_ci[kCluster];
+    __shared__ T s_cv2[2][kCluster];
+    __shared__ int s_ci2[2][kCluster];
     __shared__ int s_local;
     __shared__ int s_sel[kMaxNb];   // CTA 0: the selections, for the move plan
     __shared__ int s_inlow[kMaxNb];
@@ -252,30 +248,28 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 int xi = __shfl_xor_sync(0xffffffffu, oi, o);
                 if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; }
             }
-            if (lane == 0) {
-                cand_val[p] = ov;
-                cand_idx[p] = (oi >= 0) ? c0 + oi : -1;
-                s_local = oi;
+            // push this CTA's candidate to slot crank of every CTA
+            if (lane < kCluster) {
+                dsmem_st(&s_cv2[p][crank], lane, ov);
+                dsmem_st_s32(&s_ci2[p][crank], lane, (oi >= 0) ? c0 + oi : -1);
             }
+            if (lane == 0) s_local = oi;
         }
         __syncthreads();
+        T* allc = allc2 + (size_t)p * kCluster * nbp;   // [16][nbp] of this step
         {
             const int li = s_local;
-            for (int r = s + tid; r < nbp; r += kYThreads)
-                cand_col[p * nbp + r] = (li >= 0) ? Ys[r + (size_t)li * ldp] : T(0);
+            const int rows_left = nbp - s;
+            T* mine = allc + (size_t)crank * nbp;
+            for (int e = tid; e < kCluster * rows_left; e += kYThreads) {
+                const int q = e / rows_left, r = s + e % rows_left;
+                dsmem_st(&mine[r], q, (li >= 0) ? Ys[r + (size_t)li * ldp] : T(0));
+            }
         }
+        // (b) the barrier's release / acquire makes every CTA's pushes visible
         cluster_sync();
-        // (b) one batched DSMEM round trip: all candidates and their columns
-        if (tid < kCluster) {
-            s_cv[tid] = dsmem_ld(&cand_val[p], tid);
-            s_ci[tid] = dsmem_ld_s32(&cand_idx[p], tid);
-        }
-        const int rows_left = nbp - s;
-        for (int e = tid; e < kCluster * rows_left; e += kYThreads) {
-            int q = e / rows_left, r = s + e % rows_left;
-            allc[q * nbp + r] = dsmem_ld(&cand_col[p * nbp + r], q);
-        }
-        __syncthreads();
+        const T* s_cv = s_cv2[p];
+        const int* s_ci = s_ci2[p];
         // winner and Householder vector, in every warp (no broadcast barrier)
         T ov = lane < kCluster ? s_cv[lane] : T(-1);
         int oi = lane < kCluster ? s_ci[lane] : -1;
