@@ -220,17 +220,19 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     }
     __syncthreads();
 
+    // this thread's best column (largest norm; ties -> smallest index): from a
+    // scan for the first step, then from the norms the update phase computes
+    T bv = T(-1);
+    int bi = -1;
+    for (int c = tid; c < ncols; c += kYThreads) {
+        // a NaN norm ranks below every real one but stays selectable, so
+        // a winner always exists while untaken columns remain
+        const T nv = nrm[c] == nrm[c] ? nrm[c] : T(-0.5);
+        if (!taken[c] && nv > bv) { bv = nv; bi = c; }
+    }
     for (int s = 0; s < b; ++s) {
         const int p = s & 1;
-        // (a) local argmax (largest norm; ties -> smallest index)
-        T bv = T(-1);
-        int bi = -1;
-        for (int c = tid; c < ncols; c += kYThreads) {
-            // a NaN norm ranks below every real one but stays selectable, so
-            // a winner always exists while untaken columns remain
-            const T nv = nrm[c] == nrm[c] ? nrm[c] : T(-0.5);
-            if (!taken[c] && nv > bv) { bv = nv; bi = c; }
-        }
+        // (a) local argmax
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             T ov = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -302,6 +304,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
             const int q4 = tid & 3;
             const int gcol = tid >> 2;
             const int per_pass = kYThreads / 4;
+            bv = T(-1);
+            bi = -1;
             for (int base = 0; base < ncols; base += per_pass) {
                 const int c = base + gcol;
                 const bool act = c < ncols && !taken[c] && c != win_local;
@@ -322,7 +326,10 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 }
                 ss += __shfl_xor_sync(0xffffffffu, ss, 1);
                 ss += __shfl_xor_sync(0xffffffffu, ss, 2);
-                if (act && q4 == 0) nrm[c] = ss;
+                if (act) {   // candidate for the next step (columns ascend across passes)
+                    const T nv = ss == ss ? ss : T(-0.5);
+                    if (nv > bv) { bv = nv; bi = c; }
+                }
             }
         }
         __syncthreads();
