@@ -15,7 +15,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <array>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "skl_internal.hpp"
@@ -55,6 +57,54 @@ struct Rng {
         if (++r == 31) r = 0;
         return v >> 1;
     }
+
+    // The state after L more draws, without drawing them.  The words obey
+    // x_t = x_{t-31} + x_{t-3} (mod 2^32), so x_{t+L} is a fixed Z/2^32
+    // combination of the current window x_{t-31..t-1}: the coefficients of
+    // X^L mod (X^31 - X^28 - 1), formed by square-and-multiply.
+    Rng jumped(uint64_t L) const
+    {
+        using Poly = std::array<uint32_t, 31>;
+        auto mulmod = [](const Poly& a, const Poly& b) {
+            uint32_t prod[61] = {0};
+            for (int i = 0; i < 31; ++i)
+                for (int j = 0; j < 31; ++j) prod[i + j] += a[(size_t)i] * b[(size_t)j];
+            // X^e = X^(e-3) + X^(e-31) for e >= 31, highest degree first
+            for (int e = 60; e >= 31; --e) {
+                prod[e - 3] += prod[e];
+                prod[e - 31] += prod[e];
+                prod[e] = 0;
+            }
+            Poly r{};
+            for (int i = 0; i < 31; ++i) r[(size_t)i] = prod[i];
+            return r;
+        };
+        Poly acc{}, base{};
+        acc[0] = 1;    // X^0
+        base[1] = 1;   // X^1
+        for (uint64_t e = L; e; e >>= 1) {
+            if (e & 1) acc = mulmod(acc, base);
+            base = mulmod(base, base);
+        }
+        uint32_t w[31];   // current window, oldest first
+        for (int t = 0; t < 31; ++t) w[t] = s[(f + t) % 31];
+        Rng out;
+        Poly c = acc;     // X^(L + t) mod P for t = 0, 1, ...
+        for (int t = 0; t < 31; ++t) {
+            uint32_t v = 0;
+            for (int u = 0; u < 31; ++u) v += c[(size_t)u] * w[u];
+            out.s[(3 + t) % 31] = v;
+            // c <- X c mod P
+            const uint32_t top = c[30];
+            for (int u = 30; u > 0; --u) c[(size_t)u] = c[(size_t)u - 1];
+            c[0] = 0;
+            c[28] += top;
+            c[0] += top;
+        }
+        out.f = 3;
+        out.r = 0;
+        return out;
+    }
 };
 
 std::mutex g_mu;
@@ -86,9 +136,24 @@ void rng_srand(uint32_t seed)
     g_seeded = true;
 }
 
-// Caller holds the lock (rng_lock).
+// Caller holds the lock (rng_lock).  The n*k sign draws follow the n*k row
+// draws in the stream; they are drawn on a second thread from the state
+// jumped n*k draws ahead while this thread runs the (serial) row shuffle.
 void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
 {
+    const int64_t nk = n * k;
+    std::vector<uint8_t> neg;
+    Rng after_rows = g_rng;
+    std::thread signs;
+    const bool split = nk >= (int64_t)1 << 15;
+    if (split) {
+        after_rows = g_rng.jumped((uint64_t)nk);
+        neg.resize((size_t)nk);
+        signs = std::thread([&neg, &after_rows, nk]() {
+            for (int64_t q = 0; q < nk; ++q)
+                neg[(size_t)q] = (after_rows.next() & 1u) == 0u;   // rand()%2 == 0 -> -1
+        });
+    }
     std::vector<uint32_t> perm((size_t)m);
     for (int64_t i = 0; i < m; ++i) perm[(size_t)i] = (uint32_t)i;
     uint32_t* pa = perm.data();
@@ -113,9 +178,15 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
             }
         }
     }
-    const int64_t nk = n * k;
-    for (int64_t q = 0; q < nk; ++q)
-        if ((g_rng.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
+    if (split) {
+        signs.join();
+        for (int64_t q = 0; q < nk; ++q)
+            if (neg[(size_t)q]) hidx[q] |= 0x80000000u;
+        g_rng = after_rows;   // the stream continues after both draw sequences
+    } else {
+        for (int64_t q = 0; q < nk; ++q)
+            if ((g_rng.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
+    }
 }
 
 // Caller holds the lock.

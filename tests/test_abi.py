@@ -68,6 +68,22 @@ def test_hash_stream_continues_like_global_rand():
     np.testing.assert_array_equal(b_rows, r2)
 
 
+def test_hash_stream_large_draws_split_across_threads():
+    # n*k >= 2^15: the sign draws run on a second thread from the generator
+    # state jumped n*k draws ahead; rows, signs and the continuing stream must
+    # stay identical to one sequential stream
+    skl.srand(7)
+    a_rows, a_vals = skl.hash_generate(8500, 30000, 2)
+    b_rows, b_vals = skl.hash_generate(900, 40000, 1)
+    g = orc.Rng(7)
+    r1, v1 = orc.gen_hashing(g, 8500, 30000, 2)
+    r2, v2 = orc.gen_hashing(g, 900, 40000, 1)
+    np.testing.assert_array_equal(a_rows, r1)
+    np.testing.assert_array_equal(a_vals, v1)
+    np.testing.assert_array_equal(b_rows, r2)
+    np.testing.assert_array_equal(b_vals, v2)
+
+
 def test_hash_rejects_bad_sizes():
     with pytest.raises(skl.SklError):
         skl.hash_generate(3, 10, 5, seed=1)
