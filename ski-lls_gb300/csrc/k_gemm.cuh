@@ -337,6 +337,29 @@ k_sgemm(int M, int N, int K, float alpha, const float* __restrict__ A, int64_t l
     }
 }
 
+// Small outputs from many splits: one warp per output element, lanes over
+// the splits (strided), a fixed shuffle tree combining the lanes.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_splitk_reduce_warp(int M, int N, int splits, T alpha, const T* __restrict__ partial, T beta,
+                     T* __restrict__ C, int64_t ldc)
+{
+    const int64_t total = (int64_t)M * N;
+    const int lane = threadIdx.x & 31;
+    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (e >= total) return;
+    T s = T(0);
+    for (int z = lane; z < splits; z += 32) s += partial[(int64_t)z * total + e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        T* c = C + (int)(e % M) + (e / M) * ldc;
+        T v = alpha * s;
+        if (beta != T(0)) v += beta * *c;
+        *c = v;
+    }
+}
+
 template <typename T>
 __global__ void k_splitk_reduce(int M, int N, int splits, T alpha, const T* __restrict__ partial,
                                 T beta, T* __restrict__ C, int64_t ldc)
@@ -363,6 +386,22 @@ __global__ void k_splitk_reduce(int M, int N, int splits, T alpha, const T* __re
         if (beta != T(0)) v += beta * *c;
         *c = v;
     }
+}
+
+template <typename T>
+inline void splitk_reduce_launch(int M, int N, int splits, T alpha, const T* partial, T beta, T* C,
+                                 int64_t ldc, cudaStream_t st)
+{
+    const int64_t total = (int64_t)M * N;
+    if (splits >= 16 && total <= 65536) {
+        const unsigned g = (unsigned)((total * 32 + 255) / 256);
+        k_splitk_reduce_warp<T><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
+    } else {
+        unsigned g = (unsigned)((total + 255) / 256);
+        if (g > 152 * 8) g = 152 * 8;
+        k_splitk_reduce<T><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
+    }
+    SKL_LAUNCHED();
 }
 
 // Picks a split-K factor so that the grid covers the GPU when the output is
@@ -424,11 +463,7 @@ inline void gemm_launch_generic(bool ta, bool tb, int M, int N, int K, T alpha, 
     else k_gemm<T, true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
     SKL_LAUNCHED();
     if (splits > 1) {
-        int64_t total = (int64_t)M * N;
-        unsigned g = (unsigned)((total + 255) / 256);
-        if (g > 152 * 8) g = 152 * 8;
-        k_splitk_reduce<T><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
-        SKL_LAUNCHED();
+        splitk_reduce_launch<T>(M, N, splits, alpha, partial, beta, C, ldc, st);
     }
 }
 
@@ -482,11 +517,7 @@ inline void gemm_launch<float>(bool ta, bool tb, int M, int N, int K, float alph
     }
     SKL_LAUNCHED();
     if (splits > 1) {
-        int64_t total = (int64_t)M * N;
-        unsigned g = (unsigned)((total + 255) / 256);
-        if (g > 152 * 8) g = 152 * 8;
-        k_splitk_reduce<float><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
-        SKL_LAUNCHED();
+        splitk_reduce_launch<float>(M, N, splits, alpha, partial, beta, C, ldc, st);
     }
 }
 
