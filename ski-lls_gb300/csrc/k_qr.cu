@@ -332,8 +332,11 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 }
             }
         }
-        __syncthreads();
+        // no barrier here: the next step's first block barrier (after each warp
+        // publishes its candidate) orders these column updates before the
+        // winner's column is pushed, and the candidate buffers alternate by step
     }
+    __syncthreads();   // the selections written by thread 0, for the move plan
     // CTA 0 plans the panel's column moves while the cluster drains
     if (crank == 0) perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
     cluster_sync();   // keep shared memory alive until every CTA finished reading it
