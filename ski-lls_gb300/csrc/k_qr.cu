@@ -200,7 +200,6 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     __shared__ int s_red_i[kYWarps];
     __shared__ T s_cv2[2][kCluster];
     __shared__ int s_ci2[2][kCluster];
-    __shared__ int s_local;
     __shared__ int s_sel[kMaxNb];   // CTA 0: the selections, for the move plan
     __shared__ int s_inlow[kMaxNb];
     __shared__ int s_lowpos[kMaxNb];
@@ -241,7 +240,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
         }
         if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
         __syncthreads();
-        if (wid == 0) {
+        int li;   // this CTA's candidate, reduced redundantly by every warp (no second barrier)
+        {
             T ov = lane < kYWarps ? s_red_v[lane] : T(-1);
             int oi = lane < kYWarps ? s_red_i[lane] : -1;
 #pragma unroll
@@ -251,16 +251,14 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; }
             }
             // push this CTA's candidate to slot crank of every CTA
-            if (lane < kCluster) {
+            if (wid == 0 && lane < kCluster) {
                 dsmem_st(&s_cv2[p][crank], lane, ov);
                 dsmem_st_s32(&s_ci2[p][crank], lane, (oi >= 0) ? c0 + oi : -1);
             }
-            if (lane == 0) s_local = oi;
+            li = oi;
         }
-        __syncthreads();
         T* allc = allc2 + (size_t)p * kCluster * nbp;   // [16][nbp] of this step
         {
-            const int li = s_local;
             const int rows_left = nbp - s;
             T* mine = allc + (size_t)crank * nbp;
             for (int e = tid; e < kCluster * rows_left; e += kYThreads) {
