@@ -323,11 +323,12 @@ k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED
         __syncthreads();
     }
     if (threadIdx.x == 0) partials[blockIdx.x] = ss;
-    if (arrive_last(&S->cnt[1])) {
+    // in the iterations k_lsqr_update reduces the partials itself (every block,
+    // fixed order); only the initial product finalises alpha here
+    if (init && arrive_last(&S->cnt[1])) {
         double tot = block_reduce_partials(partials, gridDim.x);
         if (threadIdx.x == 0) {
             S->alpha_new = sqrt(tot);
-            if (!init) state_update_coefs(S);
             S->cnt[1] = 0;
         }
     }
@@ -725,11 +726,25 @@ k_lsqr_init_v(int r, double* __restrict__ vh, ValT<MIXED>* __restrict__ vs, doub
 template <bool MIXED>
 __global__ void __launch_bounds__(kLThreads)
 k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs,
-              double* __restrict__ w, double* __restrict__ y, LsqrState* __restrict__ S)
+              double* __restrict__ w, double* __restrict__ y, LsqrState* __restrict__ S,
+              const double* __restrict__ partials, int npart)
 {
     if (S->done) return;
+    // alpha' = ||vh|| from tri_t's per-block partials, reduced by every block in
+    // the same fixed order (so every block agrees bit for bit), then the
+    // Givens coefficients by one thread
+    __shared__ double s_coef[3];
+    const double alpha_new = sqrt(block_reduce_partials(partials, npart));
+    if (threadIdx.x == 0) {
+        S->alpha_new = alpha_new;   // same value from every block
+        state_update_coefs(S);
+        s_coef[0] = S->up_t1;
+        s_coef[1] = S->up_t2;
+        s_coef[2] = S->up_ia;
+    }
+    __syncthreads();
     const double beta = S->beta;
-    const double t1 = S->up_t1, t2 = S->up_t2, ia = S->up_ia;
+    const double t1 = s_coef[0], t2 = s_coef[1], ia = s_coef[2];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
         double v = (beta > 0.0) ? vh[i] * ia : 0.0;
         if (beta > 0.0) vs[i] = store_val<MIXED>(v);
@@ -932,7 +947,8 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     SKL_LAUNCHED();
     mark(7);
     unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
-    k_lsqr_update<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
+    k_lsqr_update<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S,
+                                                   B.partials, (int)gt);
     SKL_LAUNCHED();
 }
 
