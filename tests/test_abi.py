@@ -98,3 +98,36 @@ def test_solve_without_gpu_fails_loudly():
     with pytest.raises(skl.SklError) as e:
         skl.ls_sparse_spqr(A, np.ones(40), seed=1)
     assert e.value.status in (skl.SKL_ERR_NO_DEVICE, skl.SKL_ERR_CUDA)
+
+
+def test_python_structs_match_the_c_header(tmp_path):
+    # the ctypes mirrors of skl_csc / skl_opts / skl_info must have the C
+    # layout: size and the offset of every field, from a program compiled
+    # against include/skills_gb300.h
+    import ctypes
+    import subprocess
+    structs = {"skl_csc": skl.SklCsc, "skl_opts": skl.SklOpts, "skl_info": skl.SklInfo}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "skills_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0; }"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    cuda_inc = "/usr/local/cuda/include"
+    r = subprocess.run(["gcc", "-std=c11", "-I", inc, "-I", cuda_inc, str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            parts = line.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
