@@ -93,11 +93,11 @@ SKL_DEV void householder(T alpha, T sigma2, T& beta, T& tau, T& scale)
 // ------------------------------------------------------------ Y-QRP -----
 // QR with column pivoting of Y(:, j0:j0+N) (nbp x N) for b steps; writes the
 // selected columns (relative indices) in selection order to sel[0..b).
-// CTA c of the cluster holds columns [c*cn, c*cn+cn) in shared memory with an
-// odd column stride (conflict-free thread-per-column access).  One step:
-//   local argmax -> publish candidate (norm, index, column) -> cluster barrier
-//   -> every CTA reads all 16 candidates in one batched DSMEM round trip ->
-//   same winner and Householder vector everywhere -> thread-per-column update.
+// CTA c of the cluster holds columns [c*cn, c*cn+cn) in shared memory with
+// column stride ldp (see YqrpSmem).  One step:
+//   local argmax -> push the candidate (norm, index, column) to every CTA ->
+//   cluster barrier -> same winner and Householder vector everywhere ->
+//   update of the untaken columns, 4 lanes per column.
 // Column moves for a panel from its b selections (b <= 64): selected columns
 // go to the front in selection order; the displaced low positions (not
 // selected), in increasing order, fill the vacated high positions (selected
@@ -163,23 +163,44 @@ SKL_DEV void perm_plan_block(const int* s_sel, int* in_low, int* lowpos, int b, 
     if (t == 0) *plan_n = b + n_extra;
 }
 
+// Shared-memory budget of one CTA of the cluster kernels.
+constexpr size_t kClusterSmemBudget = 200 * 1024;
+
+// Column stride of the sample block in shared memory.  The update phase reads
+// 8 columns x 4 consecutive rows per warp: a float stride of 4 x odd puts those
+// 32 words in 32 distinct banks (an odd stride, conflict-free for one thread
+// per column, gives 2-way conflicts there).  The padded stride is used when it
+// fits the budget; FP64 keeps the odd stride.
 template <typename T>
 struct YqrpSmem {
-    __host__ __device__ static int ldp(int nbp) { return nbp | 1; }
-    static size_t bytes(int nbp, int cn)
+    static int ldp_odd(int nbp) { return nbp | 1; }
+    static int ldp_pad(int nbp)
     {
-        size_t s = (size_t)ldp(nbp) * cn * sizeof(T);      // Ys
+        int l = (nbp + 3) & ~3;
+        if (((l >> 2) & 1) == 0) l += 4;
+        return l;
+    }
+    static size_t bytes(int ldp, int nbp, int cn)
+    {
+        size_t s = (size_t)ldp * cn * sizeof(T);            // Ys
         s += (size_t)cn * sizeof(T);                        // nrm
         s += (size_t)cn + 16;                               // taken
         s = (s + 15) & ~(size_t)15;
         s += 2 * (size_t)kCluster * nbp * sizeof(T);        // all candidates' columns [2][16][nbp]
         return s + 256;
     }
+    static int pick_ldp(int nbp, int cn)
+    {
+        if (sizeof(T) == 4 && bytes(ldp_pad(nbp), nbp, cn) <= kClusterSmemBudget) return ldp_pad(nbp);
+        return ldp_odd(nbp);
+    }
 };
 
+// One CTA per SM (min blocks 1): ptxas may use up to 128 registers a thread
+// instead of capping the update loop at 40 with spills.
 template <typename T>
-__global__ void __launch_bounds__(kYThreads)
-k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel,
+__global__ void __launch_bounds__(kYThreads, 1)
+k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b, int* __restrict__ sel,
        int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
        unsigned* __restrict__ status)
 {
@@ -188,7 +209,6 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
     const int cn = (N + kCluster - 1) / kCluster;
     const int c0 = (int)crank * cn;
     const int ncols = max(0, min(cn, N - c0));
-    const int ldp = YqrpSmem<T>::ldp(nbp);
     T* Ys = (T*)smem_raw;
     T* nrm = Ys + (size_t)ldp * cn;
     unsigned char* taken = (unsigned char*)(nrm + cn);
@@ -296,8 +316,10 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
             if (win_local >= 0) taken[win_local] = 1;   // read again only after the next barrier
         }
         // (c) H = I - tau v v^T on the untaken local columns, new norms (rows > s):
-        // 4 lanes per column, passes uniform across the CTA (quad shuffles);
-        // v_r = 1 at r = s, wc[r] * scale below
+        // 4 lanes per column, passes uniform across the CTA (quad shuffles).
+        // v_s = 1 and v_r = scale * wc[r] below, so with u = sum_{r>s} wc[r] col[r]:
+        // w = tau (col[s] + scale u), col[s] -= w, col[r] -= (w scale) wc[r].
+        // Row s is read and written by the quad's first lane only.
         {
             const int q4 = tid & 3;
             const int gcol = tid >> 2;
@@ -308,19 +330,24 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __r
                 const int c = base + gcol;
                 const bool act = c < ncols && !taken[c] && c != win_local;
                 T* col = Ys + (size_t)(act ? c : 0) * ldp;
-                T w = T(0);
-                if (act)
-                    for (int r = s + q4; r < nbp; r += 4) w += (r == s ? T(1) : wc[r] * scale) * col[r];
-                w += __shfl_xor_sync(0xffffffffu, w, 1);
-                w += __shfl_xor_sync(0xffffffffu, w, 2);
-                w *= tau;
+                T u = T(0), cs = T(0);
+                if (act) {
+                    if (q4 == 0) cs = col[s];
+                    for (int r = s + 1 + q4; r < nbp; r += 4) u += wc[r] * col[r];
+                }
+                u += __shfl_xor_sync(0xffffffffu, u, 1);
+                u += __shfl_xor_sync(0xffffffffu, u, 2);
+                cs = __shfl_sync(0xffffffffu, cs, lane & ~3);
+                const T w = tau * (cs + scale * u);
+                const T ws = w * scale;
                 T ss = T(0);
                 if (act) {
-                    for (int r = s + q4; r < nbp; r += 4) {
-                        T y = col[r] - w * (r == s ? T(1) : wc[r] * scale);
+                    for (int r = s + 1 + q4; r < nbp; r += 4) {
+                        const T y = col[r] - ws * wc[r];
                         col[r] = y;
-                        if (r > s) ss += y * y;
+                        ss += y * y;
                     }
+                    if (q4 == 0) col[s] = cs - w;
                 }
                 ss += __shfl_xor_sync(0xffffffffu, ss, 1);
                 ss += __shfl_xor_sync(0xffffffffu, ss, 2);
@@ -791,7 +818,7 @@ static QrPlan qr_plan(int64_t m, int64_t d)
     p.R = (int)((m + kCluster - 1) / kCluster);
     p.R = (p.R + 3) / 4 * 4;   // whole float4 / double2 row vectors
     int nb = kMaxNb;
-    size_t budget = 200 * 1024;
+    const size_t budget = kClusterSmemBudget;
     while (nb > 8 && panel_smem_bytes<T>(p.R, nb) > budget) nb -= 8;
     if (panel_smem_bytes<T>(p.R, nb) > budget)
         fail(SKL_ERR_INVALID, "cpqr: sketch has too many rows for the shared-memory panel (m=" +
@@ -799,7 +826,7 @@ static QrPlan qr_plan(int64_t m, int64_t d)
     p.nb = nb;
     p.nbp = nb + kPP;
     int64_t cn = (d + kCluster - 1) / kCluster;
-    if (YqrpSmem<T>::bytes(p.nbp, (int)cn) > budget)
+    if (YqrpSmem<T>::bytes(YqrpSmem<T>::ldp_odd(p.nbp), p.nbp, (int)cn) > budget)
         fail(SKL_ERR_INVALID, "cpqr: too many columns for the shared-memory sample QRP (d=" +
                                   std::to_string(d) + ")");
     return p;
@@ -955,7 +982,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
                 B.part_cap, st);
         tm.end(8, t0);
     }
-    const size_t ysm_max = YqrpSmem<T>::bytes(nbp, (int)((d + kCluster - 1) / kCluster));
+    // one sample-block stride for every launch of this factorisation, chosen
+    // at the largest column count (later launches need no more shared memory)
+    const int ycn_max = (int)((d + kCluster - 1) / kCluster);
+    const int yldp = YqrpSmem<T>::pick_ldp(nbp, ycn_max);
+    const size_t ysm_max = YqrpSmem<T>::bytes(yldp, nbp, ycn_max);
     const size_t psm = panel_smem_bytes<T>(p.R, nb);
 
     // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
@@ -998,12 +1029,13 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         const T* Yc = B.Y;
         int* sel = B.sel;
         int nbv = nbp;
+        int ldpv = yldp;
         int* psrc = B.plan_src;
         int* pdst = B.plan_dst;
         int* pn = B.plan_n;
         unsigned* stp = status;
-        void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel, &psrc, &pdst,
-                        &pn, &stp};
+        void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &ldpv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
+                        &pdst, &pn, &stp};
         cudaEvent_t t0 = t.begin();
         launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
         t.end(0, t0);
