@@ -240,6 +240,13 @@ SKL_DEV void dsmem_st_s32(int* local, unsigned rank, int v)
 {
     asm volatile("st.shared::cluster.s32 [%0], %1;" :: "r"(dsmem_addr(local, rank)), "r"(v) : "memory");
 }
+// 16-byte remote store; `local` must be 16-byte aligned.
+SKL_DEV void dsmem_st_v4f32(float* local, unsigned rank, float4 v)
+{
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(dsmem_addr(local, rank)),
+                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
 SKL_DEV void dsmem_st(float* local, unsigned rank, float v) { dsmem_st_f32(local, rank, v); }
 SKL_DEV void dsmem_st(double* local, unsigned rank, double v) { dsmem_st_f64(local, rank, v); }
 

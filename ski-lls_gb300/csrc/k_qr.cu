@@ -48,6 +48,7 @@ constexpr int kQrWarps = kQrThreads / 32;
 constexpr int kCluster = 16;
 constexpr int kPP = 16;          // over-sampling rows of the sample Y
 constexpr int kMaxNb = 64;
+static_assert(kYWarps == kCluster, "k_yqrp: warp q pushes to cluster CTA q");
 
 // ------------------------------------------------------------- Gaussian --
 SKL_DEV unsigned long long splitmix64(unsigned long long x)
@@ -171,6 +172,74 @@ constexpr size_t kClusterSmemBudget = 200 * 1024;
 // 32 words in 32 distinct banks (an odd stride, conflict-free for one thread
 // per column, gives 2-way conflicts there).  The padded stride is used when it
 // fits the budget; FP64 keeps the odd stride.
+// Warp-wide argmax of (value, index) pairs: the largest value, ties to the
+// smallest index.  Index -1 marks "no candidate" and carries value -1, below
+// every real value (norms, or -0.5 for a NaN norm).  Every lane returns the
+// result; warp_argmax_lane also returns a lane that held it.  Generic
+// types: an xor tree with that total order.
+template <typename T>
+SKL_DEV int warp_argmax_lane(T& v, int& i)
+{
+    int src = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T xv = __shfl_xor_sync(0xffffffffu, v, o);
+        const int xi = __shfl_xor_sync(0xffffffffu, i, o);
+        const int xs = __shfl_xor_sync(0xffffffffu, src, o);
+        if (xv > v || (xv == v && xi >= 0 && (i < 0 || xi < i))) {
+            v = xv;
+            i = xi;
+            src = xs;
+        }
+    }
+    return src;
+}
+template <typename T>
+SKL_DEV void warp_argmax(T& v, int& i)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T xv = __shfl_xor_sync(0xffffffffu, v, o);
+        const int xi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (xv > v || (xv == v && xi >= 0 && (i < 0 || xi < i))) {
+            v = xv;
+            i = xi;
+        }
+    }
+}
+// float: the value mapped to an unsigned key with the same order, then one
+// warp max over the keys and one warp min over the indices holding the max
+// (redux.sync), instead of five dependent shuffle rounds.  -0.0 does not
+// occur (norms are sums of squares from +0).
+SKL_DEV unsigned f32_order_key(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+SKL_DEV float f32_from_order_key(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+template <>
+SKL_DEV int warp_argmax_lane<float>(float& v, int& i)
+{
+    const unsigned k = f32_order_key(v);
+    const unsigned km = __reduce_max_sync(0xffffffffu, k);
+    const unsigned im = __reduce_min_sync(0xffffffffu, k == km ? (unsigned)i : 0xffffffffu);
+    const int src = __ffs(__ballot_sync(0xffffffffu, k == km && (unsigned)i == im)) - 1;
+    v = f32_from_order_key(km);
+    i = (int)im;
+    return src;
+}
+template <>
+SKL_DEV void warp_argmax<float>(float& v, int& i)
+{
+    const unsigned k = f32_order_key(v);
+    const unsigned km = __reduce_max_sync(0xffffffffu, k);
+    i = (int)__reduce_min_sync(0xffffffffu, k == km ? (unsigned)i : 0xffffffffu);
+    v = f32_from_order_key(km);
+}
+
 template <typename T>
 struct YqrpSmem {
     static int ldp_odd(int nbp) { return nbp | 1; }
@@ -252,24 +321,15 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
     for (int s = 0; s < b; ++s) {
         const int p = s & 1;
         // (a) local argmax
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            T ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
-        }
+        warp_argmax(bv, bi);
         if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
         __syncthreads();
         int li;   // this CTA's candidate, reduced redundantly by every warp (no second barrier)
         {
-            T ov = lane < kYWarps ? s_red_v[lane] : T(-1);
-            int oi = lane < kYWarps ? s_red_i[lane] : -1;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                T xv = __shfl_xor_sync(0xffffffffu, ov, o);
-                int xi = __shfl_xor_sync(0xffffffffu, oi, o);
-                if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; }
-            }
+            // lanes 16-31 repeat the 16 warps' candidates (no change to the argmax)
+            T ov = s_red_v[lane & (kYWarps - 1)];
+            int oi = s_red_i[lane & (kYWarps - 1)];
+            warp_argmax(ov, oi);
             // push this CTA's candidate to slot crank of every CTA
             if (wid == 0 && lane < kCluster) {
                 dsmem_st(&s_cv2[p][crank], lane, ov);
@@ -279,28 +339,33 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
         }
         T* allc = allc2 + (size_t)p * kCluster * nbp;   // [16][nbp] of this step
         {
-            const int rows_left = nbp - s;
+            // warp q pushes rows s.. of the candidate column to CTA q's slot crank
             T* mine = allc + (size_t)crank * nbp;
-            for (int e = tid; e < kCluster * rows_left; e += kYThreads) {
-                const int q = e / rows_left, r = s + e % rows_left;
-                dsmem_st(&mine[r], q, (li >= 0) ? Ys[r + (size_t)li * ldp] : T(0));
+            const T* srcc = Ys + (size_t)(li >= 0 ? li : 0) * ldp;
+            bool done = false;
+            if constexpr (sizeof(T) == 4) {
+                if (((ldp | nbp) & 3) == 0) {   // 16-byte rows: from row s rounded down to 4
+                    const int r0 = s & ~3;
+                    for (int r = r0 + 4 * lane; r < nbp; r += 128) {
+                        const float4 v = li >= 0 ? *(const float4*)(srcc + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        dsmem_st_v4f32((float*)(mine + r), (unsigned)wid, v);
+                    }
+                    done = true;
+                }
             }
+            if (!done)
+                for (int r = s + lane; r < nbp; r += 32)
+                    dsmem_st(&mine[r], (unsigned)wid, (li >= 0) ? srcc[r] : T(0));
         }
         // (b) the barrier's release / acquire makes every CTA's pushes visible
         cluster_sync();
         const T* s_cv = s_cv2[p];
         const int* s_ci = s_ci2[p];
-        // winner and Householder vector, in every warp (no broadcast barrier)
-        T ov = lane < kCluster ? s_cv[lane] : T(-1);
-        int oi = lane < kCluster ? s_ci[lane] : -1;
-        int orank = lane;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const T xv = __shfl_xor_sync(0xffffffffu, ov, o);
-            const int xi = __shfl_xor_sync(0xffffffffu, oi, o);
-            const int xr = __shfl_xor_sync(0xffffffffu, orank, o);
-            if (xv > ov || (xv == ov && xi >= 0 && (oi < 0 || xi < oi))) { ov = xv; oi = xi; orank = xr; }
-        }
+        // winner and Householder vector, in every warp (no broadcast barrier);
+        // lanes 16-31 repeat the 16 candidates
+        T ov = s_cv[lane & (kCluster - 1)];
+        int oi = s_ci[lane & (kCluster - 1)];
+        const int orank = warp_argmax_lane(ov, oi) & (kCluster - 1);
         const T* wc = allc + orank * nbp;
         T sg = T(0);
         for (int r = s + 1 + lane; r < nbp; r += 32) sg += wc[r] * wc[r];
