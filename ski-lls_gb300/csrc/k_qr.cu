@@ -384,21 +384,40 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
         // 4 lanes per column, passes uniform across the CTA (quad shuffles).
         // v_s = 1 and v_r = scale * wc[r] below, so with u = sum_{r>s} wc[r] col[r]:
         // w = tau (col[s] + scale u), col[s] -= w, col[r] -= (w scale) wc[r].
-        // Row s is read and written by the quad's first lane only.
+        // Row s is read and written by the quad's first lane only.  Lane q4 of a
+        // quad owns rows s+1+q4+4i: their wc values stay in registers for the
+        // step, the column's values between the dot product and the update
+        // (fully unrolled over i, with the warp-uniform chunk count nI).
         {
+            constexpr int kRL = (kMaxNb + kPP + 3) / 4;   // rows below s per lane, at most
             const int q4 = tid & 3;
             const int gcol = tid >> 2;
             const int per_pass = kYThreads / 4;
+            const int nI = (nbp - s + 2) >> 2;   // ceil((nbp - s - 1) / 4)
+            T wv[kRL];
+#pragma unroll
+            for (int i = 0; i < kRL; ++i) {
+                const int r = s + 1 + q4 + 4 * i;
+                wv[i] = (i < nI && r < nbp) ? wc[r] : T(0);
+            }
             bv = T(-1);
             bi = -1;
             for (int base = 0; base < ncols; base += per_pass) {
                 const int c = base + gcol;
                 const bool act = c < ncols && !taken[c] && c != win_local;
                 T* col = Ys + (size_t)(act ? c : 0) * ldp;
+                T yv[kRL];
                 T u = T(0), cs = T(0);
-                if (act) {
-                    if (q4 == 0) cs = col[s];
-                    for (int r = s + 1 + q4; r < nbp; r += 4) u += wc[r] * col[r];
+                if (act && q4 == 0) cs = col[s];
+#pragma unroll
+                for (int i = 0; i < kRL; ++i) {
+                    if (i >= nI) break;
+                    const int r = s + 1 + q4 + 4 * i;
+                    yv[i] = T(0);
+                    if (act && r < nbp) {
+                        yv[i] = col[r];
+                        u += wv[i] * yv[i];
+                    }
                 }
                 u += __shfl_xor_sync(0xffffffffu, u, 1);
                 u += __shfl_xor_sync(0xffffffffu, u, 2);
@@ -406,14 +425,17 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
                 const T w = tau * (cs + scale * u);
                 const T ws = w * scale;
                 T ss = T(0);
-                if (act) {
-                    for (int r = s + 1 + q4; r < nbp; r += 4) {
-                        const T y = col[r] - ws * wc[r];
+#pragma unroll
+                for (int i = 0; i < kRL; ++i) {
+                    if (i >= nI) break;
+                    const int r = s + 1 + q4 + 4 * i;
+                    if (act && r < nbp) {
+                        const T y = yv[i] - ws * wv[i];
                         col[r] = y;
                         ss += y * y;
                     }
-                    if (q4 == 0) col[s] = cs - w;
                 }
+                if (act && q4 == 0) col[s] = cs - w;
                 ss += __shfl_xor_sync(0xffffffffu, ss, 1);
                 ss += __shfl_xor_sync(0xffffffffu, ss, 2);
                 if (act) {   // candidate for the next step (columns ascend across passes)
