@@ -366,7 +366,18 @@ int64_t dht_length(int64_t n, int wisdom)
     return N;
 }
 
-static size_t g_optin = 0;
+// Opt-in shared memory per block (the same on every GB300), read once; the
+// initialisation is thread-safe for concurrent solves.
+static size_t smem_optin_bytes()
+{
+    static const size_t v = [] {
+        int dev = 0, o = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return (size_t)o;
+    }();
+    return v;
+}
 
 template <typename T>
 static void launch_dht(const double* A, int64_t lda, int64_t n, int64_t d, const double* D,
@@ -378,14 +389,8 @@ static void launch_dht(const double* A, int64_t lda, int64_t n, int64_t d, const
     FftPlan P;
     if (N & 1) fail(SKL_ERR_INVALID, "DHT length must be even");
     if (!factor_plan(N / 2, P)) fail(SKL_ERR_INVALID, "DHT length must factor into 2,3,5,7");
-    if (!g_optin) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        g_optin = (size_t)v;
-    }
     const size_t need = (size_t)P.L * sizeof(C);
-    const bool in_smem = std::is_same<T, float>::value && need + 1024 <= g_optin &&
+    const bool in_smem = std::is_same<T, float>::value && need + 1024 <= smem_optin_bytes() &&
                          P.L <= kFftSmemMaxL;
     const double scale = 1.0 / std::sqrt((double)N);
     const double alpha_v = (1.0 / std::sqrt((double)k)) * (1.0 / std::sqrt((double)k));

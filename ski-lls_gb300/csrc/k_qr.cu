@@ -883,13 +883,12 @@ __global__ void k_iota_int(int* v, int n)
 template <typename T>
 static bool qr_chol_enabled()
 {
-    static int v = -1;
-    if (v < 0) {
+    static const int v = [] {
         const char* e = getenv("SKILLS_QR_PANEL");
-        if (e && std::string(e) == "pivoted") v = 0;
-        else if (e && std::string(e) == "chol") v = 1;
-        else v = 2;
-    }
+        if (e && std::string(e) == "pivoted") return 0;
+        if (e && std::string(e) == "chol") return 1;
+        return 2;
+    }();
     if (v == 2) return std::is_same<T, float>::value;
     return v == 1;
 }

@@ -124,17 +124,17 @@ k_sketch_sparse_global(const int* __restrict__ cp, const int* __restrict__ ri,
         out[h] = (T)((double)(long long)acc[h] * f);
 }
 
-static size_t g_smem_optin = 0;
-
+// Opt-in shared memory per block (the same on every GB300), read once; the
+// initialisation is thread-safe for concurrent solves.
 static size_t smem_optin()
 {
-    if (!g_smem_optin) {
-        int dev = 0, v = 0;
+    static const size_t v = [] {
+        int dev = 0, o = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        g_smem_optin = (size_t)v;
-    }
-    return g_smem_optin;
+        cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return (size_t)o;
+    }();
+    return v;
 }
 
 template <typename T>

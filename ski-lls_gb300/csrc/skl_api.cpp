@@ -57,11 +57,10 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line)
 
 static int trace_enabled()
 {
-    static int v = -1;
-    if (v < 0) {
-        const char* e = getenv("SKILLS_TRACE");
-        v = (e && e[0] == '1') ? 1 : 0;
-    }
+    static const int v = [] {
+        const char* e = std::getenv("SKILLS_TRACE");
+        return (e && e[0] == '1') ? 1 : 0;
+    }();
     return v;
 }
 
