@@ -64,6 +64,21 @@ def test_dht_is_orthonormal_and_involutive():
         np.testing.assert_allclose(orc.unitary_dht(y, D), x, atol=1e-12)
 
 
+def test_dht_matches_the_cas_definition_with_signs_and_padding():
+    """FFTW's DHT kind (src/fftw_r2r.cpp:45-51) is Y_k = sum_j X_j cas(2 pi j k / N),
+    cas = cos + sin; the reference scales by 1/sqrt(N) and zero-pads to N
+    (src/fast_unitary_transform.cpp:63-64, :79, :98-99)."""
+    rng = np.random.default_rng(11)
+    for n, N in ((6, 6), (7, 7), (10, 16), (30, 42)):
+        x = rng.standard_normal((n, 2))
+        D = rng.choice([-1.0, 1.0], size=n)
+        jk = np.outer(np.arange(N), np.arange(n)) * (2 * np.pi / N)
+        H = (np.cos(jk) + np.sin(jk)) / np.sqrt(N)
+        np.testing.assert_allclose(orc.unitary_dht(x, D, N), H @ (D[:, None] * x), atol=1e-12)
+        if N == n:
+            np.testing.assert_allclose(orc.dht_unscaled(x), np.sqrt(N) * H @ x, atol=1e-12)
+
+
 def test_dense_example_known_answer(fixtures):
     A = fixtures["dense_example/A"]
     b = fixtures["dense_example/b"]
