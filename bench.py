@@ -116,6 +116,47 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# --------------------------------------------------------------- replicas --
+class Replicas:
+    """The ranks of a torchrun launch, one GPU each.  Every rank solves its own
+    problems (the path has no exchange step), so the only collectives are a
+    barrier around the timed region and the max (or sum) of a scalar over
+    ranks.  With one process there is no process group and these are no-ops."""
+
+    def __init__(self, world, backend="nccl", device=None):
+        self.world = world
+        self.device = device
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            kw = {"device_id": device} if backend == "nccl" and device is not None else {}
+            dist.init_process_group(backend, **kw)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def _reduce(self, x, op):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, self.dist.ReduceOp.MAX if self.dist else None)
+
+    def sum(self, x):
+        return self._reduce(x, self.dist.ReduceOp.SUM if self.dist else None)
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 # --------------------------------------------------------------- workload --
 def make_workload(name):
     import synthetic
@@ -188,14 +229,8 @@ def run_ours(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
+    ranks = Replicas(world, "nccl", dev)
+    barrier = ranks.barrier
 
     w, A, b, gen_s = make_workload(args.workload)
     if w["kind"] != "sparse":
@@ -253,11 +288,7 @@ def run_ours(args, rank, world):
     # above is timed without them); the kernel roofline uses these events
     _, infos, _ = timed("mixed", args.steps, 1, 1)
     x_mixed = xd.cpu().numpy()
-    step_s = statistics.mean(ms) / 1e3
-    if dist is not None:
-        t = torch.tensor([step_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s = float(t.item())
+    step_s = ranks.max(statistics.mean(ms) / 1e3)
     last = infos[-1]
 
     fp64 = None
@@ -352,7 +383,7 @@ def run_ours(args, rank, world):
             t = time.perf_counter() - t0
             if q >= max(3, args.warmup):
                 times.append(t)
-        e2e = {"value": statistics.mean(times), "unit": "s",
+        e2e = {"value": ranks.max(statistics.mean(times)), "unit": "s",
                "h2d_bytes_per_step": int(8 * (d + 1) + 16 * nnz + 8 * n),
                "d2h_bytes_per_step": int(8 * d),
                "x_matches_device_path": bool(np.array_equal(hxo.numpy(), x_mixed))}
@@ -415,44 +446,50 @@ def run_batched(args, rank, world):
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    ranks = Replicas(world, "nccl", torch.device("cuda", local))
     t0 = time.perf_counter()
-    probs = synthetic.batched(seed=2024 + rank, count=args.batch_count)
+    probs = synthetic.batched(seed=2024 + rank, count=args.batch_count)   # this rank's shard
     gen_s = time.perf_counter() - t0
+    total = int(ranks.sum(len(probs)))
     warm = probs[: min(8, len(probs))]
     skl.batched_sparse_spqr(warm, 1.7, 2, it_tol=IT_TOL, seed=1, device=local)
     batched_s = []
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
+        ranks.barrier()
         t0 = time.perf_counter()
         xs, infos, status = skl.batched_sparse_spqr(probs, 1.7, 2, it_tol=IT_TOL, seed=1,
                                                     device=local)
-        batched_s.append(time.perf_counter() - t0)
+        batched_s.append(ranks.max(time.perf_counter() - t0))   # the slowest rank's time
     # a loop of single solves (one pass; it is the slow reference point)
     torch.cuda.synchronize()
+    ranks.barrier()
     t0 = time.perf_counter()
     same = True
     for p, (A, b) in enumerate(probs):
         r = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=IT_TOL, seed=1, device=local)
         same = same and np.array_equal(r.x, xs[p])
-    loop_s = time.perf_counter() - t0
+    loop_s = ranks.max(time.perf_counter() - t0)
+    same = ranks.sum(0 if same else 1) == 0
     be = [backward_error(A, xs[p], b) for p, (A, b) in enumerate(probs[:32])]
     if rank != 0:
         return
     best = min(batched_s)
     line = {
-        "metric": "batched sparse solves per second", "value": len(probs) / best,
+        "metric": "batched sparse solves per second", "value": total / best,
         "unit": "problems/s", "n_gpus": world, "steps": len(batched_s), "warmup": 1,
         "ms_per_step": best * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "batched_sparse", "problems": len(probs),
+        "config": {"workload": "batched_sparse", "problems": total,
+                   "problems_per_rank": len(probs),
                    "d_range": [50, 500], "n_rule": "n ~ U[2000, 50000], n >= 20 d",
                    "streams": int(os.environ.get("SKILLS_BATCH_STREAMS", "8")), "gamma": 1.7,
                    "k": 2, "it_tol": IT_TOL, "inputs": "host buffers (H2D inside the timing)"},
-        "e2e": {"value": len(probs) / best, "unit": "problems/s",
+        "e2e": {"value": total / best, "unit": "problems/s",
                 "h2d_bytes_per_step": int(sum(16 * A.nnz + 8 * (A.shape[1] + 1) + 8 * A.shape[0]
                                               for A, _ in probs)),
                 "d2h_bytes_per_step": int(sum(8 * A.shape[1] for A, _ in probs))},
-        "loop_of_single_solves": {"value": len(probs) / loop_s, "unit": "problems/s",
+        "loop_of_single_solves": {"value": total / loop_s, "unit": "problems/s",
                                   "batched_speedup": loop_s / best,
                                   "x_bit_identical": bool(same)},
         "status_ok": int(sum(1 for s_ in status if s_ == 0)),
