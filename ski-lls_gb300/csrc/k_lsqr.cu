@@ -1081,14 +1081,6 @@ k_tri_n_f64acc(const MT* __restrict__ Mr, int64_t ldm, int r, const double* __re
 }
 
 // x_full[cols[i]] = colscale[cols[i]] * (M yv)[i] (FP64 output), other entries untouched.
-__global__ void k_split_vec(const double* __restrict__ x, int n, float2* __restrict__ out)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        ff f = ff_from_double(x[i]);
-        out[i] = make_float2(f.hi, f.lo);
-    }
-}
-
 void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
                    cudaStream_t st)
 {

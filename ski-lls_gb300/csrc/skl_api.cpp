@@ -259,7 +259,6 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     info.sketch_rows = m;
 
     // ---- workspace layout (sized once, then carved) ----
-    const size_t vsz = mixed ? sizeof(float2) : sizeof(double);
     const size_t qr_ws = cpqr_workspace_bytes<T>(m, d);
     const size_t inv_ws = trinv_workspace_bytes<T>(d) + (size_t)d * d * sizeof(T);
     LsqrProblem Pq;
