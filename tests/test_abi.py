@@ -100,6 +100,55 @@ def test_solve_without_gpu_fails_loudly():
     assert e.value.status in (skl.SKL_ERR_NO_DEVICE, skl.SKL_ERR_CUDA)
 
 
+def test_argument_errors_come_before_any_device_work(L):
+    """The argument checks run before a device is touched, so they answer on a
+    machine without a GPU, with the reference's message for m < n
+    (src/ls_sparse_spqr.cpp:98-101, src/ls_dense_hashing_blendenpik.cpp:41-44);
+    d = 0 is an empty solve.  The library stays usable after each error."""
+    import ctypes
+    vp = ctypes.c_void_p
+
+    def sparse(m, n, p, b, x, **opt):
+        o = skl.default_opts()
+        for k, v in opt.items():
+            setattr(o, k, v)
+        A = skl.SklCsc(m, n, int(p[-1]) if p is not None else 0,
+                       p.ctypes.data if p is not None else None, None, None)
+        info = skl.SklInfo()
+        return L.skl_sparse_solve(ctypes.byref(A), vp(b), vp(x), ctypes.byref(o), ctypes.byref(info))
+
+    def dense(n, d, lda, **opt):
+        o = skl.default_opts()
+        for k, v in opt.items():
+            setattr(o, k, v)
+        a, b, x = np.zeros(max(lda * d, 1)), np.ones(max(n, 1)), np.zeros(max(d, 1))
+        info = skl.SklInfo()
+        return L.skl_dense_solve(vp(a.ctypes.data), lda, n, d, vp(b.ctypes.data), vp(x.ctypes.data),
+                                 ctypes.byref(o), ctypes.byref(info))
+
+    b, x = np.ones(8), np.zeros(8)
+    p5 = np.zeros(6, np.int64)
+    assert sparse(4, 5, p5, b.ctypes.data, x.ctypes.data) == skl.SKL_ERR_NOT_OVERDETERMINED
+    assert skl.last_error() == "Matrix is not overdetermined."
+    assert L.skl_sparse_solve(None, vp(b.ctypes.data), vp(x.ctypes.data), None, None) == skl.SKL_ERR_INVALID
+    assert "A is null" in skl.last_error()
+    p3 = np.zeros(4, np.int64)
+    assert sparse(8, 3, p3, b.ctypes.data, x.ctypes.data, gamma=0.0) == skl.SKL_ERR_INVALID
+    assert "gamma" in skl.last_error()
+    assert sparse(8, 3, p3, b.ctypes.data, x.ctypes.data, k=0) == skl.SKL_ERR_INVALID
+    assert sparse(8, 3, p3, b.ctypes.data, x.ctypes.data, precision=7) == skl.SKL_ERR_INVALID
+    assert sparse(8, 3, p3, None, x.ctypes.data) == skl.SKL_ERR_INVALID
+    assert "null" in skl.last_error()
+    assert sparse(8, 0, np.zeros(1, np.int64), b.ctypes.data, x.ctypes.data) == skl.SKL_OK
+    assert skl.last_error() == ""
+
+    assert dense(4, 5, 4) == skl.SKL_ERR_NOT_OVERDETERMINED
+    assert skl.last_error() == "Matrix is not overdetermined."
+    assert dense(8, 3, 5) == skl.SKL_ERR_INVALID
+    assert "lda" in skl.last_error()
+    assert dense(8, 0, 8) == skl.SKL_OK
+
+
 def test_python_structs_match_the_c_header(tmp_path):
     # the ctypes mirrors of skl_csc / skl_opts / skl_info must have the C
     # layout: size and the offset of every field, from a program compiled
