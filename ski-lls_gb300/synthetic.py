@@ -65,7 +65,6 @@ def sparse_illcond(seed=2024, n=120000, d=5000, per_col=1200, n_dep=50, scale_ex
     # replace n_dep columns by a*A_p + b*A_q with p, q outside the replaced set
     dep = rng.choice(d, size=n_dep, replace=False)
     keep = np.setdiff1d(np.arange(d), dep)
-    A = A.tolil() if n_dep and d < 2000 else A
     if n_dep:
         p = rng.choice(keep, size=n_dep)
         q = rng.choice(keep, size=n_dep)
@@ -76,8 +75,6 @@ def sparse_illcond(seed=2024, n=120000, d=5000, per_col=1200, n_dep=50, scale_ex
                              (np.concatenate([p, q]), np.concatenate([np.arange(n_dep)] * 2))),
                             shape=(d, n_dep))
         newcols = (A @ mix).tocsc()
-        keep_mask = np.ones(d, dtype=bool)
-        keep_mask[dep] = False
         # assemble: columns `dep` taken from newcols, others from A
         order = np.empty(d, dtype=np.int64)
         order[keep] = np.arange(keep.size)
