@@ -5,6 +5,7 @@
 // entries are summed.  Throws std::runtime_error on malformed input.
 #pragma once
 #include <algorithm>
+#include <cctype>
 #include <cstdint>
 #include <cstdio>
 #include <fstream>
