@@ -114,3 +114,20 @@ def test_full_rank_fixtures_vs_lstsq(fixtures, tag):
     xr = np.linalg.lstsq(As, b, rcond=None)[0]
     out = orc.ls_sparse_spqr(n, d, p, i, x, b, 1.4, 2, it_tol=1e-12)
     assert np.linalg.norm(out["x"] - xr) <= 1e-8 * np.linalg.norm(xr)
+
+
+@pytest.mark.parametrize("tag", FULL_RANK_TAGS)
+def test_noCPQR_full_rank_fixtures_vs_lstsq(fixtures, tag):
+    """The _noCPQR restatement (unpivoted QR of the sketch, LSQR from zero) on
+    the reference's dense full-rank fixtures, against LAPACK least squares."""
+    Ad = fixtures[f"{tag}DenseFullRank/dense"]
+    b = np.ones(Ad.shape[0])
+    xr = np.linalg.lstsq(Ad, b, rcond=None)[0]
+    out = orc.ls_dense_hashing_blendenpik_noCPQR(Ad, b, 1.7, 1, it_tol=1e-12, seed=5)
+    assert out["rank"] == Ad.shape[1] and out["flag"] == 0
+    assert np.linalg.norm(out["x"] - xr) <= 1e-8 * np.linalg.norm(xr)
+
+
+def test_noCPQR_rejects_underdetermined():
+    with pytest.raises(RuntimeError, match="Matrix is not overdetermined."):
+        orc.ls_dense_hashing_blendenpik_noCPQR(np.ones((3, 5)), np.ones(3), 1.7, 1)
