@@ -13,13 +13,17 @@
 //     3. trailing update A(j:m, j+nb:) <- Q^T A(j:m, j+nb:)  (skint.c:540-551);
 //     4. Y downdate and G <- G Q  (skint.c:554-568, :627-718).
 //
-// GB300 mapping.  Steps 1 and 2 are chains of rank-1 steps, each needing a
-// reduction over the whole column set or row set.  Each runs as ONE cluster
-// of 16 CTAs with the operand resident in the cluster's shared memory
-// (distributed shared memory): a reduction is a write to local shared memory,
-// a hardware cluster barrier (~0.25 us) and DSMEM loads, instead of a
-// grid-wide barrier (~2 us) or a kernel launch per column.  Steps 3-4 are
-// GEMMs.  The sample G is drawn on the device from a counter-based generator
+// GB300 mapping.  Step 1 is a chain of rank-1 steps, each needing a reduction
+// over the whole column set; it runs as ONE cluster of 16 CTAs with the sample
+// resident in the cluster's shared memory: each CTA pushes its candidate to
+// every CTA with remote shared-memory stores, then one hardware cluster
+// barrier (~0.25 us) replaces a grid-wide barrier (~2 us) or a launch per
+// column.  Step 2 on the FP32 path is CholeskyQR2 of the panel in the order
+// the sample chose (GEMMs over the whole GPU plus small one-CTA kernels, in
+// k_qr_chol.cu), falling back to the pivoted cluster panel (k_panel) when the
+// Cholesky breaks down; the FP64 path uses k_panel.  Steps 3-4 are GEMMs, the
+// sample work (step 4 and the next step 1) on a second, high-priority stream
+// overlapping the trailing update.  The sample G is drawn on the device from a counter-based generator
 // (the reference draws it from srand(12) + Marsaglia's polar method,
 // skint.c:390,584-624; the pivots of a randomized QR are not expected to be
 // reproduced bit for bit, only the solution).
