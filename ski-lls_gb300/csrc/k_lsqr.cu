@@ -14,8 +14,10 @@
 //   tri_t   vh = M^T t - (beta'/alpha) vh  (triangular mat-vec, column-major M), alpha'
 //   update  Givens rotation, x += (phi/rho) w, w = v - (theta/rho) w, stop test
 // u and v are kept unnormalised (uh = beta u, vh = alpha v) so normalisation
-// folds into the next product.  Norms are reduced by the last block of each
-// kernel in a fixed order, so every run is bitwise reproducible.
+// folds into the next product.  Norms are reduced from per-block partials in a
+// fixed order (by the last block of spmv_n; tri_t's partials by every block of
+// the update kernel, which needs alpha' anyway), so every run is bitwise
+// reproducible.
 //
 // Mixed precision: the products accumulate in float-float (see common.cuh):
 // matrix values are stored as (hi, lo) float pairs (8 bytes, like FP64), the
