@@ -22,6 +22,8 @@
  *   skl_trsv_upper    <- cs_usolve/utsolve_cholmod_structure, dtrsv
  *                                                        src/sparse_helpers.cpp:122-181,
  *                                                        src/IterSolver.cpp:89,95
+ *   skl_csc_mv        <- csc_mv 'n' / 't' (CSC_Mat::mv)  src/SpMat.cpp:37-74,
+ *                                                        include/SpMat.hpp:132-136
  */
 #ifndef SKILLS_GB300_H
 #define SKILLS_GB300_H
@@ -67,7 +69,10 @@ typedef struct {
     double perturb;          /* sparse path: pivot perturbation when ill cond.    */
     double rcond;            /* dense path: minimal |R_ii| kept (absolute rule)   */
     double rank_tol;         /* sparse path: relative rank tolerance on |R_ii|;
-                                <= 0 selects 20*(m+d)*eps(working precision)     */
+                                <= 0 selects 20*(m+d)*eps_64 (SPQR's default) on
+                                the FP64 path and 2*sqrt(m)*eps_32 on the mixed
+                                path, which keeps the columns below it in LSQR's
+                                basis (skl_info.unresolved_cols); > 0 drops them */
     int precision;           /* skl_precision                                     */
     int use_cpqr;            /* dense path: 1 = CPQR + rank (ls_dense_hashing_blendenpik),
                                 0 = unpivoted QR (..._noCPQR)                     */
@@ -115,6 +120,15 @@ typedef struct {
     /* mixed path: refinement steps of the explicit sketch solution against
        the FP64 residual (each ||b - A xs|| at least halved) */
     int64_t sketch_refine_steps;
+    /* mixed sparse path: pivoted columns whose |R_ii| lies below what the
+       FP32 factorization resolves (2 sqrt(m) eps_32 |R_00|).  They are not
+       dropped: LSQR carries them with unit preconditioning, so its FP64-class
+       iteration decides whether they reduce the residual.  Not counted in
+       `rank`. */
+    int64_t unresolved_cols;
+    /* mixed dense path: 1 if A held values outside [2^-100, 2^100] in
+       magnitude and the solve ran on the FP64 path instead */
+    int fp64_fallback;
 } skl_info;
 
 /* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,
@@ -236,6 +250,14 @@ skl_status skl_cpqr(double* A, int64_t m, int64_t d, int precision, int64_t* jpv
  * inverse used by the LSQR operator. */
 skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, int precision,
                           double* x);
+
+/* y = A x (trans 'n', y has A->m entries) or y = A^T x ('t', A->n entries)
+ * through the LSQR product kernels of the solve, with their storage: on the
+ * mixed path A's values are equilibrated by column and held as (hi, lo)
+ * float pairs with float-float accumulation (relative error of each entry
+ * <= 2^-45 of sum_j |a_ij x_j|); on the FP64 path plain FP64.  Replaces the
+ * reference's csc_mv (src/SpMat.cpp:37-74) for checking the operator. */
+skl_status skl_csc_mv(const skl_csc* A, char trans, const double* x, double* y, int precision);
 
 /* Release all device memory and streams held by the library. */
 void skl_finalize(void);

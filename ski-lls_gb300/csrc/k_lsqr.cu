@@ -20,9 +20,11 @@
 // reproducible.
 //
 // Mixed precision: the products accumulate in float-float (see common.cuh):
-// matrix values are stored as (hi, lo) float pairs (8 bytes, like FP64), the
-// input vectors as (hi, lo) pairs, and the scalar recurrences stay in FP64.
-// The all-FP64 path uses plain double values and DFMA.
+// matrix values are stored as (hi, lo) float pairs (8 bytes, like FP64, with
+// 48 of FP64's 53 significand bits), the input vectors as (hi, lo) pairs, and
+// the scalar recurrences stay in FP64.  On the sparse path the pairs hold the
+// equilibrated values A(:, c) / ||A(:, c)||, so no value leaves the float
+// range.  The all-FP64 path uses plain double values and DFMA.
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -253,7 +255,8 @@ SKL_DEV void block_reduce2(Acc<MIXED>& a, Acc<MIXED>& b, Acc<MIXED>* sm)
 }
 
 // ------------------------------------------------------------- tri_n -----
-// z[cols[i]] = colscale[cols[i]] * sum_{j>=i} M[i][j] v[j]   (Mr row-major)
+// z[cols[i]] = colscale[cols[i]] * sum_{j>=i} M[i][j] v[j]   (Mr row-major;
+// colscale == nullptr: no scale, the stored values are already equilibrated)
 // One block per row pair (i, r-1-i): every block reads ~r+1 entries.
 template <bool MIXED>
 __global__ void __launch_bounds__(kTriThreads, MIXED ? kTriMinBlocks : 1)
@@ -273,12 +276,12 @@ k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED
         block_reduce2<MIXED>(a, b, sm);
         if (threadIdx.x == 0) {
             int c = cols[i1];
-            double val = colscale[c] * a.value();
+            double val = (colscale ? colscale[c] : 1.0) * a.value();
             if (plain_out) zplain[c] = val;
             else z[c] = store_val<MIXED>(val);
             if (i2 != i1) {
                 c = cols[i2];
-                val = colscale[c] * b.value();
+                val = (colscale ? colscale[c] : 1.0) * b.value();
                 if (plain_out) zplain[c] = val;
                 else z[c] = store_val<MIXED>(val);
             }
@@ -526,6 +529,7 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
 
 // --------------------------------------------------------- spmv_t (CSC) --
 // t[i] = colscale[c] * (sum_{p in col c} A[p] u[row p]) / beta,  c = cols[i]
+// (colscale == nullptr: no scale)
 // L lanes per column, kTU entries per lane per step; the (index, value) loads
 // of the next step are issued before the gathers of the current step are
 // consumed, so the HBM stream of A overlaps the L2 gathers of u.  Each warp
@@ -585,7 +589,8 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
         acc.add(acc2);
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
-        if (active && lane == 0) t[i] = store_val<MIXED>(colscale[c] * acc.value() * ib);
+        if (active && lane == 0)
+            t[i] = store_val<MIXED>((colscale ? colscale[c] : 1.0) * acc.value() * ib);
     }
 }
 
@@ -661,7 +666,7 @@ k_spmv_t_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int*
         if (threadIdx.x == 0) {
             Acc<MIXED> s = red[0];
             for (int q = 1; q < kLThreads / 32; ++q) s.add(red[q]);
-            t[i] = store_val<MIXED>(colscale[c] * s.value() * ib);
+            t[i] = store_val<MIXED>((colscale ? colscale[c] : 1.0) * s.value() * ib);
         }
         __syncthreads();
     }
@@ -897,7 +902,7 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     if (P.Ad) {
         unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
         k_spmv_t_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
-                                                       P.colscale, (int)P.r, (const V*)B.us,
+                                                       P.opscale, (int)P.r, (const V*)B.us,
                                                        (V*)B.t, B.S);
         SKL_LAUNCHED();
         return;
@@ -906,7 +911,7 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     const int L = lanes_for(avg);
     const int64_t threads = (int64_t)P.r * L;
     unsigned g = (unsigned)std::min<int64_t>((threads + kLThreads - 1) / kLThreads, 152 * 32);
-#define SPMV_T(LL) k_spmv_t_csc<MIXED, LL><<<g, kLThreads, 0, st>>>(P.cp, P.ri, (const V*)P.rx, P.cols, P.colscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
+#define SPMV_T(LL) k_spmv_t_csc<MIXED, LL><<<g, kLThreads, 0, st>>>(P.cp, P.ri, (const V*)P.rx, P.cols, P.opscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
     if (L == 32) SPMV_T(32);
     else if (L == 16) SPMV_T(16);
     else if (L == 8) SPMV_T(8);
@@ -934,7 +939,7 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     const unsigned gt = tri_blocks(P.r);
     mark(4);
     k_tri_n<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
-                                              P.cols, P.colscale, (V*)B.z, B.S, 0, nullptr);
+                                              P.cols, P.opscale, (V*)B.z, B.S, 0, nullptr);
     SKL_LAUNCHED();
     mark(5);
     mark(0);
@@ -1058,6 +1063,65 @@ LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t m
     if (P.precision == SKL_PREC_MIXED)
         return run_impl<true>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
     return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
+}
+
+// ------------------------------------------------ one product in isolation --
+// y = A x ('n', the CSR kernel of spmv_n) or y = A^T x ('t', the CSC kernel of
+// spmv_t) with the storage and arithmetic LSQR uses: on the mixed path the
+// stored values are A(:, c) * vscale[c], so the input is divided by vscale
+// ('n') or the output ('t').  Used to measure the operator's accuracy.
+template <bool MIXED>
+__global__ void k_prod_in(const double* __restrict__ x, int64_t len, const double* __restrict__ vscale,
+                          ValT<MIXED>* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = store_val<MIXED>(vscale ? x[i] / vscale[i] : x[i]);
+}
+
+template <bool MIXED>
+__global__ void k_prod_out(const ValT<MIXED>* __restrict__ v, const double* __restrict__ vplain,
+                           int64_t len, const double* __restrict__ vscale, double* __restrict__ y)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double val;
+        if constexpr (MIXED) val = (double)v[i].x + (double)v[i].y;
+        else val = vplain ? vplain[i] : v[i];
+        y[i] = vscale ? val / vscale[i] : val;
+    }
+}
+
+template <bool MIXED>
+static void product_impl(const LsqrProblem& P, char trans, const double* x, double* y,
+                         const double* vscale, void* work, cudaStream_t st)
+{
+    using V = ValT<MIXED>;
+    LsqrBufs B = carve(P, work);
+    LsqrState init{};
+    init.ib = 1.0;   // t = A^T u / beta with beta = 1; coef_n = 0: u = A z
+    SKL_CUDA(cudaMemcpyAsync(B.S, &init, sizeof(LsqrState), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(B.uh, 0, P.n * sizeof(double), st));
+    SKL_CUDA(cudaMemsetAsync(B.us, 0, P.n * sizeof(V), st));
+    const unsigned g = 152 * 8;
+    if (trans == 'n') {
+        k_prod_in<MIXED><<<g, 256, 0, st>>>(x, P.d, vscale, (V*)B.z);
+        launch_spmv_n<MIXED>(P, B, st);
+        k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.us, MIXED ? nullptr : B.uh, P.n, nullptr, y);
+    } else {
+        k_prod_in<MIXED><<<g, 256, 0, st>>>(x, P.n, nullptr, (V*)B.us);
+        launch_spmv_t<MIXED>(P, B, st);
+        k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.t, nullptr, P.r, vscale, y);
+    }
+    SKL_LAUNCHED();
+    SKL_LAUNCHED();
+}
+
+void lsqr_product(const LsqrProblem& P, char trans, const double* x, double* y,
+                  const double* vscale, void* work, cudaStream_t st)
+{
+    if (P.precision == SKL_PREC_MIXED) product_impl<true>(P, trans, x, y, vscale, work, st);
+    else product_impl<false>(P, trans, x, y, vscale, work, st);
 }
 
 // Final assembly x_full[cols[i]] = colscale[cols[i]] * (M y)[i] with FP64
@@ -1346,43 +1410,118 @@ void residual_and_backward(const LsqrProblem& P, const double* x, const double* 
     for (int q = 0; q < 4; ++q) SKL_LAUNCHED();
 }
 
-// (hi, lo) float pairs of FP64 values (matrix storage of the mixed path).
-__global__ void k_split_vals(const double* __restrict__ x, int64_t n, float2* __restrict__ out)
+// (hi, lo) float pairs of the equilibrated values A(:, c) * colscale[c] (the
+// matrix storage of the mixed sparse path).  The pair carries 48 of the 53
+// significand bits (|v - hi - lo| <= 2^-48 |v|); with |v| <= 1 neither part
+// overflows, and a value that underflows is below 2^-126 of its column's norm.
+__global__ void k_split_csr_scaled(const int* __restrict__ ci, const double* __restrict__ cx,
+                                   int64_t nnz, const double* __restrict__ colscale,
+                                   float2* __restrict__ out)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        ff f = ff_from_double(x[i]);
-        out[i] = make_float2(f.hi, f.lo);
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        ff f = ff_from_double(cx[p] * colscale[ci[p]]);
+        out[p] = make_float2(f.hi, f.lo);
     }
 }
 
-void split_values(const double* x, int64_t n, float2* out, cudaStream_t st)
+void split_csr_scaled(const int* ci, const double* cx, int64_t nnz, const double* colscale,
+                      float2* out, cudaStream_t st)
 {
-    if (n <= 0) return;
-    unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32);
-    k_split_vals<<<g, 256, 0, st>>>(x, n, out);
+    if (nnz <= 0) return;
+    unsigned g = (unsigned)std::min<int64_t>((nnz + 255) / 256, 152 * 32);
+    k_split_csr_scaled<<<g, 256, 0, st>>>(ci, cx, nnz, colscale, out);
     SKL_LAUNCHED();
 }
 
-// Dense matrix variant: column-major n x d with lda -> packed n x d float2.
-__global__ void k_split_dense(const double* __restrict__ A, int64_t lda, int64_t n, int64_t d,
-                              float2* __restrict__ out)
+// CSC variant: one warp per column.
+__global__ void __launch_bounds__(kLThreads)
+k_split_csc_scaled(const int* __restrict__ cp, const double* __restrict__ Ax, int d,
+                   const double* __restrict__ colscale, float2* __restrict__ out)
 {
-    int64_t total = n * d;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = gw; c < d; c += nw) {
+        const double s = colscale[c];
+        for (int p = cp[c] + lane; p < cp[c + 1]; p += 32) {
+            ff f = ff_from_double(Ax[p] * s);
+            out[p] = make_float2(f.hi, f.lo);
+        }
+    }
+}
+
+void split_csc_scaled(const int* cp, const double* Ax, int64_t d, const double* colscale,
+                      float2* out, cudaStream_t st)
+{
+    if (d <= 0) return;
+    unsigned g = (unsigned)std::min<int64_t>((d * 32 + kLThreads - 1) / kLThreads, 152 * 16);
+    k_split_csc_scaled<<<g, kLThreads, 0, st>>>(cp, Ax, (int)d, colscale, out);
+    SKL_LAUNCHED();
+}
+
+// Dense matrix: column-major n x d with lda -> packed n x d float2.  A nonzero
+// magnitude outside [2^-100, 2^100] sets kStatusRange: the FP32 sketch and
+// the float pairs lose accuracy there, and the caller takes the FP64 path.
+__global__ void k_split_dense(const double* __restrict__ A, int64_t lda, int64_t n, int64_t d,
+                              float2* __restrict__ out, unsigned* __restrict__ status)
+{
+    const int64_t total = n * d;
+    bool bad = false;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = e % n, j = e / n;
-        ff f = ff_from_double(A[i + j * lda]);
+        const int64_t i = e % n, j = e / n;
+        const double a = A[i + j * lda];
+        const double aa = fabs(a);
+        bad |= (aa > 0x1p100) || (aa != 0.0 && aa < 0x1p-100);
+        ff f = ff_from_double(a);
         out[e] = make_float2(f.hi, f.lo);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, kStatusRange);
+}
+
+void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out,
+                 unsigned* status, cudaStream_t st)
+{
+    if (n * d <= 0) return;
+    k_split_dense<<<152 * 32, 256, 0, st>>>(A, lda, n, d, out, status);
+    SKL_LAUNCHED();
+}
+
+__global__ void k_vec_add(double* __restrict__ x, const double* __restrict__ a, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += a[i];
+}
+
+void vec_add(double* x, const double* a, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return;
+    unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    k_vec_add<<<g, 256, 0, st>>>(x, a, n);
+    SKL_LAUNCHED();
+}
+
+template <typename T>
+__global__ void k_extend_identity(T* __restrict__ Mc, int64_t ldm, int r, int r2)
+{
+    for (int j = r + blockIdx.x; j < r2; j += gridDim.x) {
+        T* col = Mc + (int64_t)j * ldm;
+        for (int i = threadIdx.x; i <= j; i += blockDim.x) col[i] = (i == j) ? T(1) : T(0);
     }
 }
 
-void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out, cudaStream_t st)
+template <typename T>
+void extend_identity(T* Mc, int64_t ldm, int64_t r, int64_t r2, cudaStream_t st)
 {
-    if (n * d <= 0) return;
-    k_split_dense<<<152 * 32, 256, 0, st>>>(A, lda, n, d, out);
+    if (r2 <= r) return;
+    unsigned g = (unsigned)std::min<int64_t>(r2 - r, 152 * 8);
+    k_extend_identity<T><<<g, 256, 0, st>>>(Mc, ldm, (int)r, (int)r2);
     SKL_LAUNCHED();
 }
+template void extend_identity<float>(float*, int64_t, int64_t, int64_t, cudaStream_t);
+template void extend_identity<double>(double*, int64_t, int64_t, int64_t, cudaStream_t);
 
 // Row-major copy of the r x r upper triangle (for the forward triangular product).
 template <typename T>

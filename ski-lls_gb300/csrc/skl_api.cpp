@@ -315,10 +315,6 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
     csc_narrow(in.Ap, in.Ai, in.Ax, n, d, nnz, cp, ri, C.dev_status, st);
     build_csr(cp, ri, in.Ax, n, d, nnz, rp, ci, cx, (int*)work, st);
-    if (mixed) {
-        split_values(cx, nnz, cx2, st);
-        split_values(in.Ax, nnz, rx2, st);
-    }
     // ---- hash stream (host) -> device buckets ----
     if (hash_thread) hash_thread->join();
     if (!host_hidx || (int64_t)host_hidx->size() != n * k)
@@ -338,6 +334,12 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     // ---- sketch ----
     sketch_sparse<T>(cp, ri, in.Ax, n, d, hidx, (int)k, m, SA, ld, 1, colnorm, colscale, st);
     sketch_rhs(bptr, bent, m, (int)k, in.b, cvec, st);
+    if (mixed) {
+        // LSQR's float pairs hold the equilibrated values A(:, c) / ||A(:, c)||:
+        // |value| <= 1, so no finite input overflows the float range
+        split_csr_scaled(ci, cx, nnz, colscale, cx2, st);
+        split_csc_scaled(cp, in.Ax, d, colscale, rx2, st);
+    }
     trace_phase(st, "sketch");
     SKL_CUDA(cudaEventRecord(ev[3], st));
     // ---- randomized CPQR, c = Q^T S b ----
@@ -347,12 +349,26 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     trace_phase(st, "cpqr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank, inverse, condition ----
+    // FP64: SPQR's default tolerance 20 (m + d) eps relative to the largest
+    // (equilibrated) column.  FP32: an exactly dependent column leaves |R_ii|
+    // of up to ~sqrt(m) eps_32 |R_00| (measured: 1.6e-6 at m = 8,500), so the
+    // factorization resolves nothing below 2 sqrt(m) eps_32.  Columns under
+    // that bound are not dropped: they stay in LSQR's basis with unit
+    // preconditioning (M extended by an identity block), and the FP64-class
+    // iteration decides whether they reduce the residual, as an FP64
+    // factorization would have.  Exactly dependent ones cost nothing there
+    // (their gradient is a combination of the resolved columns' gradients).
     double rel = o.rank_tol;
-    if (!(rel > 0.0)) rel = mixed ? 1e-5 : 20.0 * (double)(m + d) * 2.220446049250313e-16;
+    const bool carry_unresolved = mixed && !(rel > 0.0);
+    if (!(rel > 0.0))
+        rel = mixed ? 2.0 * std::sqrt((double)m) * 5.960464477539063e-08
+                    : 20.0 * (double)(m + d) * 2.220446049250313e-16;
     int64_t rank = count_rank<T>(SA, ld, mn, 0.0, rel, dint, (int*)C.host_pinned, st);
     if (rank == 0) fail(SKL_ERR_RANK_ZERO, "SPQR Factorization fails");
     info.rank = rank;
-    const int64_t ldm = round_up(rank, 4);   // 16-byte aligned rows/columns of M
+    const int64_t rank_lsqr = carry_unresolved ? mn : rank;
+    info.unresolved_cols = rank_lsqr - rank;
+    const int64_t ldm = round_up(rank_lsqr, 4);   // 16-byte aligned rows/columns of M
     trinv_upper<T>(SA, ld, rank, 0.0, Mc, ldm, norms, work, st);
     SKL_CUDA(cudaMemcpyAsync(C.host_pinned, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     SKL_CUDA(cudaStreamSynchronize(st));
@@ -363,7 +379,8 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     if (!info.success && o.perturb != 0.0) {
         trinv_upper<T>(SA, ld, rank, o.perturb, Mc, ldm, norms, work, st);
     }
-    transpose_upper<T>(Mc, ldm, rank, Mr, st);
+    extend_identity<T>(Mc, ldm, rank, rank_lsqr, st);
+    transpose_upper<T>(Mc, ldm, rank_lsqr, Mr, st);
     trace_phase(st, "rank+inverse");
     LsqrProblem P;
     P.n = n; P.d = d; P.nnz = nnz;
@@ -371,8 +388,9 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     P.cp = cp; P.ri = ri; P.rx = mixed ? (const void*)rx2 : (const void*)in.Ax;
     P.cx64 = cx; P.rx64 = in.Ax;
     P.cols = jpvt; P.colscale = colscale;
+    P.opscale = mixed ? nullptr : colscale;   // the float pairs are already equilibrated
     P.M = Mc; P.Mrow = Mr; P.ldm = ldm; P.r = rank; P.precision = o.precision;
-    // ---- explicit sketch solution xs = D P1 M c ----
+    // ---- explicit sketch solution xs = D P1 M c (resolved columns only) ----
     SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
     precond_apply(P, cvec, x_dev, ysplit, st);
     residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
@@ -435,7 +453,13 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     }
     double be = (rnorm > 0 && fro > 0) ? ((double*)C.host_pinned)[1] / (fro * rnorm) : 0.0;
     if (!(rnorm < o.abs_tol)) {
-        // ---- LSQR from r_s; x = D P1 M (c + y) ----
+        // ---- LSQR from r_s; x = x_s + D P1 M y (src/ls_sparse_spqr.cpp:181-208) ----
+        // The correction is added to the same rounded x_s that r_s was formed
+        // from: LSQR compensates x_s's rounding, and D P1 M (c + y) recomputed
+        // in one product would re-round it with cond(R) amplification (on the
+        // 120,000 x 5,000 workload that left ||b - A x|| 1.4e-3 relative above
+        // the minimum and the backward error at 2.3e-3 instead of 3.4e-4).
+        P.r = rank_lsqr;
         int64_t total_it = 0;
         int flag = 1;
         int64_t restarts = 0;
@@ -452,21 +476,9 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
         add_prof(R);
         total_it += R.it;
         flag = R.flag;
-        // y <- y + c (first r entries), x = D P1 M y
-        {
-            auto add_c = [&](double* yy) {
-                std::vector<double> h((size_t)rank), hc((size_t)rank);
-                SKL_CUDA(cudaMemcpyAsync(h.data(), yy, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
-                SKL_CUDA(cudaMemcpyAsync(hc.data(), cvec, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
-                SKL_CUDA(cudaStreamSynchronize(st));
-                for (int64_t i = 0; i < rank; ++i) h[(size_t)i] += hc[(size_t)i];
-                SKL_CUDA(cudaMemcpyAsync(yy, h.data(), rank * sizeof(double), cudaMemcpyHostToDevice, st));
-                SKL_CUDA(cudaStreamSynchronize(st));
-            };
-            add_c(yv);
-        }
-        SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
-        precond_apply(P, yv, x_dev, ysplit, st);
+        SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
+        precond_apply(P, yv, xacc, ysplit, st);
+        vec_add(x_dev, xacc, d, st);
         residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
         SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
@@ -482,13 +494,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
             flag = R.flag;
             SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
             precond_apply(P, yv, xacc, ysplit, st);
-            // x += xacc
-            std::vector<double> hx((size_t)d), ha((size_t)d);
-            SKL_CUDA(cudaMemcpyAsync(hx.data(), x_dev, d * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaMemcpyAsync(ha.data(), xacc, d * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaStreamSynchronize(st));
-            for (int64_t j = 0; j < d; ++j) hx[(size_t)j] += ha[(size_t)j];
-            SKL_CUDA(cudaMemcpyAsync(x_dev, hx.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+            vec_add(x_dev, xacc, d, st);
             residual_and_backward(P, x_dev, in.b, rs, part, scal, st);
             SKL_CUDA(cudaMemcpyAsync(C.host_pinned, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
             SKL_CUDA(cudaStreamSynchronize(st));
@@ -727,8 +733,10 @@ static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double*
 // with use_cpqr = 0, ls_dense_hashing_blendenpik_noCPQR
 // (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-59).
 
+// Returns false (nothing solved) when the mixed path meets values outside its
+// range; the caller then runs the FP64 pipeline.
 template <typename T>
-static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t lda, int64_t n,
+static bool dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t lda, int64_t n,
                            int64_t d, const double* b, double* x_dev, const skl_opts& o,
                            skl_info& info, bool timing_upload, std::thread* host_thread,
                            const std::vector<double>* hD, const std::vector<uint32_t>* hh,
@@ -784,13 +792,17 @@ static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
     float2* ysplit = Ar.alloc<float2>(d);
     cudaEvent_t* ev = C.ev;
     SKL_CUDA(cudaEventRecord(ev[1], st));
-    if (mixed) split_dense(A, lda, n, d, A2, st);
+    if (mixed) {
+        SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+        split_dense(A, lda, n, d, A2, C.dev_status, st);
+    }
     {
         std::vector<double> ones((size_t)d, 1.0);
         SKL_CUDA(cudaMemcpyAsync(colscale, ones.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
         SKL_CUDA(cudaStreamSynchronize(st));
     }
-    host_thread->join();
+    if (mixed && (read_status(C, st) & kStatusRange)) return false;
+    if (host_thread->joinable()) host_thread->join();
     SKL_CUDA(cudaMemcpyAsync(Dd, hD->data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
     SKL_CUDA(cudaMemcpyAsync(hidx, hh->data(), N * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
     build_buckets(hidx, N, (int)k, m, bptr, bent, (int*)work, st);
@@ -877,16 +889,12 @@ static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
         add_prof(R);
         int64_t total_it = R.it;
         int flag = R.flag;
-        if (cpqr_on) {
-            std::vector<double> h((size_t)rank), hc((size_t)rank);
-            SKL_CUDA(cudaMemcpyAsync(h.data(), yv, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaMemcpyAsync(hc.data(), cvec, rank * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaStreamSynchronize(st));
-            for (int64_t i = 0; i < rank; ++i) h[(size_t)i] += hc[(size_t)i];
-            SKL_CUDA(cudaMemcpyAsync(yv, h.data(), rank * sizeof(double), cudaMemcpyHostToDevice, st));
-        }
-        SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
-        precond_apply(P, yv, x_dev, ysplit, st);
+        // x = x_s + P1 M y (src/ls_dense_hashing_blendenpik.cpp:130-144; x_s = 0
+        // on the noCPQR path): the correction is added to the rounded x_s that
+        // r_s was formed from
+        SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
+        precond_apply(P, yv, xacc, ysplit, st);
+        vec_add(x_dev, xacc, d, st);
         residual();
         int64_t restarts = 0;
         while (o.backward_tol > 0.0 && be > o.backward_tol && restarts < o.max_refine &&
@@ -899,12 +907,7 @@ static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
             flag = R.flag;
             SKL_CUDA(cudaMemsetAsync(xacc, 0, d * sizeof(double), st));
             precond_apply(P, yv, xacc, ysplit, st);
-            std::vector<double> hx((size_t)d), ha((size_t)d);
-            SKL_CUDA(cudaMemcpyAsync(hx.data(), x_dev, d * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaMemcpyAsync(ha.data(), xacc, d * sizeof(double), cudaMemcpyDeviceToHost, st));
-            SKL_CUDA(cudaStreamSynchronize(st));
-            for (int64_t j = 0; j < d; ++j) hx[(size_t)j] += ha[(size_t)j];
-            SKL_CUDA(cudaMemcpyAsync(x_dev, hx.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+            vec_add(x_dev, xacc, d, st);
             residual();
         }
         info.it = total_it;
@@ -921,6 +924,29 @@ static void dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
     info.t_lsqr_ms = elapsed(ev[5], ev[6]);
     info.t_total_ms = elapsed(timing_upload ? ev[0] : ev[1], ev[6]);
     if (timing_upload) info.t_upload_ms = elapsed(ev[0], ev[1]);
+    return true;
+}
+
+// The mixed pipeline, or the FP64 one when the mixed one declines the input.
+static void dense_pipeline_any(Context& C, cudaStream_t st, const double* A, int64_t lda,
+                               int64_t n, int64_t d, const double* b, double* x_dev,
+                               const skl_opts& o, skl_info& info, bool timing_upload,
+                               std::thread* host_thread, const std::vector<double>* hD,
+                               const std::vector<uint32_t>* hh, int64_t N)
+{
+    if (o.precision == SKL_PREC_MIXED &&
+        dense_pipeline<float>(C, st, A, lda, n, d, b, x_dev, o, info, timing_upload, host_thread,
+                              hD, hh, N))
+        return;
+    const bool fell_back = o.precision == SKL_PREC_MIXED;
+    if (fell_back) {
+        std::memset(&info, 0, sizeof info);
+        info.fp64_fallback = 1;
+    }
+    skl_opts o64 = o;
+    o64.precision = SKL_PREC_FP64;
+    dense_pipeline<double>(C, st, A, lda, n, d, b, x_dev, o64, info, timing_upload, host_thread,
+                           hD, hh, N);
 }
 
 static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
@@ -979,17 +1005,11 @@ static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t 
         SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double),
                                    d, cudaMemcpyHostToDevice, st));
         SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
-        if (o.precision == SKL_PREC_MIXED)
-            dense_pipeline<float>(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
-        else
-            dense_pipeline<double>(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
+        dense_pipeline_any(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
         SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
     } else {
-        if (o.precision == SKL_PREC_MIXED)
-            dense_pipeline<float>(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
-        else
-            dense_pipeline<double>(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
+        dense_pipeline_any(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
     }
     // HQRRP reseeds the C library stream with srand(12) and draws its Gaussian
     // sample (hqrrp/.../NoFLA_HQRRP_WY_blk_var4_skint.c:390,414) when

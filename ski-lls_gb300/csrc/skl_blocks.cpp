@@ -216,6 +216,83 @@ static void sketch_dense_block(const double* A, int64_t lda, int64_t n, int64_t 
     SKL_CUDA(cudaStreamSynchronize(st));
 }
 
+// y = A x or A^T x through LSQR's product kernels.  The mixed path stores the
+// equilibrated values A(:, c) / ||A(:, c)|| as (hi, lo) float pairs, as the
+// sparse solve does.
+static void csc_mv_block(const skl_csc* A, char trans, const double* x, double* y, int precision)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const bool mixed = precision != SKL_PREC_FP64;
+    const int64_t n = A->m, d = A->n, nnz = A->p[d];
+    if (n > 0x7fffffff || d > 0x7fffffff || nnz > 0x7fffffff)
+        fail(SKL_ERR_INVALID, "skl_csc_mv: problem too large for 32-bit device indices");
+    std::vector<double> cs((size_t)d, 1.0);
+    for (int64_t j = 0; j < d; ++j) {
+        double ss = 0.0;
+        for (int64_t p = A->p[j]; p < A->p[j + 1]; ++p) ss += A->x[p] * A->x[p];
+        if (mixed && ss > 0.0) cs[(size_t)j] = 1.0 / std::sqrt(ss);
+    }
+    std::vector<int> cols((size_t)d);
+    for (int64_t j = 0; j < d; ++j) cols[(size_t)j] = (int)j;
+    LsqrProblem P;
+    P.n = n; P.d = d; P.nnz = nnz; P.r = d; P.precision = mixed ? SKL_PREC_MIXED : SKL_PREC_FP64;
+    const size_t ws = lsqr_workspace_bytes(P);
+    Sizer S;
+    S.add<int64_t>(d + 1); S.add<int64_t>(nnz); S.add<double>(nnz);
+    S.add<int>(d + 1); S.add<int>(nnz); S.add<int>(n + 1); S.add<int>(nnz); S.add<double>(nnz);
+    S.add<float2>(nnz); S.add<float2>(nnz); S.add<double>(d); S.add<int>(d);
+    S.add<double>(n); S.add<double>(n);
+    S.add<char>((int64_t)std::max(ws, build_csr_scratch_ints(n, nnz) * sizeof(int)));
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    Arena& Ar = C.arena;
+    int64_t* Ap = Ar.alloc<int64_t>(d + 1);
+    int64_t* Ai = Ar.alloc<int64_t>(nnz);
+    double* Ax = Ar.alloc<double>(nnz);
+    int* cp = Ar.alloc<int>(d + 1);
+    int* ri = Ar.alloc<int>(nnz);
+    int* rp = Ar.alloc<int>(n + 1);
+    int* ci = Ar.alloc<int>(nnz);
+    double* cx = Ar.alloc<double>(nnz);
+    float2* cx2 = Ar.alloc<float2>(nnz);
+    float2* rx2 = Ar.alloc<float2>(nnz);
+    double* csd = Ar.alloc<double>(d);
+    int* colsd = Ar.alloc<int>(d);
+    double* xd = Ar.alloc<double>(n);
+    double* yd = Ar.alloc<double>(n);
+    void* work = Ar.take(std::max(ws, build_csr_scratch_ints(n, nnz) * sizeof(int)));
+    SKL_CUDA(cudaMemcpyAsync(Ap, A->p, (d + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    if (nnz) {
+        SKL_CUDA(cudaMemcpyAsync(Ai, A->i, nnz * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        SKL_CUDA(cudaMemcpyAsync(Ax, A->x, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    SKL_CUDA(cudaMemcpyAsync(csd, cs.data(), d * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpyAsync(colsd, cols.data(), d * sizeof(int), cudaMemcpyHostToDevice, st));
+    const int64_t lin = trans == 'n' ? d : n, lout = trans == 'n' ? n : d;
+    SKL_CUDA(cudaMemcpyAsync(xd, x, lin * sizeof(double), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+    csc_narrow(Ap, Ai, Ax, n, d, nnz, cp, ri, C.dev_status, st);
+    build_csr(cp, ri, Ax, n, d, nnz, rp, ci, cx, (int*)work, st);
+    {
+        unsigned stt = 0;
+        SKL_CUDA(cudaMemcpyAsync(&stt, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        SKL_CUDA(cudaStreamSynchronize(st));
+        if (stt & 3u) fail(SKL_ERR_INVALID, "skl_csc_mv: invalid CSC structure");
+        if (stt & 4u) fail(SKL_ERR_NONFINITE, "A contains NaN or Inf");
+    }
+    if (mixed) {
+        split_csr_scaled(ci, cx, nnz, csd, cx2, st);
+        split_csc_scaled(cp, Ax, d, csd, rx2, st);
+    }
+    P.rp = rp; P.ci = ci; P.cx = mixed ? (const void*)cx2 : (const void*)cx;
+    P.cp = cp; P.ri = ri; P.rx = mixed ? (const void*)rx2 : (const void*)Ax;
+    P.cols = colsd; P.colscale = csd; P.opscale = nullptr;
+    lsqr_product(P, trans, xd, yd, mixed ? csd : nullptr, work, st);
+    SKL_CUDA(cudaMemcpyAsync(y, yd, lout * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+}
+
 }  // namespace skl
 
 using namespace skl;
@@ -252,6 +329,21 @@ skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, in
         if (!R || !x || r <= 0 || ld < r) fail(SKL_ERR_INVALID, "skl_trsv_upper: bad argument");
         if (precision == SKL_PREC_FP64) trsv_block<double>(R, ld, r, trans, x);
         else trsv_block<float>(R, ld, r, trans, x);
+    });
+}
+
+skl_status skl_csc_mv(const skl_csc* A, char trans, const double* x, double* y, int precision)
+{
+    return guard([&] {
+        if (!A || !A->p || !x || !y || A->m < 0 || A->n < 0 || (trans != 'n' && trans != 't'))
+            fail(SKL_ERR_INVALID, "skl_csc_mv: bad argument");
+        if (A->p[A->n] > 0 && (!A->i || !A->x)) fail(SKL_ERR_INVALID, "skl_csc_mv: bad argument");
+        if (A->m == 0 || A->n == 0) {
+            const int64_t lout = trans == 'n' ? A->m : A->n;
+            for (int64_t i = 0; i < lout; ++i) y[i] = 0.0;
+            return;
+        }
+        csc_mv_block(A, trans, x, y, precision);
     });
 }
 

@@ -187,6 +187,10 @@ struct LsqrProblem {
     // row-major copy Mrow, both ldm)
     const int* cols = nullptr;
     const double* colscale = nullptr;
+    // scale the LSQR products apply to column c of the stored values: colscale
+    // when the stored values are A's own, nullptr (1) when they already hold
+    // A(:, c) * colscale[c] (the mixed sparse path) or D = I (dense paths)
+    const double* opscale = nullptr;
     const void* M = nullptr; const void* Mrow = nullptr; int64_t ldm = 0; int64_t r = 0;
     int precision = SKL_PREC_MIXED;
 };
@@ -203,6 +207,12 @@ size_t lsqr_workspace_bytes(const LsqrProblem& P);
 LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t max_it, double* y,
                     void* work, unsigned* status, void* host_pinned, cudaStream_t st,
                     int profile = 0, cudaStream_t capture_stream = nullptr);
+// One product in isolation with LSQR's storage and arithmetic: y = A x
+// (trans 'n', CSR kernel) or y = A^T x ('t', CSC kernel, P.cols = 0..d-1,
+// P.r = d).  The stored values are A(:, c) * vscale[c] (vscale nullptr: A's
+// own); work holds lsqr_workspace_bytes(P).
+void lsqr_product(const LsqrProblem& P, char trans, const double* x, double* y,
+                  const double* vscale, void* work, cudaStream_t st);
 // xfull[cols[i]] = colscale[cols[i]] * (M yv)[i]; scratch holds r float2.
 void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
                    cudaStream_t st);
@@ -222,8 +232,24 @@ void sketch_refine_direction(const LsqrProblem& P, const int* bptr, const unsign
 void sketch_refine_apply(const LsqrProblem& P, double sgn, const double* dc, double* c,
                          const double* b, double* x, double* rs, double* part, double* rnorm,
                          cudaStream_t st);
-void split_values(const double* x, int64_t n, float2* out, cudaStream_t st);
-void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out, cudaStream_t st);
+// (hi, lo) float pairs of the equilibrated values A(:, c) * colscale[c]
+// (|value| <= 1, so neither part overflows): CSR entries (column ci[p]) and
+// CSC entries (columns by cp).
+void split_csr_scaled(const int* ci, const double* cx, int64_t nnz, const double* colscale,
+                      float2* out, cudaStream_t st);
+void split_csc_scaled(const int* cp, const double* Ax, int64_t d, const double* colscale,
+                      float2* out, cudaStream_t st);
+// (hi, lo) float pairs of a dense column-major A; sets kStatusRange in
+// *status if a nonzero |A_ij| lies outside [2^-100, 2^100].
+constexpr unsigned kStatusRange = 32u;
+void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out,
+                 unsigned* status, cudaStream_t st);
+// x[0..n) += a[0..n)
+void vec_add(double* x, const double* a, int64_t n, cudaStream_t st);
+// Columns r..r2-1 of the upper-triangular M (column-major, ldm) become the
+// unit vectors e_j (zeros above the diagonal, 1 on it).
+template <typename T>
+void extend_identity(T* Mc, int64_t ldm, int64_t r, int64_t r2, cudaStream_t st);
 template <typename T>
 void transpose_upper(const T* Mc, int64_t ldm, int64_t r, T* Mr, cudaStream_t st);
 

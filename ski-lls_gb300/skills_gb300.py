@@ -77,7 +77,8 @@ class SklInfo(ctypes.Structure):
                 ("t_lsqr_ms", ctypes.c_double), ("t_host_hash_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("prof_ms", ctypes.c_double * 4),
                 ("prof_launches", ctypes.c_int64 * 4), ("qr_prof_ms", ctypes.c_double * 9),
-                ("sketch_refine_steps", ctypes.c_int64)]
+                ("sketch_refine_steps", ctypes.c_int64), ("unresolved_cols", ctypes.c_int64),
+                ("fp64_fallback", ctypes.c_int)]
 
     def as_dict(self):
         out = {}
@@ -134,6 +135,8 @@ def lib():
         L.skl_cpqr.restype = ctypes.c_int
         L.skl_trsv_upper.argtypes = [vp, i64, i64, ctypes.c_char, ctypes.c_int, vp]
         L.skl_trsv_upper.restype = ctypes.c_int
+        L.skl_csc_mv.argtypes = [ctypes.POINTER(SklCsc), ctypes.c_char, vp, vp, ctypes.c_int]
+        L.skl_csc_mv.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -366,6 +369,20 @@ def trsv_upper(R, x, trans="n", precision="mixed"):
     _check(lib().skl_trsv_upper(_ptr(R), max(R.shape[0], 1), r, trans.encode(), PREC[precision],
                                 _ptr(xx)))
     return xx
+
+
+def csc_mv(A, x, trans="n", precision="mixed"):
+    """y = A x ('n') or A^T x ('t') through the solve's LSQR product kernels
+    (mixed: equilibrated float-pair storage, float-float accumulation)."""
+    indptr, indices, data, shape = _as_csc(A)
+    n, d = shape
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    if xx.shape != ((d,) if trans == "n" else (n,)):
+        raise ValueError("x has the wrong length")
+    y = np.zeros(n if trans == "n" else d, dtype=np.float64)
+    csc = SklCsc(n, d, int(indptr[-1]), indptr.ctypes.data, indices.ctypes.data, data.ctypes.data)
+    _check(lib().skl_csc_mv(ctypes.byref(csc), trans.encode(), _ptr(xx), _ptr(y), PREC[precision]))
+    return y
 
 
 def dht_length(n, wisdom=0):

@@ -1,0 +1,204 @@
+"""GPU parity at the benchmark configurations' full sizes.
+
+  20,000 x 1,000 sparse (s = 2)         x to 1e-8 of the oracle, backward error <= 1e-10
+  40,000 x 4,000 dense, kappa = 1e6     x to 1e-8 of a dense FP64 Householder QR solve,
+                                         backward error <= 1e-10
+  120,000 x 5,000 sparse, column scales 10^U[0,8], 50 dependent columns
+                                         ||b - A x|| (correctly rounded) within 1e-6
+                                         relative of the oracle's, same rank
+  120,000 x 5,000 sparse, unscaled, full rank
+                                         x to 1e-8 of the oracle
+  1,000,000 x 10,000 sparse, Zipf columns (s = 3)
+                                         mixed vs FP64 path: ||b - A x|| to 1e-9,
+                                         backward error <= 1e-10 on both
+plus the cases the benchmark shapes do not reach: genuine columns with
+|R_ii| / |R_00| ~ 1e-6 (below what an FP32 factorization resolves), values
+near 1e40 and 1e-40, the global-memory sketch kernel (sketch column larger
+than shared memory), and the error bound of the mixed LSQR products.
+
+The 120,000 x 5,000 configuration's residual is ~13 orders of magnitude below
+||A|| ||x||, so residuals are evaluated exactly (tests/accurate.py): an FP64
+evaluation there is off by ~10 % per entry.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sla
+import scipy.sparse as sp
+
+import accurate
+import skills_gb300 as skl
+import ski_lls_oracle as orc
+import synthetic
+
+pytestmark = pytest.mark.gpu
+
+XTOL = 1e-8
+BETOL = 1e-10
+
+
+def _orc_sparse(A, b, gamma, k, it_tol):
+    n, d = A.shape
+    return orc.ls_sparse_spqr(n, d, A.indptr, A.indices, A.data, b, gamma, k, it_tol=it_tol,
+                              rng=orc.Rng(1))
+
+
+@pytest.fixture(scope="module")
+def illcond():
+    A, b, _ = synthetic.sparse_illcond()
+    ref = _orc_sparse(A, b, 1.7, 2, 1e-10)
+    return A, b, ref, accurate.residual_norm(A, ref["x"], b), accurate.backward_error(A, ref["x"], b)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_illcond_120000x5000_residual_parity(illcond, precision):
+    A, b, ref, rn_ref, be_ref = illcond
+    res = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-10, seed=1, precision=precision)
+    rn = accurate.residual_norm(A, res.x, b)
+    assert abs(rn - rn_ref) <= 1e-6 * rn_ref, (precision, rn, rn_ref)
+    assert res.rank == ref["rank"] == 4950
+    # the backward error's floor here is the rounding of x to FP64 (~3e-4 for
+    # the oracle, ~6e-4 after a 1-ulp perturbation of its x)
+    be = accurate.backward_error(A, res.x, b)
+    assert be <= 3.0 * be_ref, (precision, be, be_ref)
+
+
+def test_unscaled_120000x5000_x_parity():
+    A, b, _ = synthetic.sparse_illcond(seed=5, scale_exp=0.0, n_dep=0)
+    ref = _orc_sparse(A, b, 1.7, 2, 1e-10)
+    for precision in ("mixed", "fp64"):
+        res = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-10, seed=1, precision=precision)
+        assert res.rank == ref["rank"] == 5000
+        assert np.linalg.norm(res.x - ref["x"]) <= XTOL * np.linalg.norm(ref["x"]), precision
+
+
+def test_sparse_20000x1000_vs_oracle():
+    A, b = synthetic.sparse_uniform_1pct()
+    ref = _orc_sparse(A, b, 1.7, 2, 1e-10)
+    for precision in ("mixed", "fp64"):
+        res = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-10, seed=1, precision=precision,
+                                 backward_tol=BETOL)
+        assert res.rank == ref["rank"] == 1000
+        assert np.linalg.norm(res.x - ref["x"]) <= XTOL * np.linalg.norm(ref["x"]), precision
+        assert accurate.backward_error(A, res.x, b) <= BETOL, precision
+
+
+def test_dense_40000x4000_kappa1e6():
+    A, b = synthetic.dense_kappa()
+    Q, R = np.linalg.qr(A)
+    x_qr = sla.solve_triangular(R, Q.T @ b)
+    del Q
+    fro = np.linalg.norm(A)
+    for precision in ("mixed", "fp64"):
+        res = skl.ls_dense_hashing_blendenpik(A, b, 1.7, 1, it_tol=1e-10, seed=1,
+                                              precision=precision, backward_tol=BETOL)
+        assert res.rank == 4000
+        assert np.linalg.norm(res.x - x_qr) <= XTOL * np.linalg.norm(x_qr), precision
+        r = b - A @ res.x
+        be = np.linalg.norm(A.T @ r) / (fro * np.linalg.norm(r))
+        assert be <= BETOL, (precision, be)
+
+
+def test_zipf_1000000x10000_mixed_vs_fp64():
+    A, b = synthetic.sparse_zipf()
+    fro = sp.linalg.norm(A, "fro")
+    rn = {}
+    for precision in ("mixed", "fp64"):
+        res = skl.ls_sparse_spqr(A, b, 1.5, 3, it_tol=1e-10, seed=1, precision=precision)
+        r = b - A @ res.x
+        rn[precision] = np.linalg.norm(r)
+        be = np.linalg.norm(A.T @ r) / (fro * rn[precision])
+        assert be <= BETOL, (precision, be)
+    assert abs(rn["mixed"] - rn["fp64"]) <= 1e-9 * rn["fp64"], rn
+
+
+def _near_dependent(n=6000, d=300, nnear=6, rel=1e-6, seed=7):
+    """Random sparse A whose columns `near` equal another column plus a
+    perturbation of relative size `rel`: genuine columns that an FP64
+    factorization keeps and an FP32 one cannot tell from dependent ones."""
+    rng = np.random.default_rng(seed)
+    A, _ = synthetic.sparse_uniform(n, d, 60, 11, 1e-3)
+    A = A.tolil()
+    near = rng.choice(d, nnear, replace=False)
+    for j, c in enumerate(near):
+        p = (c + 1 + j) % d
+        col = A[:, p].toarray().ravel()
+        pert = np.zeros(n)
+        idx = rng.choice(n, 60, replace=False)
+        pert[idx] = rng.standard_normal(60)
+        pert *= rel * np.linalg.norm(col) / np.linalg.norm(pert)
+        A[:, c] = (col + pert).reshape(-1, 1)
+    A = A.tocsc()
+    A.sort_indices()
+    return A, rng.standard_normal(n)
+
+
+def test_genuine_columns_below_fp32_resolution():
+    A, b = _near_dependent()
+    ref = _orc_sparse(A, b, 1.7, 2, 1e-12)
+    assert ref["rank"] == 300
+    rn_ref = accurate.residual_norm(A, ref["x"], b)
+    mixed = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-12, seed=1, precision="mixed")
+    assert mixed.info["unresolved_cols"] >= 6
+    rn = accurate.residual_norm(A, mixed.x, b)
+    # dropping the six columns would leave ||r|| ~5e-5 relative above the minimum
+    assert abs(rn - rn_ref) <= 1e-9 * rn_ref, (rn, rn_ref)
+    fp64 = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-12, seed=1, precision="fp64")
+    assert fp64.rank == 300 and fp64.info["unresolved_cols"] == 0
+    assert abs(accurate.residual_norm(A, fp64.x, b) - rn_ref) <= 1e-9 * rn_ref
+
+
+def test_values_near_float_range_limits():
+    # columns scaled by 1e40 and 1e-40: beyond FP32's range as raw values;
+    # the mixed path stores the equilibrated values, the dense mixed path
+    # hands such inputs to the FP64 path
+    rng = np.random.default_rng(3)
+    A, b = synthetic.sparse_uniform(4000, 120, 80, 17, 1e-3)
+    scale = np.ones(120)
+    scale[:10] = 1e40
+    scale[10:20] = 1e-40
+    As = (A @ sp.diags(scale)).tocsc()
+    As.sort_indices()
+    b = A @ rng.standard_normal(120) + 1e-3 * rng.standard_normal(4000)
+    # exact LS solution of the scaled problem: x = D^-1 lstsq(A, b)
+    y = np.linalg.lstsq(A.toarray(), b, rcond=None)[0]
+    for precision in ("mixed", "fp64"):
+        res = skl.ls_sparse_spqr(As, b, 1.7, 2, it_tol=1e-12, seed=1, precision=precision)
+        assert res.rank == 120
+        ys = res.x * scale
+        assert np.linalg.norm(ys - y) <= XTOL * np.linalg.norm(y), precision
+    Ad = As.toarray()
+    mixed = skl.ls_dense_hashing_blendenpik(Ad, b, 1.7, 1, it_tol=1e-12, seed=5, precision="mixed")
+    fp64 = skl.ls_dense_hashing_blendenpik(Ad, b, 1.7, 1, it_tol=1e-12, seed=5, precision="fp64")
+    assert mixed.info["fp64_fallback"] == 1 and fp64.info["fp64_fallback"] == 0
+    assert np.array_equal(mixed.x, fp64.x)
+
+
+def test_sketch_global_memory_kernel():
+    # m * 8 B beyond the per-block shared memory: the global-memory column kernel
+    A, b = synthetic.sparse_uniform(60000, 24, 3000, 23, 1e-3)
+    m, k = 40000, 3
+    rows, vals = orc.gen_hashing(orc.Rng(9), m, 60000, k)
+    SA_ref, Sb_ref = orc.sparse_sketch(60000, 24, A.indptr, A.indices, A.data, b, m, k, rows, vals)
+    SA, Sb = skl.sketch_sparse(A, b, m, k, rows, vals, precision="fp64")
+    assert np.max(np.abs(SA - SA_ref)) <= 1e-13 * np.max(np.abs(SA_ref))
+    np.testing.assert_array_equal(Sb, Sb_ref)
+    SA32, _ = skl.sketch_sparse(A, b, m, k, rows, vals, precision="mixed")
+    assert np.max(np.abs(SA32 - SA_ref)) <= 1e-6 * np.max(np.abs(SA_ref))
+
+
+def test_mixed_operator_error_bound(illcond):
+    # float-float products over (hi, lo) pairs of the equilibrated values:
+    # each entry within 2^-45 of sum_j |a_ij x_j| (FP64 path: (row length) eps)
+    A, b, ref, _, _ = illcond
+    rng = np.random.default_rng(1)
+    z = rng.standard_normal(A.shape[1]) * 10.0 ** rng.uniform(-8, 0, A.shape[1])
+    u = rng.standard_normal(A.shape[0])
+    exact_n = -accurate.residual(A, z, np.zeros(A.shape[0]))
+    exact_t = -accurate.residual(A.T.tocsc(), u, np.zeros(A.shape[1]))
+    bound_n = abs(A) @ np.abs(z)
+    bound_t = abs(A).T @ np.abs(u)
+    for precision, tol in (("mixed", 2.0 ** -45), ("fp64", 2.0 ** -44)):
+        yn = skl.csc_mv(A, z, "n", precision)
+        yt = skl.csc_mv(A, u, "t", precision)
+        assert np.max(np.abs(yn - exact_n) / bound_n) <= tol, precision
+        assert np.max(np.abs(yt - exact_t) / bound_t) <= tol, precision
