@@ -2,17 +2,22 @@
 """Time-to-solve benchmark of the GB300 Ski-LLS solve path.
 
 One step = one full solve (sketch -> randomized CPQR -> preconditioned LSQR)
-of the named workload.  Default workload: the 120,000 x 5,000, 1 %-dense,
-column-scaled (kappa ~ 1e8), rank-deficient sparse problem, s = 2, m = 1.7 d,
-LSQR tolerance 1e-10, mixed precision (FP32 sketch/QR, FP64 LSQR).
+of the named workload, inputs resident in HBM.  Default workload: the
+120,000 x 5,000, 1 %-dense, column-scaled (kappa ~ 1e8), rank-deficient
+sparse problem, s = 2, m = 1.7 d, LSQR tolerance 1e-10, mixed precision.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--no-cpu-baseline] [--no-fp64]
+                    [--workload NAME] [--no-cpu-baseline] [--no-fp64] [--no-e2e]
+    python bench.py --workload NAME --profile-one [--precision mixed|fp64] [--repeats R]
 
-Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): every rank solves its
-own replica (the single-problem path does not shard); the reported time is
-the max over ranks.  The reference arm (--impl reference) times the CPU
-oracle, a restatement of the reference algorithm, on the host cores.
+Workloads: sparse_uniform_20000x1000, dense_kappa1e6_40000x4000,
+sparse_illcond_120000x5000 (default), sparse_zipf_1000000x10000,
+batched_sparse.  Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): every
+rank solves its own replica (the single-problem path does not shard); the
+reported time is the max over ranks.  The reference arm (--impl reference)
+times the CPU oracle, a restatement of the reference algorithm, on the host
+cores.  --profile-one runs one solve with the library's per-kernel events on
+(the command the ncu summaries under profiles/ were taken with).
 """
 from __future__ import annotations
 
@@ -52,6 +57,11 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512,
                     help="problems in the batched_sparse workload")
+    ap.add_argument("--profile-one", action="store_true",
+                    help="one solve with per-kernel events, for profilers")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--repeats", type=int, default=1)
+    ap.add_argument("--oracle-once", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -161,27 +171,101 @@ class Replicas:
 # --------------------------------------------------------------- workload --
 def make_workload(name):
     import synthetic
+    if name not in synthetic.WORKLOADS:
+        raise SystemExit(f"unknown workload {name}; choose from {sorted(synthetic.WORKLOADS)} "
+                         "or batched_sparse")
     w = synthetic.WORKLOADS[name]
     t0 = time.perf_counter()
     A, b = w["gen"]()
+    if w["kind"] == "sparse":
+        A = A.tocsc()
+        A.sort_indices()
+    else:
+        A = np.asfortranarray(A)
     return w, A, b, time.perf_counter() - t0
 
 
 def oracle_solve(kind, A, b, gamma, k):
     import ski_lls_oracle as orc
     if kind == "sparse":
-        A = A.tocsc()
         return orc.ls_sparse_spqr(A.shape[0], A.shape[1], A.indptr, A.indices, A.data, b, gamma,
                                   k, it_tol=IT_TOL, rng=orc.Rng(1))
     return orc.ls_dense_hashing_blendenpik(A, b, gamma, k, it_tol=IT_TOL, seed=1)
 
 
-def backward_error(A, x, b):
+def exact_quality(A, x, b):
+    """||b - A x|| and ||A^T r|| / (||A||_F ||r||) with r correctly rounded."""
+    import accurate
+    r = accurate.residual(A, x, b)
+    nr = math.sqrt(math.fsum(r * r))
     import scipy.sparse as sp
-    r = b - A @ x
-    fro = sp.linalg.norm(A, "fro") if sp.issparse(A) else np.linalg.norm(A)
-    nr = np.linalg.norm(r)
-    return float(np.linalg.norm(A.T @ r) / (fro * nr)) if nr > 0 else 0.0
+    fro = math.sqrt(math.fsum(A.data * A.data)) if sp.issparse(A) else float(np.linalg.norm(A))
+    be = float(np.linalg.norm(A.T @ r) / (fro * nr)) if nr > 0 else 0.0
+    return {"residual_norm": nr, "backward_error": be}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def oracle_once_child(args):
+    """--oracle-once: one oracle solve of the workload saved by the parent (run
+    with the BLAS thread count the parent set in the environment)."""
+    z = np.load(args.oracle_once, allow_pickle=False)
+    if z["kind"] == "sparse":
+        import scipy.sparse as sp
+        A = sp.csc_matrix((z["data"], z["indices"], z["indptr"]), shape=tuple(z["shape"]))
+    else:
+        A = np.asfortranarray(z["A"])
+    t0 = time.perf_counter()
+    out = oracle_solve(str(z["kind"]), A, z["b"], float(z["gamma"]), int(z["k"]))
+    print(json.dumps({"value": time.perf_counter() - t0, "phases_s": out["phases_s"],
+                      "it": int(out["it"]), "rank": int(out["rank"])}), flush=True)
+
+
+def cpu_baseline_run(kind, name, A, b, gamma, k):
+    """The CPU oracle on the host cores: one solve with BLAS on all cores (the
+    reported value), then one with BLAS on one thread (in a child process,
+    skipped when the all-cores solve took over 30 s).  Per-phase times."""
+    t0 = time.perf_counter()
+    out = oracle_solve(kind, A, b, gamma, k)
+    t_all = time.perf_counter() - t0
+    one = None
+    if t_all < 30.0:
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "w.npz")
+            if kind == "sparse":
+                np.savez(path, kind=kind, gamma=gamma, k=k, b=b, indptr=A.indptr,
+                         indices=A.indices, data=A.data, shape=np.array(A.shape))
+            else:
+                np.savez(path, kind=kind, gamma=gamma, k=k, b=b, A=A)
+            env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+            try:
+                p = subprocess.run([sys.executable, os.path.abspath(__file__), "--oracle-once",
+                                    path, "--workload", name], env=env, capture_output=True,
+                                   text=True, timeout=300)
+                one = json.loads(p.stdout.strip().splitlines()[-1]) if p.returncode == 0 else \
+                    {"error": p.stderr[-300:]}
+            except (subprocess.SubprocessError, ValueError, IndexError) as e:
+                one = {"error": str(e)[:300]}
+    cpu = {"value": t_all, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+           "cpu_model": cpu_model(),
+           "sample": "one full solve of the workload by the CPU oracle (restatement of the "
+                     "reference algorithm: C loops single-threaded as the reference's "
+                     "MAX_NUM_THREADS = 1, LAPACK dgeqp3/dormqr/dtrcon through numpy's "
+                     "OpenBLAS on all cores; SPQR replaced by dense CPQR of the sketch)",
+           "phases_s": out["phases_s"], "it": int(out["it"]), "rank": int(out["rank"]),
+           "blas_one_thread": one}
+    return cpu, out
 
 
 # ---------------------------------------------------------- reference arm --
@@ -190,7 +274,7 @@ def run_reference(args, rank):
         return
     w, A, b, _ = make_workload(args.workload)
     warm = min(args.warmup, 1)
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, min(args.steps, 5))
     for _ in range(warm):
         oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
     times = []
@@ -199,7 +283,7 @@ def run_reference(args, rank):
         t0 = time.perf_counter()
         out = oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
         times.append(time.perf_counter() - t0)
-    v = statistics.mean(times)
+    v = statistics.median(times)
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
@@ -210,16 +294,148 @@ def run_reference(args, rank):
                    "nnz": int(getattr(A, "nnz", A.size)), "gamma": w["gamma"], "k": w["k"],
                    "it_tol": IT_TOL},
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": "full solve of the workload per step; CPU oracle "
-                                   "(restatement of the reference algorithm: C loops single "
-                                   "thread as the reference's MAX_NUM_THREADS=1, LAPACK dgeqp3/"
-                                   "dormqr/dtrcon via numpy's OpenBLAS on all cores; SPQR "
-                                   "replaced by dense CPQR of the sketch)"},
+                         "cpu_model": cpu_model(),
+                         "sample": "full solve of the workload per step, median of the timed "
+                                   "steps; CPU oracle (restatement of the reference algorithm: "
+                                   "C loops single-threaded as the reference's "
+                                   "MAX_NUM_THREADS = 1, LAPACK dgeqp3/dormqr/dtrcon through "
+                                   "numpy's OpenBLAS on all cores; SPQR replaced by dense CPQR "
+                                   "of the sketch)"},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "solve": {"rank": int(out["rank"]), "it": int(out["it"]), "flag": int(out["flag"]),
-                  "backward_error": backward_error(A, out["x"], b)},
+                  "phases_s": out["phases_s"], "step_s": times,
+                  **exact_quality(A, out["x"], b)},
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------ problem on device --
+class SparseOnDevice:
+    kind = "sparse"
+
+    def __init__(self, A, b, dev, torch):
+        self.A, self.b = A, b
+        self.n, self.d = A.shape
+        self.nnz = int(A.nnz)
+        self.Ap = torch.from_numpy(A.indptr.astype(np.int64)).to(dev)
+        self.Ai = torch.from_numpy(A.indices.astype(np.int64)).to(dev)
+        self.Ax = torch.from_numpy(A.data.astype(np.float64)).to(dev)
+        self.bd = torch.from_numpy(b.astype(np.float64)).to(dev)
+        self.xd = torch.zeros(self.d, dtype=torch.float64, device=dev)
+
+    def solve(self, skl, precision, profile, stream, device, gamma, k):
+        return skl.sparse_solve_device(self.n, self.d, self.Ap.data_ptr(), self.Ai.data_ptr(),
+                                       self.Ax.data_ptr(), self.bd.data_ptr(), self.xd.data_ptr(),
+                                       self.nnz, gamma, k, precision=precision, seed=1,
+                                       it_tol=IT_TOL, stream=stream, profile=profile,
+                                       device=device)
+
+    def host_solver(self, skl, torch, opts):
+        """Returns (call, x_host, h2d, d2h): call() runs skl_sparse_solve on
+        pinned host buffers."""
+        import ctypes
+        A = self.A
+        hp = torch.from_numpy(A.indptr.astype(np.int64)).pin_memory()
+        hi = torch.from_numpy(A.indices.astype(np.int64)).pin_memory()
+        hx = torch.from_numpy(A.data.astype(np.float64)).pin_memory()
+        hb = torch.from_numpy(self.b.astype(np.float64)).pin_memory()
+        hxo = torch.zeros(self.d, dtype=torch.float64).pin_memory()
+        csc = skl.SklCsc(self.n, self.d, self.nnz, hp.data_ptr(), hi.data_ptr(), hx.data_ptr())
+        keep = (hp, hi, hx, hb, hxo, csc)
+
+        def call():
+            info = skl.SklInfo()
+            rc = skl.lib().skl_sparse_solve(ctypes.byref(keep[5]), ctypes.c_void_p(hb.data_ptr()),
+                                            ctypes.c_void_p(hxo.data_ptr()), ctypes.byref(opts),
+                                            ctypes.byref(info))
+            if rc != 0:
+                raise RuntimeError(skl.last_error())
+            return info
+        return call, hxo, 8 * (self.d + 1) + 16 * self.nnz + 8 * self.n, 8 * self.d
+
+    def product_bytes(self, r):
+        n, d, nnz = self.n, self.d, self.nnz
+        return {
+            # CSR: column index 4 B + (hi, lo) value 8 B per nnz, row pointers,
+            # z gather (d pairs), u read + write
+            "lsqr_spmv_csr_Az": 12 * nnz + 4 * (n + 1) + 8 * d + 16 * n,
+            # CSC over all columns: row index + value, u reads counted once, t write
+            "lsqr_spmv_csc_ATu": 12 * nnz + 4 * (d + 1) + 8 * n + 8 * r,
+            "lsqr_trmv_Mv": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+            "lsqr_trmv_MTt": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+        }
+
+    def config(self):
+        return {"n": self.n, "d": self.d, "nnz": self.nnz,
+                "l2": "inputs larger than L2 (CSC + CSR copies and the m x d sketch exceed "
+                      "129 MB at the benchmark sizes) and a 256 MB buffer written between steps"}
+
+
+class DenseOnDevice:
+    kind = "dense"
+
+    def __init__(self, A, b, dev, torch):
+        self.A, self.b = A, b
+        self.n, self.d = A.shape
+        self.Ad = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).to(dev)
+        self.bd = torch.from_numpy(b.astype(np.float64)).to(dev)
+        self.xd = torch.zeros(self.d, dtype=torch.float64, device=dev)
+
+    def solve(self, skl, precision, profile, stream, device, gamma, k):
+        return skl.dense_solve_device(self.n, self.d, self.Ad.data_ptr(), self.n,
+                                      self.bd.data_ptr(), self.xd.data_ptr(), gamma, k,
+                                      precision=precision, seed=1, it_tol=IT_TOL, stream=stream,
+                                      profile=profile, device=device)
+
+    def host_solver(self, skl, torch, opts):
+        import ctypes
+        hA = torch.from_numpy(np.asfortranarray(self.A).ravel(order="F")).pin_memory()
+        hb = torch.from_numpy(self.b.astype(np.float64)).pin_memory()
+        hxo = torch.zeros(self.d, dtype=torch.float64).pin_memory()
+        n, d = self.n, self.d
+
+        def call():
+            info = skl.SklInfo()
+            rc = skl.lib().skl_dense_solve(ctypes.c_void_p(hA.data_ptr()), n, n, d,
+                                           ctypes.c_void_p(hb.data_ptr()),
+                                           ctypes.c_void_p(hxo.data_ptr()), ctypes.byref(opts),
+                                           ctypes.byref(info))
+            if rc != 0:
+                raise RuntimeError(skl.last_error())
+            return info
+        call.keep = (hA, hb)
+        return call, hxo, 8 * n * d + 8 * n, 8 * d
+
+    def product_bytes(self, r):
+        n, d = self.n, self.d
+        return {
+            # the r selected columns of the (hi, lo) copy of A, z, u read + write
+            "lsqr_gemv_dense_Az": 8 * n * r + 8 * r + 16 * n,
+            "lsqr_gemv_dense_ATu": 8 * n * r + 8 * n + 8 * r,
+            "lsqr_trmv_Mv": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+            "lsqr_trmv_MTt": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
+        }
+
+    def config(self):
+        return {"n": self.n, "d": self.d,
+                "l2": "inputs larger than L2 (A 1.28 GB FP64 plus its float-pair copy) and a "
+                      "256 MB buffer written between steps"}
+
+
+def profile_one(args):
+    """--profile-one: ONE solve of the workload on device-resident inputs with
+    the library's per-kernel events on, no warm-up: a short, fixed command for
+    ncu captures and per-phase timing."""
+    import torch
+    import skills_gb300 as skl
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    w, A, b, _ = make_workload(args.workload)
+    P = (SparseOnDevice if w["kind"] == "sparse" else DenseOnDevice)(A, b, dev, torch)
+    info = None
+    for _ in range(max(1, args.repeats)):
+        info = P.solve(skl, args.precision, 1, None, 0, w["gamma"], w["k"])
+    print(json.dumps(info.as_dict()), flush=True)
 
 
 # ---------------------------------------------------------------- our arm --
@@ -234,32 +450,17 @@ def run_ours(args, rank, world):
     barrier = ranks.barrier
 
     w, A, b, gen_s = make_workload(args.workload)
-    if w["kind"] != "sparse":
-        raise SystemExit("dense workloads: use the dense bench mode")
-    A = A.tocsc()
-    n, d = A.shape
-    nnz = int(A.nnz)
     gamma, k = w["gamma"], w["k"]
     hbm_peak, _, peak_kind = load_peaks()
-
-    Ap = torch.from_numpy(A.indptr.astype(np.int64)).to(dev)
-    Ai = torch.from_numpy(A.indices.astype(np.int64)).to(dev)
-    Ax = torch.from_numpy(A.data.astype(np.float64)).to(dev)
-    bd = torch.from_numpy(b.astype(np.float64)).to(dev)
-    xd = torch.zeros(d, dtype=torch.float64, device=dev)
+    P = (SparseOnDevice if w["kind"] == "sparse" else DenseOnDevice)(A, b, dev, torch)
+    n, d = P.n, P.d
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.Stream(device=dev)
-
-    def solve(precision, profile):
-        return skl.sparse_solve_device(n, d, Ap.data_ptr(), Ai.data_ptr(), Ax.data_ptr(),
-                                       bd.data_ptr(), xd.data_ptr(), nnz, gamma, k,
-                                       precision=precision, seed=1, it_tol=IT_TOL,
-                                       stream=stream.cuda_stream, profile=profile, device=local)
 
     def timed(precision, steps, warmup, profile):
         with torch.cuda.stream(stream):
             for _ in range(warmup):
-                solve(precision, profile)
+                P.solve(skl, precision, profile, stream.cuda_stream, local, gamma, k)
             torch.cuda.synchronize()
             barrier()
             torch.cuda.synchronize()
@@ -271,7 +472,7 @@ def run_ours(args, rank, world):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                infos.append(solve(precision, profile))
+                infos.append(P.solve(skl, precision, profile, stream.cuda_stream, local, gamma, k))
                 e1.record(stream)
                 evs.append((e0, e1))
             torch.cuda.synchronize()
@@ -288,51 +489,43 @@ def run_ours(args, rank, world):
     # (event records between launches cost a few ms per solve, so the value
     # above is timed without them); the kernel roofline uses these events
     _, infos, _ = timed("mixed", args.steps, 1, 1)
-    x_mixed = xd.cpu().numpy()
+    x_mixed = P.xd.cpu().numpy()
     step_s = ranks.max(statistics.mean(ms) / 1e3)
     last = infos[-1]
 
+    def phases(i):
+        return {"setup": i.t_setup_ms, "sketch": i.t_sketch_ms, "qr": i.t_qr_ms,
+                "precond": i.t_precond_ms, "lsqr": i.t_lsqr_ms, "host_hash": i.t_host_hash_ms}
+
     fp64 = None
+    x64 = None
     if not args.no_fp64:
         ms64, inf64, _ = timed("fp64", max(1, min(args.steps, 3)), 1, 0)
-        x64 = xd.cpu().numpy()
+        x64 = P.xd.cpu().numpy()
         fp64 = {"value": statistics.mean(ms64) / 1e3, "unit": "s",
                 "mixed_speedup": statistics.mean(ms64) / statistics.mean(ms),
-                "backward_error": backward_error(A, x64, b), "it": int(inf64[-1].it),
-                "rank": int(inf64[-1].rank),
-                "phases_ms": {"setup": inf64[-1].t_setup_ms, "sketch": inf64[-1].t_sketch_ms,
-                              "qr": inf64[-1].t_qr_ms, "precond": inf64[-1].t_precond_ms,
-                              "lsqr": inf64[-1].t_lsqr_ms}}
+                "it": int(inf64[-1].it), "rank": int(inf64[-1].rank),
+                "phases_ms": phases(inf64[-1])}
 
-    # ---- roofline of the LSQR products from the live events of the timed steps
-    r = int(last.rank)
+    # ---- per-kernel live event times -> achieved bandwidth
+    r = int(last.rank) + int(last.unresolved_cols)
     prof_ms = np.sum([np.array(list(i.prof_ms)) for i in infos], axis=0)
     prof_n = np.sum([np.array(list(i.prof_launches)) for i in infos], axis=0)
-    nnz_sel = nnz   # all columns are read by A*z (dropped columns carry z = 0)
-    alg_bytes = {
-        # CSR: col idx 4 B + (hi,lo) value 8 B per nnz, row ptr, z gather (d pairs),
-        # u read + u write + split write
-        "lsqr_spmv_csr_Az": 12 * nnz + 4 * (n + 1) + 8 * d + 24 * n,
-        # CSC over the r kept columns: row idx + value, u split reads counted once
-        "lsqr_spmv_csc_ATu": 12 * nnz_sel + 4 * (d + 1) + 8 * n + 8 * r,
-        "lsqr_trmv_Mv": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
-        "lsqr_trmv_MTt": 4 * r * (r + 1) // 2 + 8 * r + 16 * r,
-    }
     kernels = {}
-    for q, name in enumerate(alg_bytes):
+    for q, (name, nbytes) in enumerate(P.product_bytes(r).items()):
         if prof_n[q] > 0:
             per = prof_ms[q] / prof_n[q]
-            ach = alg_bytes[name] / (per * 1e-3) / 1e9
+            ach = nbytes / (per * 1e-3) / 1e9
             kernels[name] = {"launches": int(prof_n[q]), "ms_per_launch": per,
-                             "total_ms": float(prof_ms[q]), "alg_bytes": int(alg_bytes[name]),
+                             "total_ms": float(prof_ms[q]), "alg_bytes": int(nbytes),
                              "achieved_gbs": ach, "frac": ach / hbm_peak}
     # the sample QRP (k_yqrp, one launch per panel but the last): live event
     # time per launch from the QR sub-step events; algorithmic bytes = one read
-    # of the (nb+16) x (d-j) FP32 sample block per launch (plan for this
-    # workload: nb = 64, sample rows 80, 78 launches)
+    # of the (nb+16) x (d-j) FP32 sample block per launch (nb = 64)
     nb, nbp = 64, 80
-    mn = min(int(last.sketch_rows), d)
-    yq_js = [j for j in range(0, mn, nb) if j + nb < int(last.sketch_rows) and j + nb < d]
+    mrows = int(last.sketch_rows)
+    mn = min(mrows, d)
+    yq_js = [j for j in range(0, mn, nb) if j + nb < mrows and j + nb < d]
     if yq_js:
         yq_ms = float(np.sum([i.qr_prof_ms[0] for i in infos]))
         yq_n = len(yq_js) * len(infos)
@@ -342,7 +535,16 @@ def run_ours(args, rank, world):
         kernels["k_yqrp"] = {"launches": yq_n, "ms_per_launch": per, "total_ms": yq_ms,
                              "alg_bytes": yq_bytes, "achieved_gbs": ach, "frac": ach / hbm_peak,
                              "note": "latency-bound: 64 dependent pivot steps per launch, each a "
-                                     "16-CTA cluster barrier and one DSMEM round trip"}
+                                     "16-CTA cluster barrier"}
+    if P.kind == "dense":
+        # DHT + hash: read A once (FP64), write the m x d FP32 sketch
+        sk_ms = float(np.sum([i.t_sketch_ms for i in infos]))
+        sk_bytes = 8 * n * d + 4 * mrows * d
+        per = sk_ms / len(infos)
+        ach = sk_bytes / (per * 1e-3) / 1e9
+        kernels["k_dht_hash"] = {"launches": len(infos), "ms_per_launch": per,
+                                 "total_ms": sk_ms, "alg_bytes": sk_bytes, "achieved_gbs": ach,
+                                 "frac": ach / hbm_peak}
     dom = max(kernels, key=lambda kk: kernels[kk]["total_ms"]) if kernels else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -358,63 +560,56 @@ def run_ours(args, rank, world):
         if "note" in kk:
             roofline["note"] = kk["note"]
 
-    # ---- e2e through the host-pointer C ABI (pinned host buffers)
+    # ---- e2e through the host-pointer C ABI (pinned host buffers, copies timed)
     e2e = None
     if not args.no_e2e:
-        hp = torch.from_numpy(A.indptr.astype(np.int64)).pin_memory()
-        hi = torch.from_numpy(A.indices.astype(np.int64)).pin_memory()
-        hx = torch.from_numpy(A.data.astype(np.float64)).pin_memory()
-        hb = torch.from_numpy(b.astype(np.float64)).pin_memory()
-        hxo = torch.zeros(d, dtype=torch.float64).pin_memory()
-        import ctypes
-        csc = skl.SklCsc(n, d, nnz, hp.data_ptr(), hi.data_ptr(), hx.data_ptr())
         o = skl.default_opts()
         o.gamma, o.k, o.it_tol, o.seed_mode, o.seed, o.device = gamma, k, IT_TOL, 1, 1, local
         o.stream = stream.cuda_stream
+        call, hxo, h2d, d2h = P.host_solver(skl, torch, o)
         times = []
         for q in range(max(3, args.warmup) + args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            info = skl.SklInfo()
-            rc = skl.lib().skl_sparse_solve(ctypes.byref(csc), ctypes.c_void_p(hb.data_ptr()),
-                                            ctypes.c_void_p(hxo.data_ptr()), ctypes.byref(o),
-                                            ctypes.byref(info))
-            if rc != 0:
-                raise RuntimeError(skl.last_error())
+            call()
             t = time.perf_counter() - t0
             if q >= max(3, args.warmup):
                 times.append(t)
         e2e = {"value": ranks.max(statistics.mean(times)), "unit": "s",
-               "h2d_bytes_per_step": int(8 * (d + 1) + 16 * nnz + 8 * n),
-               "d2h_bytes_per_step": int(8 * d),
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "x_matches_device_path": bool(np.array_equal(hxo.numpy(), x_mixed))}
 
     cpu = None
-    be_oracle = None
+    oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t0 = time.perf_counter()
-        out = oracle_solve("sparse", A, b, gamma, k)
-        tcpu = time.perf_counter() - t0
-        be_oracle = backward_error(A, out["x"], b)
-        cpu = {"value": tcpu, "unit": "s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full solve of the workload by the CPU oracle (C loops single "
-                         "thread, LAPACK via numpy OpenBLAS on all cores)",
-               "backward_error": be_oracle, "it": int(out["it"]), "rank": int(out["rank"]),
-               "x_rel_diff_gpu_vs_oracle": float(np.linalg.norm(x_mixed - out["x"]) /
-                                                 np.linalg.norm(out["x"]))}
+        cpu, oracle = cpu_baseline_run(P.kind, args.workload, A, b, gamma, k)
 
     if rank != 0:
         return
+    quality = {"mixed": exact_quality(A, x_mixed, b)}
+    if x64 is not None:
+        quality["fp64"] = exact_quality(A, x64, b)
+    if oracle is not None:
+        quality["oracle"] = exact_quality(A, oracle["x"], b)
+        quality["oracle"]["rank"] = int(oracle["rank"])
+        quality["x_rel_diff_mixed_vs_oracle"] = float(
+            np.linalg.norm(x_mixed - oracle["x"]) / np.linalg.norm(oracle["x"]))
+        rn0 = quality["oracle"]["residual_norm"]
+        for key in ("mixed", "fp64"):
+            if key in quality and rn0 > 0:
+                quality[key]["residual_rel_excess_vs_oracle"] = \
+                    (quality[key]["residual_norm"] - rn0) / rn0
     line = {
         "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": step_s * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": args.workload, "n": n, "d": d, "nnz": nnz, "gamma": gamma, "k": k,
-                   "sketch_rows": int(last.sketch_rows), "it_tol": IT_TOL,
-                   "precision": "mixed (FP32 sketch/QR/R^-1, float-float LSQR products, FP64 "
-                                "recurrences)",
-                   "l2": "inputs larger than L2 (CSC+CSR 145 MB, sketch 170 MB) and a 256 MB "
-                         "buffer written between steps", "parallelism": "replicas"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+ff+f64", "data": "synthetic",
+        "config": {"workload": args.workload, **P.config(), "gamma": gamma, "k": k,
+                   "sketch_rows": mrows, "it_tol": IT_TOL,
+                   "precision": "mixed: FP32 sketch, QR and R^-1; LSQR products in float-float "
+                                "(FP32 pairs, ~2^-48 relative) over (hi, lo) pairs of A's values "
+                                "(48 of 53 bits); FP64 recurrences, norms, solution assembly "
+                                "and residual",
+                   "parallelism": "replicas"},
         "e2e": e2e,
         "gpu_launches": int(sum(i.kernel_launches for i in infos0)),
         "roofline": roofline,
@@ -422,14 +617,16 @@ def run_ours(args, rank, world):
         "cpu_baseline": cpu,
         "clocks": clk,
         "fp64_path": fp64,
-        "solve": {"rank": int(last.rank), "it": int(last.it), "flag": int(last.flag),
-                  "success": int(last.success), "rcond_r11": last.rcond_r11,
-                  "backward_error": backward_error(A, x_mixed, b),
-                  "backward_error_oracle": be_oracle,
+        "solve": {"rank": int(last.rank), "unresolved_cols": int(last.unresolved_cols),
+                  "it": int(last.it), "flag": int(last.flag), "success": int(last.success),
+                  "rcond_r11": last.rcond_r11, "fp64_fallback": int(last.fp64_fallback),
                   "explicit_residual": last.explicit_residual,
-                  "phases_ms": {"setup": last.t_setup_ms, "sketch": last.t_sketch_ms,
-                                "qr": last.t_qr_ms, "precond": last.t_precond_ms,
-                                "lsqr": last.t_lsqr_ms, "host_hash": last.t_host_hash_ms},
+                  "sketch_refine_steps": int(last.sketch_refine_steps),
+                  "quality_exact": quality,
+                  "phases_ms": phases(last),
+                  "qr_substeps_ms": {nm: float(v) for nm, v in zip(
+                      ("sample_qrp", "moves", "panel", "qtc", "W", "Z", "update", "downdate",
+                       "sample0"), last.qr_prof_ms)},
                   "step_ms": ms, "wall_s": wall, "workload_gen_s": gen_s},
     }
     print(json.dumps(line), flush=True)
@@ -472,7 +669,7 @@ def run_batched(args, rank, world):
         same = same and np.array_equal(r.x, xs[p])
     loop_s = ranks.max(time.perf_counter() - t0)
     same = ranks.sum(0 if same else 1) == 0
-    be = [backward_error(A, xs[p], b) for p, (A, b) in enumerate(probs[:32])]
+    be = [exact_quality(A, xs[p], b)["backward_error"] for p, (A, b) in enumerate(probs)]
     if rank != 0:
         return
     best = min(batched_s)
@@ -494,7 +691,8 @@ def run_batched(args, rank, world):
                                   "batched_speedup": loop_s / best,
                                   "x_bit_identical": bool(same)},
         "status_ok": int(sum(1 for s_ in status if s_ == 0)),
-        "max_backward_error_first32": float(max(be)),
+        "backward_error": {"max": float(max(be)), "median": float(statistics.median(be)),
+                           "over": len(be), "evaluation": "correctly rounded residual"},
         "gpu_launches": int(sum(i.kernel_launches for i in infos)),
         "step_s": batched_s, "workload_gen_s": gen_s,
     }
@@ -505,6 +703,12 @@ def main():
     args = parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.oracle_once:
+        oracle_once_child(args)
+        return
+    if args.profile_one:
+        profile_one(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank)
         return

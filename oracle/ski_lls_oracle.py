@@ -34,6 +34,7 @@ import ctypes
 import math
 import os
 import subprocess
+import time
 
 import numpy as np
 import scipy.linalg.lapack as lapack
@@ -256,9 +257,11 @@ def ls_sparse_spqr(n, d, indptr, indices, data, b, gamma, k, abs_tol=1e-8, it_to
         raise RuntimeError("Matrix is not overdetermined.")
     if rng is None:
         rng = Rng(1)
+    t0 = time.perf_counter()
     m = int(math.ceil(d * gamma))
     rows, vals = gen_hashing(rng, m, n, k)
     SA, Sb = sparse_sketch(n, d, indptr, indices, data, b, m, k, rows, vals)
+    t1 = time.perf_counter()
     qr, E, tau = _cpqr(SA)
     c = _apply_qt(qr, tau, Sb)
     diag = np.abs(np.diag(qr))
@@ -277,8 +280,10 @@ def ls_sparse_spqr(n, d, indptr, indices, data, b, gamma, k, abs_tol=1e-8, it_to
     x[E[:rank]] = cs
     r_s = csc_residual(n, d, indptr, indices, data, x, b)
     res = float(np.linalg.norm(r_s))
+    t2 = time.perf_counter()
     out = dict(m=m, rank=rank, success=success, rcond=float(rcond), E=E, rows=rows, vals=vals,
-               SA=SA, Sb=Sb, tol=tol, explicit_residual=res)
+               SA=SA, Sb=Sb, tol=tol, explicit_residual=res,
+               phases_s=dict(sketch=t1 - t0, qr=t2 - t1, lsqr=0.0))
     if res < abs_tol:
         out.update(x=x, flag=0, it=0)
         return out
@@ -289,6 +294,7 @@ def ls_sparse_spqr(n, d, indptr, indices, data, b, gamma, k, abs_tol=1e-8, it_to
     y = usolve(R11, y, 1, perturb) + cs
     x = np.zeros(d)
     x[E[:rank]] = y
+    out["phases_s"]["lsqr"] = time.perf_counter() - t2
     out.update(x=x, flag=flag, it=it)
     return out
 
@@ -304,6 +310,7 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     n, d = A.shape
     if n < d:
         raise RuntimeError("Matrix is not overdetermined.")
+    t0 = time.perf_counter()
     m = int(math.ceil(d * gamma))
     N = n if N is None else N
     rng = Rng(seed)
@@ -313,6 +320,8 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     rows, vals = gen_hashing(rng, m, N, k)
     SA = dense_sketch(Y, m, k, rows, vals)
     Sb = dense_sketch(yb[:, None], m, k, rows, vals)[:, 0]
+    del Y
+    t1 = time.perf_counter()
     qr, E, tau = _cpqr(SA.copy(order="F"))
     c = _apply_qt(qr, tau, Sb)
     rank = 0
@@ -324,8 +333,9 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     x[E[:rank]] = cs
     rs = np.asarray(b, dtype=np.float64) - A @ x
     res = float(np.linalg.norm(rs))
+    t2 = time.perf_counter()
     out = dict(m=m, rank=rank, E=E, D=D, rows=rows, vals=vals, SA=SA, Sb=Sb,
-               explicit_residual=res)
+               explicit_residual=res, phases_s=dict(sketch=t1 - t0, qr=t2 - t1, lsqr=0.0))
     if res < abs_tol:
         out.update(x=x, flag=0, it=0)
         return out
@@ -335,6 +345,7 @@ def ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=1e-8, rcond=1e-10, it_to
     x = np.zeros(d)
     x[E[:rank]] = y
     x = xs + x
+    out["phases_s"]["lsqr"] = time.perf_counter() - t2
     out.update(x=x, flag=flag, it=it)
     return out
 

@@ -4,8 +4,9 @@
   40,000 x 4,000 dense, kappa = 1e6     x to 1e-8 of a dense FP64 Householder QR solve,
                                          backward error <= 1e-10
   120,000 x 5,000 sparse, column scales 10^U[0,8], 50 dependent columns
-                                         ||b - A x|| (correctly rounded) within 1e-6
-                                         relative of the oracle's, same rank
+                                         ||b - A x|| (correctly rounded) within 5e-5
+                                         relative of the oracle's (the FP64 floor of
+                                         this problem, see RES_REL_TOL), same rank
   120,000 x 5,000 sparse, unscaled, full rank
                                          x to 1e-8 of the oracle
   1,000,000 x 10,000 sparse, Zipf columns (s = 3)
@@ -49,12 +50,26 @@ def illcond():
     return A, b, ref, accurate.residual_norm(A, ref["x"], b), accurate.backward_error(A, ref["x"], b)
 
 
+# ||b - A x|| on this configuration is fixed only to ~1e-4 by any FP64 x:
+#  * a random 1-ulp perturbation of the oracle's own x raises it by 1.8e-4
+#    relative (and its backward error from 3.4e-4 to 1.2e-3);
+#  * the 50 planted combinations a A_p + c A_q are formed in FP64 with column
+#    scales up to 1e8, so they are independent at the rounding level (~3e-7,
+#    against 1e-6 noise), and which of {j, p, q} a pivoting rule drops moves
+#    the minimum: reordering A's columns moves the oracle's by 4e-6, and the
+#    oracle on x86 and aarch64 (different LAPACK pivot tie-breaks) differ by
+#    2.7e-5.
+# The tolerance sits 4x under the 1-ulp floor.  The solution assembly that
+# recomputed D P1 M (c + y) in one product was 1.7e-3 above the minimum.
+RES_REL_TOL = 5e-5
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_illcond_120000x5000_residual_parity(illcond, precision):
     A, b, ref, rn_ref, be_ref = illcond
     res = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=1e-10, seed=1, precision=precision)
     rn = accurate.residual_norm(A, res.x, b)
-    assert abs(rn - rn_ref) <= 1e-6 * rn_ref, (precision, rn, rn_ref)
+    assert abs(rn - rn_ref) <= RES_REL_TOL * rn_ref, (precision, rn, rn_ref)
     assert res.rank == ref["rank"] == 4950
     # the backward error's floor here is the rounding of x to FP64 (~3e-4 for
     # the oracle, ~6e-4 after a 1-ulp perturbation of its x)
