@@ -24,6 +24,8 @@
  *                                                        src/IterSolver.cpp:89,95
  *   skl_csc_mv        <- csc_mv 'n' / 't' (CSC_Mat::mv)  src/SpMat.cpp:37-74,
  *                                                        include/SpMat.hpp:132-136
+ *   skl_gemm_vta      <- the W = C^T V product of dlarfb in NoFLA_Apply_Q_WY_lhfc_blk_var4
+ *                        hqrrp/lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4_skint.c:721-746
  */
 #ifndef SKILLS_GB300_H
 #define SKILLS_GB300_H
@@ -258,6 +260,15 @@ skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, in
  * <= 2^-45 of sum_j |a_ij x_j|); on the FP64 path plain FP64.  Replaces the
  * reference's csc_mv (src/SpMat.cpp:37-74) for checking the operator. */
 skl_status skl_csc_mv(const skl_csc* A, char trans, const double* x, double* y, int precision);
+
+/* W (b x N, column-major, ld b) = V^T A in FP32 for V (M x b, ldv, b <= 64)
+ * and A (M x N, lda), host buffers: the product the randomized CPQR forms
+ * for every panel's block reflector.  tensor = 1: the tcgen05 kernel (3xTF32
+ * on the tensor cores, TMA-fed, accumulator in tensor memory); tensor = 0:
+ * the CUDA-core FP32 kernel.  Each entry is within ~2^-20 of
+ * sum_k |v_kc a_kn| of the exact product. */
+skl_status skl_gemm_vta(int64_t M, int64_t N, int64_t b, const float* V, int64_t ldv,
+                        const float* A, int64_t lda, float* W, int tensor);
 
 /* Release all device memory and streams held by the library. */
 void skl_finalize(void);

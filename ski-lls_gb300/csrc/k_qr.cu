@@ -930,6 +930,8 @@ struct QrBuffers {
     int* tmpI;    // 2 nb pivot indices being moved
     T *cg, *cr1, *cx1, *cw;   // CholeskyQR2 panel: Gram, R1, R1^{-1}, R2^{-1} U^{-1}
     double *qw;
+    float* tcs;   // tensor-core W = V^T A: split V and split-K partials (FP32 path)
+    size_t tcs_floats;
     int64_t part_cap, part2_cap, tmp_rows;   // part2: split-K partials of the side stream
 };
 
@@ -973,6 +975,8 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.cx1 = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.cw = (T*)take((size_t)p.nb * p.nb * sizeof(T));
     B.qw = (double*)take(kMaxNb * sizeof(double));
+    B.tcs_floats = std::is_same<T, float>::value ? tc_vta_scratch_floats(m) : 0;
+    B.tcs = (float*)take(B.tcs_floats * sizeof(float));
     if (total) *total = off;
     return B;
 }
@@ -1205,8 +1209,14 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         if (N2 > 0) {
             // W = V^T A_trail ; Z = T^T W
             cudaEvent_t t0 = tm.begin();
-            gemm<T>(true, false, b, N2, M, T(1), B.V, m, Atr, ld, T(0), B.W, b, B.part,
-                    B.part_cap, st);
+            if constexpr (std::is_same<T, float>::value) {
+                // tensor cores (tcgen05, 3xTF32): W is on the panel chain's critical path
+                vta_product(tc_qr_enabled(), M, N2, b, B.V, m, Atr, ld, B.W, B.tcs, B.tcs_floats,
+                            status, st);
+            } else {
+                gemm<T>(true, false, b, N2, M, T(1), B.V, m, Atr, ld, T(0), B.W, b, B.part,
+                        B.part_cap, st);
+            }
             tm.end(4, t0);
             t0 = tm.begin();
             gemm<T>(true, false, b, N2, b, T(1), B.Tm, nb, B.W, b, T(0), B.Z, b, nullptr, 0, st);

@@ -345,7 +345,11 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     // ---- randomized CPQR, c = Q^T S b ----
     cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1,
             o.profile ? info.qr_prof_ms : nullptr);
-    if (read_status(C, st) & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
+    {
+        const unsigned qs = read_status(C, st);
+        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+        if (qs & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
+    }
     trace_phase(st, "cpqr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank, inverse, condition ----
@@ -816,7 +820,11 @@ static bool dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
     SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
     cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cpqr_on ? cvec : nullptr,
             cpqr_on ? 1 : 0, o.profile ? info.qr_prof_ms : nullptr);
-    if (read_status(C, st) & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
+    {
+        const unsigned qs = read_status(C, st);
+        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+        if (qs & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
+    }
     trace_phase(st, "dense qr");
     SKL_CUDA(cudaEventRecord(ev[4], st));
     // ---- rank: leading |R_ii| > rcond (absolute, :79-89); noCPQR keeps all ----

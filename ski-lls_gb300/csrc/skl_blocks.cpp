@@ -114,6 +114,7 @@ static void cpqr_block(double* A, int64_t m, int64_t d, int64_t* jpvt, double* t
         unsigned stt = 0;
         SKL_CUDA(cudaMemcpyAsync(&stt, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
+        if (stt & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
         if (stt & 8u) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
     }
     from_device_as<T>(Ad, m, d, ld, A, m, st);
@@ -293,6 +294,36 @@ static void csc_mv_block(const skl_csc* A, char trans, const double* x, double* 
     SKL_CUDA(cudaStreamSynchronize(st));
 }
 
+// W = V^T A (FP32) through the CPQR's product for the block reflector:
+// tensor = 1 the tcgen05 3xTF32 kernel, 0 the CUDA-core FP32 kernel.
+static void gemm_vta_block(int64_t M, int64_t N, int64_t b, const float* V, int64_t ldv,
+                           const float* A, int64_t lda, float* W, int tensor)
+{
+    Context& C = context(0);
+    cudaStream_t st = C.stream;
+    const int64_t ldd = (M + 31) / 32 * 32;
+    const size_t scr = std::max(tc_vta_scratch_floats(M), (size_t)(b * N * 128));
+    Sizer S;
+    S.add<float>(ldd * b); S.add<float>(ldd * N); S.add<float>(b * N); S.add<float>((int64_t)scr);
+    C.arena.reserve(S.bytes());
+    C.arena.reset();
+    float* Vd = C.arena.alloc<float>(ldd * b);
+    float* Ad = C.arena.alloc<float>(ldd * N);
+    float* Wd = C.arena.alloc<float>(b * N);
+    float* sd = C.arena.alloc<float>((int64_t)scr);
+    SKL_CUDA(cudaMemcpy2DAsync(Vd, ldd * sizeof(float), V, ldv * sizeof(float), M * sizeof(float), b,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpy2DAsync(Ad, ldd * sizeof(float), A, lda * sizeof(float), M * sizeof(float), N,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+    vta_product(tensor != 0, (int)M, (int)N, (int)b, Vd, ldd, Ad, ldd, Wd, sd, scr, C.dev_status, st);
+    unsigned stt = 0;
+    SKL_CUDA(cudaMemcpyAsync(&stt, C.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaMemcpyAsync(W, Wd, b * N * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    if (stt & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+}
+
 }  // namespace skl
 
 using namespace skl;
@@ -329,6 +360,17 @@ skl_status skl_trsv_upper(const double* R, int64_t ld, int64_t r, char trans, in
         if (!R || !x || r <= 0 || ld < r) fail(SKL_ERR_INVALID, "skl_trsv_upper: bad argument");
         if (precision == SKL_PREC_FP64) trsv_block<double>(R, ld, r, trans, x);
         else trsv_block<float>(R, ld, r, trans, x);
+    });
+}
+
+skl_status skl_gemm_vta(int64_t M, int64_t N, int64_t b, const float* V, int64_t ldv,
+                        const float* A, int64_t lda, float* W, int tensor)
+{
+    return guard([&] {
+        if (!V || !A || !W || M <= 0 || N <= 0 || b <= 0 || b > 64 || ldv < M || lda < M ||
+            M > 0x7fffffff || N > 0x7fffffff)
+            fail(SKL_ERR_INVALID, "skl_gemm_vta: bad argument");
+        gemm_vta_block(M, N, b, V, ldv, A, lda, W, tensor);
     });
 }
 

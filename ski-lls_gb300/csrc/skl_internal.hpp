@@ -156,6 +156,23 @@ template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
           unsigned* status, cudaStream_t st, double* c, int pivoting, double* qr_prof = nullptr);
 
+// --------------------------------------------------------------- k_tc.cu --
+// Status bit of a tensor-core kernel whose bounded mbarrier wait gave up.
+constexpr unsigned kStatusTcTimeout = 64u;
+// W (b x N, ld b) = V^T A on the tensor cores (tcgen05, 3xTF32): V is M x b
+// (ldv, b <= 64), A is M x N (lda); both 16-byte aligned with ld*4 a multiple
+// of 16 bytes.  scratch holds tc_vta_scratch_floats(M) floats.
+size_t tc_vta_scratch_floats(int64_t M);
+void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, int64_t lda, float* W,
+            float* scratch, size_t scratch_floats, unsigned* status, cudaStream_t st);
+// The CPQR's FP32 products go to the tensor cores unless SKILLS_QR_TC=0.
+bool tc_qr_enabled();
+// W = V^T A by tc_vta (tensor = true) or the CUDA-core FP32 GEMM; the same
+// scratch serves both (split-K partials).
+void vta_product(bool tensor, int M, int N, int b, const float* V, int64_t ldv, const float* A,
+                 int64_t lda, float* W, float* scratch, size_t scratch_floats, unsigned* status,
+                 cudaStream_t st);
+
 // ----------------------------------------------------------- k_trinv.cu --
 // M = inv(R11 + perturb*I) for the r x r upper triangle of R (ld); M is r x r
 // (ldm), upper triangular, zeros below.  Also ||R11||_inf and ||M||_inf.

@@ -137,6 +137,8 @@ def lib():
         L.skl_trsv_upper.restype = ctypes.c_int
         L.skl_csc_mv.argtypes = [ctypes.POINTER(SklCsc), ctypes.c_char, vp, vp, ctypes.c_int]
         L.skl_csc_mv.restype = ctypes.c_int
+        L.skl_gemm_vta.argtypes = [i64, i64, i64, vp, i64, vp, i64, vp, ctypes.c_int]
+        L.skl_gemm_vta.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -383,6 +385,20 @@ def csc_mv(A, x, trans="n", precision="mixed"):
     csc = SklCsc(n, d, int(indptr[-1]), indptr.ctypes.data, indices.ctypes.data, data.ctypes.data)
     _check(lib().skl_csc_mv(ctypes.byref(csc), trans.encode(), _ptr(xx), _ptr(y), PREC[precision]))
     return y
+
+
+def gemm_vta(V, A, tensor=True):
+    """W = V^T A in FP32 through the CPQR's block-reflector product
+    (tensor=True: tcgen05 3xTF32 kernel; False: CUDA-core FP32 kernel)."""
+    V = np.asfortranarray(V, dtype=np.float32)
+    A = np.asfortranarray(A, dtype=np.float32)
+    M, b = V.shape
+    if A.shape[0] != M:
+        raise ValueError("V and A need the same number of rows")
+    N = A.shape[1]
+    W = np.zeros((b, N), dtype=np.float32, order="F")
+    _check(lib().skl_gemm_vta(M, N, b, _ptr(V), M, _ptr(A), M, _ptr(W), 1 if tensor else 0))
+    return W
 
 
 def dht_length(n, wisdom=0):
