@@ -224,7 +224,12 @@ skl_status skl_dht(const double* A, int64_t lda, int64_t n, int64_t d, const dou
  *    first call before any stream capture begins.
  *  - All calls on one device share that scratch: calls that may overlap in
  *    time (different streams or host threads without ordering between them)
- *    race on it and give wrong results.  Order them (one stream, or events). */
+ *    race on it and give wrong results.  Order them (one stream, or events).
+ *  - Footprint: with CUDA's default lazy module loading the array is
+ *    committed on a device when this entry point is first used there; with
+ *    CUDA_MODULE_LOADING=EAGER, on every device the process initialises.
+ *  - After cudaDeviceReset, call skl_finalize() before using it again (the
+ *    looked-up address belonged to the destroyed context). */
 #define SKL_DHT_NOALLOC_SCRATCH_BYTES (64u << 20)
 #define SKL_DHT_NOALLOC_MAX_N 4194304
 skl_status skl_dht_device_noalloc(const double* A, int64_t lda, int64_t n, int64_t d,

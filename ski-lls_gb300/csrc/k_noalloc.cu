@@ -10,8 +10,12 @@
 // the whole device) would stall every other stream.
 //
 // The scratch array lives in this translation unit alone, so with CUDA's lazy
-// module loading its memory is committed on a device only once this entry
-// point is used there.
+// module loading (the default) its memory is committed on a device only once
+// this entry point is used there; with CUDA_MODULE_LOADING=EAGER every device
+// the process initialises commits it when the library's module loads.
+// The device address is looked up once per device and kept; after
+// cudaDeviceReset call skl_finalize() (which forgets it) before using this
+// entry point again.
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -50,6 +54,14 @@ static void* scratch_for_current_device()
         g_scratch_ptr[dev] = p;
     }
     return g_scratch_ptr[dev];
+}
+
+// Forget the per-device addresses (skl_finalize): a device reset destroys
+// the context they belong to.
+void noalloc_forget_scratch()
+{
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    for (auto& p : g_scratch_ptr) p = nullptr;
 }
 
 template <typename T>

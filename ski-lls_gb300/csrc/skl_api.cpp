@@ -1074,6 +1074,10 @@ skl_status skl_dense_solve_device(const double* A, int64_t lda, int64_t n, int64
     return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, false); });
 }
 
-void skl_finalize(void) { release_all_contexts(); }
+void skl_finalize(void)
+{
+    release_all_contexts();
+    noalloc_forget_scratch();
+}
 
 }  // extern "C"

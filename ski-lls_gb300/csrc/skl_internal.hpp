@@ -84,6 +84,8 @@ Context& context(int device, int slot = 0);
 // Runs fn and converts exceptions into an skl_status (C ABI guard).
 skl_status run_guarded(void (*fn)(void*), void* arg);
 void release_all_contexts();
+// Forgets skl_dht_device_noalloc's per-device scratch addresses (k_noalloc.cu).
+void noalloc_forget_scratch();
 
 // ---------------------------------------------------------- k_format.cu --
 size_t scan_scratch_ints(int64_t n);

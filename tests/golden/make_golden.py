@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures from the reference's own test data.
 
-Run in a container where the reference source tree is mounted (default
-/root/reference, override with SKILLS_REF_DIR).  Produces:
+Run where the reference source tree is available, with SKILLS_REF_DIR set to
+its root.  Produces:
 
   fixtures.npz   the 12 full-rank matrices of data/*.mtx and the 12
                  rank-deficient matrices of data/rank_deficient_sparse_paper/
@@ -24,7 +24,9 @@ import scipy.io
 import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("SKILLS_REF_DIR", "/root/reference")
+REF = os.environ.get("SKILLS_REF_DIR")
+if not REF:
+    raise SystemExit("set SKILLS_REF_DIR to the reference source tree")
 
 FULL_RANK = ["50by15", "50by20", "100by15", "100by20", "120by15", "120by20"]
 # test/test_solvers.sh:138-141 (matrix order and expected residual of b = ones)
