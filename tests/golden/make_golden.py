@@ -25,8 +25,6 @@ import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("SKILLS_REF_DIR")
-if not REF:
-    raise SystemExit("set SKILLS_REF_DIR to the reference source tree")
 
 FULL_RANK = ["50by15", "50by20", "100by15", "100by20", "120by15", "120by20"]
 # test/test_solvers.sh:138-141 (matrix order and expected residual of b = ones)
@@ -124,6 +122,8 @@ def hashing():
 
 
 if __name__ == "__main__":
+    if not REF:
+        raise SystemExit("set SKILLS_REF_DIR to the reference source tree")
     fixtures()
     rand_glibc()
     hashing()
