@@ -26,6 +26,7 @@
  *                                                        include/SpMat.hpp:132-136
  *   skl_gemm_vta      <- the W = C^T V product of dlarfb in NoFLA_Apply_Q_WY_lhfc_blk_var4
  *                        hqrrp/lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4_skint.c:721-746
+ *   skl_gemm_update   <- the C -= V W^T product of the same dlarfb call
  */
 #ifndef SKILLS_GB300_H
 #define SKILLS_GB300_H
@@ -274,6 +275,14 @@ skl_status skl_csc_mv(const skl_csc* A, char trans, const double* x, double* y, 
  * sum_k |v_kc a_kn| of the exact product. */
 skl_status skl_gemm_vta(int64_t M, int64_t N, int64_t b, const float* V, int64_t ldv,
                         const float* A, int64_t lda, float* W, int tensor);
+
+/* C (M x N, ldc) rows r0..M-1 -= V Z in FP32, V (M x b, ldv, b <= 64), Z
+ * (b x N, ldz), r0 a multiple of 4, host buffers: the randomized CPQR's
+ * trailing update of every panel.  tensor = 1: the tcgen05 kernel (3xTF32,
+ * TMA loads and stores, accumulator in tensor memory); tensor = 0: the
+ * CUDA-core FP32 kernel. */
+skl_status skl_gemm_update(int64_t M, int64_t N, int64_t b, int64_t r0, const float* V, int64_t ldv,
+                           const float* Z, int64_t ldz, float* C, int64_t ldc, int tensor);
 
 /* Release all device memory and streams held by the library. */
 void skl_finalize(void);

@@ -932,6 +932,7 @@ struct QrBuffers {
     double *qw;
     float* tcs;   // tensor-core W = V^T A: split V and split-K partials (FP32 path)
     size_t tcs_floats;
+    float* tcu;   // tensor-core A -= V Z: split V and Z (FP32 path)
     int64_t part_cap, part2_cap, tmp_rows;   // part2: split-K partials of the side stream
 };
 
@@ -977,6 +978,8 @@ static QrBuffers<T> qr_carve(void* work, int64_t m, int64_t d, const QrPlan& p, 
     B.qw = (double*)take(kMaxNb * sizeof(double));
     B.tcs_floats = std::is_same<T, float>::value ? tc_vta_scratch_floats(m) : 0;
     B.tcs = (float*)take(B.tcs_floats * sizeof(float));
+    B.tcu = (float*)take((std::is_same<T, float>::value ? tc_update_scratch_floats(m, d) : 0) *
+                         sizeof(float));
     if (total) *total = off;
     return B;
 }
@@ -1256,8 +1259,16 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             // A_trail -= V Z (rows b.. when the first b went ahead)
             cudaEvent_t t0 = tm.begin();
             const int r0 = split_update ? b : 0;
-            gemm<T>(false, false, M - r0, N2, b, T(-1), B.V + r0, m, B.Z, b, T(1), Atr + r0, ld, nullptr, 0,
-                    st);
+            if constexpr (std::is_same<T, float>::value) {
+                if (tc_qr_enabled())
+                    tc_update(M, N2, b, r0, B.V, m, B.Z, b, Atr, ld, B.tcu, status, st);
+                else
+                    gemm<T>(false, false, M - r0, N2, b, T(-1), B.V + r0, m, B.Z, b, T(1), Atr + r0, ld,
+                            nullptr, 0, st);
+            } else {
+                gemm<T>(false, false, M - r0, N2, b, T(-1), B.V + r0, m, B.Z, b, T(1), Atr + r0, ld,
+                        nullptr, 0, st);
+            }
             tm.end(6, t0);
         }
         if (c) {

@@ -386,6 +386,226 @@ __global__ void k_tc_split_v(const float* __restrict__ V, int64_t ldv, int M, in
     }
 }
 
+// ---- C -= V Z (the trailing update) ------------------------------------------
+// C is the M x N trailing block (column-major, ld), V the panel's M x b
+// reflectors, Z = T^T W (b x N).  Rows r0.. of C are updated (the first b
+// rows, R12, go ahead as their own small product).  D[128 x 64] = Vt_tile Zt_tile
+// with M = 128 rows of C, N = 64 columns, K = b <= 64 (both operands K-major:
+// Vt is V stored row by row, Zt is Z with leading dimension 64), 3xTF32.
+// One CTA owns a 128-row tile (its V hi / lo stay in shared memory) and a
+// run of 64-column tiles: Z tiles through a 2-stage ring, C tiles TMA-loaded
+// into a 3-stage ring, updated in place by the epilogue warps from the TMEM
+// accumulator (double-buffered), and TMA-stored back.
+constexpr int kUpdThreads = 192;   // producer, MMA, 4 epilogue warps
+constexpr int kUN = 64;            // columns per tile (MMA N)
+constexpr int kUZStages = 2;
+constexpr int kUCStages = 3;
+constexpr int kUVBytes = 4 * kTM * kBK * 4;          // hi/lo x 2 K halves x 128 rows x 128 B
+constexpr int kUZBytes = 4 * kUN * kBK * 4;          // hi/lo x 2 K halves x 64 rows x 128 B
+constexpr int kUCBytes = kTM * kUN * 4;              // 128 rows x 64 columns
+constexpr int kUSmemBytes = kUVBytes + kUZStages * kUZBytes + kUCStages * kUCBytes + 1024 + 1024;
+constexpr unsigned kUTmemCols = 2 * kUN;
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, unsigned src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kUpdThreads, 1)
+k_tc_update(const __grid_constant__ CUtensorMap mapVh, const __grid_constant__ CUtensorMap mapVl,
+            const __grid_constant__ CUtensorMap mapZh, const __grid_constant__ CUtensorMap mapZl,
+            const __grid_constant__ CUtensorMap mapC, int r0, int nct, int ct_per,
+            unsigned* __restrict__ status)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* vbuf = smem;                                   // [hi0, hi1, lo0, lo1] x 16 KB
+    unsigned char* zbuf = smem + kUVBytes;                        // [stage][hi0, hi1, lo0, lo1] x 8 KB
+    unsigned char* cbuf = zbuf + kUZStages * kUZBytes;            // [stage] 128 x 64 floats
+    uint64_t* bars = reinterpret_cast<uint64_t*>(cbuf + kUCStages * kUCBytes);
+    // vfull, zfull[2], zempty[2], cfull[3], cempty[3], tfull[2], tempty[2], done
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + 16);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = r0 + blockIdx.x * kTM;            // first row of C of this CTA
+    const int ct0 = blockIdx.y * ct_per;
+    const int nt = min(ct_per, nct - ct0);
+    const unsigned vfull = smem_u32(bars + 0);
+    auto zfull = [&](int q) { return smem_u32(bars + 1 + q); };
+    auto zempty = [&](int q) { return smem_u32(bars + 3 + q); };
+    auto cfull = [&](int q) { return smem_u32(bars + 5 + q); };
+    auto cempty = [&](int q) { return smem_u32(bars + 8 + q); };
+    auto tfull = [&](int q) { return smem_u32(bars + 11 + q); };
+    auto tempty = [&](int q) { return smem_u32(bars + 13 + q); };
+    const unsigned done = smem_u32(bars + 15);
+    auto vtile = [&](int part) { return vbuf + part * (kTM * kBK * 4); };          // part = 2*lo + khalf
+    auto ztile = [&](int st, int part) { return zbuf + st * kUZBytes + part * (kUN * kBK * 4); };
+    auto ctile = [&](int st) { return cbuf + st * kUCBytes; };
+
+    if (threadIdx.x == 0) {
+        mbar_init(vfull, 1);
+        for (int q = 0; q < kUZStages; ++q) {
+            mbar_init(zfull(q), 1);
+            mbar_init(zempty(q), 1);
+        }
+        for (int q = 0; q < kUCStages; ++q) {
+            mbar_init(cfull(q), 1);
+            mbar_init(cempty(q), 1);
+        }
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(tfull(q), 1);
+            mbar_init(tempty(q), 128);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kUTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            bool ok = true;
+            mbar_expect_tx(vfull, kUVBytes);
+            for (int part = 0; part < 4; ++part)
+                tma_load_2d(smem_u32(vtile(part)), (part >> 1) ? &mapVl : &mapVh, (part & 1) * kBK, row,
+                            vfull);
+            int zi = 0, ci = 0;
+            for (int t = 0; t < nt && ok; ++t) {
+                const int col = (ct0 + t) * kUN;
+                const int zs = t % kUZStages, cs = t % kUCStages;
+                if (t >= kUZStages) ok = mbar_wait(zempty(zs), ((t / kUZStages) - 1) & 1, status);
+                if (!ok) break;
+                mbar_expect_tx(zfull(zs), kUZBytes);
+                for (int part = 0; part < 4; ++part)
+                    tma_load_2d(smem_u32(ztile(zs, part)), (part >> 1) ? &mapZl : &mapZh, (part & 1) * kBK,
+                                col, zfull(zs));
+                ++zi;
+                if (t >= kUCStages) ok = mbar_wait(cempty(cs), ((t / kUCStages) - 1) & 1, status);
+                if (!ok) break;
+                mbar_expect_tx(cfull(cs), kUCBytes);
+                tma_load_2d(smem_u32(ctile(cs)), &mapC, row, col, cfull(cs));
+                ++ci;
+            }
+            // this CTA's copies have landed before it may exit
+            mbar_wait(vfull, 0, status);
+            for (int t = std::max(0, zi - kUZStages); t < zi; ++t)
+                mbar_wait(zfull(t % kUZStages), (t / kUZStages) & 1, status);
+            for (int t = std::max(0, ci - kUCStages); t < ci; ++t)
+                mbar_wait(cfull(t % kUCStages), (t / kUCStages) & 1, status);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tf32_idesc(kTM, kUN);
+            bool ok = mbar_wait(vfull, 0, status);
+            for (int t = 0; t < nt && ok; ++t) {
+                const int zs = t % kUZStages, tb = t & 1;
+                ok = mbar_wait(zfull(zs), (t / kUZStages) & 1, status);
+                if (ok && t >= 2) ok = mbar_wait(tempty(tb), ((t >> 1) - 1) & 1, status);
+                if (!ok) break;
+                tc_fence_after();
+                const unsigned d = tmem + (unsigned)(tb * kUN);
+#pragma unroll
+                for (int k8 = 0; k8 < 2 * kBK / 8; ++k8) {
+                    const int kh = k8 >> 2;
+                    const unsigned off = (k8 & 3) * 32;
+                    const unsigned ah = smem_u32(vtile(kh)) + off, al = smem_u32(vtile(2 + kh)) + off;
+                    const unsigned bh = smem_u32(ztile(zs, kh)) + off, bl = smem_u32(ztile(zs, 2 + kh)) + off;
+                    mma_tf32(d, sw128_desc(al), sw128_desc(bh), idesc, k8 > 0 ? 1u : 0u);
+                    mma_tf32(d, sw128_desc(ah), sw128_desc(bl), idesc, 1u);
+                    mma_tf32(d, sw128_desc(ah), sw128_desc(bh), idesc, 1u);
+                }
+                mma_commit(zempty(zs));
+                mma_commit(tfull(tb));
+            }
+            mma_commit(done);
+            mbar_wait(done, 0, status);
+        }
+    } else {
+        // warps 2..5: C tile -= D, each thread one row of the tile
+        const int quad = warp & 3;
+        const int r = quad * 32 + lane;
+        const bool leader = threadIdx.x == 64;
+        volatile int* s_fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+        if (leader) *s_fail = 0;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        int stored = 0;
+        for (int t = 0; t < nt; ++t) {
+            const int tb = t & 1, cs = t % kUCStages;
+            const bool got = mbar_wait(tfull(tb), (t >> 1) & 1, status) &&
+                             mbar_wait(cfull(cs), (t / kUCStages) & 1, status);
+            // the four warps leave together: the named barriers below have no timeout
+            if (!got) *s_fail = 1;
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (*s_fail) break;
+            tc_fence_after();
+            float* c = reinterpret_cast<float*>(ctile(cs));
+#pragma unroll
+            for (int h = 0; h < kUN / 32; ++h) {
+                float v[32];
+                tmem_ld32(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(tb * kUN + h * 32), v);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) c[(h * 32 + q) * kTM + r] -= v[q];
+            }
+            tc_fence_before();
+            mbar_arrive(tempty(tb));
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (leader) {
+                tma_store_2d(&mapC, row, (ct0 + t) * kUN, smem_u32(c));
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                ++stored;
+                // the previous tile's store has read its stage: release it
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                if (t >= 1) mbar_arrive(cempty((t - 1) % kUCStages));
+            }
+        }
+        if (leader && stored > 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kUTmemCols)
+                     : "memory");
+    }
+}
+
+// Vt (rows of V, ld 64) and Zt (Z with ld 64) split into hi / lo
+__global__ void k_tc_split_vz(const float* __restrict__ V, int64_t ldv, int M, int b,
+                              const float* __restrict__ Z, int64_t ldz, int N, float* __restrict__ Vth,
+                              float* __restrict__ Vtl, float* __restrict__ Zth, float* __restrict__ Ztl)
+{
+    const int64_t nv = (int64_t)M * b, total = nv + (int64_t)N * b;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < nv) {
+            const int c = (int)(e % b), i = (int)(e / b);
+            const float a = V[i + (int64_t)c * ldv];
+            const float h = tf32_hi(a);
+            Vth[(int64_t)i * kTN + c] = h;
+            Vtl[(int64_t)i * kTN + c] = a - h;
+        } else {
+            const int64_t f = e - nv;
+            const int c = (int)(f % b), n = (int)(f / b);
+            const float a = Z[c + (int64_t)n * ldz];
+            const float h = tf32_hi(a);
+            Zth[c + (int64_t)n * kTN] = h;
+            Ztl[c + (int64_t)n * kTN] = a - h;
+        }
+    }
+}
+
 // ---- host side ---------------------------------------------------------------
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
@@ -483,6 +703,80 @@ void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, in
                                                                 out, status);
     SKL_LAUNCHED();
     if (splits > 1) splitk_reduce_launch<float>(b, N, splits, 1.0f, partial, 0.0f, W, b, st);
+}
+
+size_t tc_update_scratch_floats(int64_t M, int64_t N)
+{
+    return (size_t)(2 * M * kTN + 2 * N * kTN) + 64;
+}
+
+void tc_update(int M, int N, int b, int r0, const float* V, int64_t ldv, const float* Z, int64_t ldz,
+               float* C, int64_t ldc, float* scratch, unsigned* status, cudaStream_t st)
+{
+    if (M - r0 <= 0 || N <= 0 || b <= 0) return;
+    if (b > kTN) fail(SKL_ERR_INVALID, "tc_update: panel wider than 64");
+    float* Vth = scratch;
+    float* Vtl = Vth + (int64_t)M * kTN;
+    float* Zth = Vtl + (int64_t)M * kTN;
+    float* Ztl = Zth + (int64_t)N * kTN;
+    {
+        const int64_t total = (int64_t)(M + N) * b;
+        const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 8);
+        k_tc_split_vz<<<g, 256, 0, st>>>(V, ldv, M, b, Z, ldz, N, Vth, Vtl, Zth, Ztl);
+        SKL_LAUNCHED();
+    }
+    // K-major operands: dims {K = b, rows}, rows 64 floats apart; C: {rows, cols}
+    auto kmap = [&](const float* base, int64_t rows, int box_rows) {
+        CUtensorMap m;
+        cuuint64_t dims[2] = {(cuuint64_t)b, (cuuint64_t)rows};
+        cuuint64_t strides[1] = {(cuuint64_t)(kTN * 4)};
+        cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) fail(SKL_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return m;
+    };
+    const CUtensorMap mVh = kmap(Vth, M, kTM), mVl = kmap(Vtl, M, kTM);
+    const CUtensorMap mZh = kmap(Zth, N, kUN), mZl = kmap(Ztl, N, kUN);
+    CUtensorMap mC;
+    {
+        if (((uintptr_t)C & 15) || ((ldc * 4) & 15))
+            fail(SKL_ERR_INVALID, "tc_update: C base or stride not 16-byte aligned");
+        cuuint64_t dims[2] = {(cuuint64_t)M, (cuuint64_t)N};
+        cuuint64_t strides[1] = {(cuuint64_t)(ldc * 4)};
+        cuuint32_t box[2] = {(cuuint32_t)kTM, (cuuint32_t)kUN};
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = encode_fn()(&mC, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)C, dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) fail(SKL_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    const int nrt = (M - r0 + kTM - 1) / kTM;
+    const int nct = (N + kUN - 1) / kUN;
+    int splits = std::max(1, std::min(nct, sm_count() / nrt));
+    const int ct_per = (nct + splits - 1) / splits;
+    splits = (nct + ct_per - 1) / ct_per;
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [] {
+        cudaFuncSetAttribute((const void*)k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kUSmemBytes);
+    });
+    k_tc_update<<<dim3(nrt, splits), kUpdThreads, kUSmemBytes, st>>>(mVh, mVl, mZh, mZl, mC, r0, nct, ct_per,
+                                                                     status);
+    SKL_LAUNCHED();
+}
+
+void update_product(bool tensor, int M, int N, int b, int r0, const float* V, int64_t ldv,
+                    const float* Z, int64_t ldz, float* C, int64_t ldc, float* scratch,
+                    unsigned* status, cudaStream_t st)
+{
+    if (tensor)
+        tc_update(M, N, b, r0, V, ldv, Z, ldz, C, ldc, scratch, status, st);
+    else
+        gemm<float>(false, false, M - r0, N, b, -1.0f, V + r0, ldv, Z, ldz, 1.0f, C + r0, ldc, nullptr,
+                    0, st);
 }
 
 bool tc_qr_enabled()

@@ -324,6 +324,39 @@ static void gemm_vta_block(int64_t M, int64_t N, int64_t b, const float* V, int6
     if (stt & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
 }
 
+// C (M x N) rows r0.. -= V Z (FP32): the trailing update of the CPQR.
+static void gemm_update_block(int64_t M, int64_t N, int64_t b, int64_t r0, const float* V, int64_t ldv,
+                              const float* Z, int64_t ldz, float* C, int64_t ldc, int tensor)
+{
+    Context& Cx = context(0);
+    cudaStream_t st = Cx.stream;
+    const int64_t ldd = (M + 31) / 32 * 32;
+    const size_t scr = tc_update_scratch_floats(M, N);
+    Sizer S;
+    S.add<float>(ldd * b); S.add<float>(b * N); S.add<float>(ldd * N); S.add<float>((int64_t)scr);
+    Cx.arena.reserve(S.bytes());
+    Cx.arena.reset();
+    float* Vd = Cx.arena.alloc<float>(ldd * b);
+    float* Zd = Cx.arena.alloc<float>(b * N);
+    float* Cd = Cx.arena.alloc<float>(ldd * N);
+    float* sd = Cx.arena.alloc<float>((int64_t)scr);
+    SKL_CUDA(cudaMemcpy2DAsync(Vd, ldd * sizeof(float), V, ldv * sizeof(float), M * sizeof(float), b,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpy2DAsync(Zd, b * sizeof(float), Z, ldz * sizeof(float), b * sizeof(float), N,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemcpy2DAsync(Cd, ldd * sizeof(float), C, ldc * sizeof(float), M * sizeof(float), N,
+                               cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(Cx.dev_status, 0, sizeof(unsigned), st));
+    update_product(tensor != 0, (int)M, (int)N, (int)b, (int)r0, Vd, ldd, Zd, b, Cd, ldd, sd,
+                   Cx.dev_status, st);
+    unsigned stt = 0;
+    SKL_CUDA(cudaMemcpyAsync(&stt, Cx.dev_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaMemcpy2DAsync(C, ldc * sizeof(float), Cd, ldd * sizeof(float), M * sizeof(float), N,
+                               cudaMemcpyDeviceToHost, st));
+    SKL_CUDA(cudaStreamSynchronize(st));
+    if (stt & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+}
+
 }  // namespace skl
 
 using namespace skl;
@@ -371,6 +404,17 @@ skl_status skl_gemm_vta(int64_t M, int64_t N, int64_t b, const float* V, int64_t
             M > 0x7fffffff || N > 0x7fffffff)
             fail(SKL_ERR_INVALID, "skl_gemm_vta: bad argument");
         gemm_vta_block(M, N, b, V, ldv, A, lda, W, tensor);
+    });
+}
+
+skl_status skl_gemm_update(int64_t M, int64_t N, int64_t b, int64_t r0, const float* V, int64_t ldv,
+                           const float* Z, int64_t ldz, float* C, int64_t ldc, int tensor)
+{
+    return guard([&] {
+        if (!V || !Z || !C || M <= 0 || N <= 0 || b <= 0 || b > 64 || r0 < 0 || r0 > M || (r0 & 3) ||
+            ldv < M || ldz < b || ldc < M || M > 0x7fffffff || N > 0x7fffffff)
+            fail(SKL_ERR_INVALID, "skl_gemm_update: bad argument");
+        gemm_update_block(M, N, b, r0, V, ldv, Z, ldz, C, ldc, tensor);
     });
 }
 

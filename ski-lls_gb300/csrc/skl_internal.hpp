@@ -167,6 +167,16 @@ constexpr unsigned kStatusTcTimeout = 64u;
 size_t tc_vta_scratch_floats(int64_t M);
 void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, int64_t lda, float* W,
             float* scratch, size_t scratch_floats, unsigned* status, cudaStream_t st);
+// C (M x N, ldc) rows r0.. -= V Z on the tensor cores (tcgen05, 3xTF32):
+// V is M x b (ldv), Z is b x N (ldz), b <= 64; C 16-byte aligned with ldc*4 a
+// multiple of 16 bytes.  scratch holds tc_update_scratch_floats(M, N) floats.
+size_t tc_update_scratch_floats(int64_t M, int64_t N);
+void tc_update(int M, int N, int b, int r0, const float* V, int64_t ldv, const float* Z, int64_t ldz,
+               float* C, int64_t ldc, float* scratch, unsigned* status, cudaStream_t st);
+// C rows r0.. -= V Z by tc_update (tensor = true) or the CUDA-core FP32 GEMM.
+void update_product(bool tensor, int M, int N, int b, int r0, const float* V, int64_t ldv,
+                    const float* Z, int64_t ldz, float* C, int64_t ldc, float* scratch,
+                    unsigned* status, cudaStream_t st);
 // The CPQR's FP32 products go to the tensor cores unless SKILLS_QR_TC=0.
 bool tc_qr_enabled();
 // W = V^T A by tc_vta (tensor = true) or the CUDA-core FP32 GEMM; the same

@@ -139,6 +139,8 @@ def lib():
         L.skl_csc_mv.restype = ctypes.c_int
         L.skl_gemm_vta.argtypes = [i64, i64, i64, vp, i64, vp, i64, vp, ctypes.c_int]
         L.skl_gemm_vta.restype = ctypes.c_int
+        L.skl_gemm_update.argtypes = [i64, i64, i64, i64, vp, i64, vp, i64, vp, i64, ctypes.c_int]
+        L.skl_gemm_update.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -399,6 +401,19 @@ def gemm_vta(V, A, tensor=True):
     W = np.zeros((b, N), dtype=np.float32, order="F")
     _check(lib().skl_gemm_vta(M, N, b, _ptr(V), M, _ptr(A), M, _ptr(W), 1 if tensor else 0))
     return W
+
+
+def gemm_update(C, V, Z, r0=0, tensor=True):
+    """C[r0:, :] - V[r0:, :] Z in FP32 (returns a new array) through the CPQR's
+    trailing-update product (tensor=True: tcgen05 3xTF32 kernel)."""
+    C = np.array(C, dtype=np.float32, order="F", copy=True)
+    V = np.asfortranarray(V, dtype=np.float32)
+    Z = np.asfortranarray(Z, dtype=np.float32)
+    M, N = C.shape
+    b = V.shape[1]
+    _check(lib().skl_gemm_update(M, N, b, r0, _ptr(V), M, _ptr(Z), b, _ptr(C), M,
+                                 1 if tensor else 0))
+    return C
 
 
 def dht_length(n, wisdom=0):

@@ -47,3 +47,27 @@ def test_tensor_core_vta_matches_cuda_core_kernel():
     assert np.max(np.abs(Wt - Ws) / bound) <= 2.0 ** -14
     # deterministic: a second call gives the same bits
     assert np.array_equal(skl.gemm_vta(V, A, tensor=True), Wt.astype(np.float32))
+
+
+UPDATE_SHAPES = [(8500, 4936, 64, 64), (8500, 130, 64, 64), (1000, 300, 40, 40), (97, 130, 64, 0),
+                 (33, 1, 64, 0), (4100, 1000, 8, 8)]
+
+
+@pytest.mark.parametrize("shape", UPDATE_SHAPES)
+def test_tensor_core_update_accuracy(shape):
+    """C[r0:] -= V[r0:] Z (the trailing update): rows above r0 untouched, the
+    rest within ~2^-21 of |C| + |V| |Z| entry by entry (FP32-class)."""
+    M, N, b, r0 = shape
+    rng = np.random.default_rng(M + 3 * N + b)
+    V = rng.standard_normal((M, b)).astype(np.float32)
+    Z = (rng.standard_normal((b, N)) * 10.0 ** rng.uniform(-2, 2, N)).astype(np.float32)
+    C = (rng.standard_normal((M, N)) * 10.0 ** rng.uniform(-2, 2, N)).astype(np.float32)
+    exact = C.astype(np.float64).copy()
+    exact[r0:] -= V[r0:].astype(np.float64) @ Z.astype(np.float64)
+    bound = np.abs(C.astype(np.float64))
+    bound[r0:] += np.abs(V[r0:].astype(np.float64)) @ np.abs(Z.astype(np.float64))
+    for tensor in (True, False):
+        out = skl.gemm_update(C, V, Z, r0, tensor=tensor)
+        assert np.array_equal(out[:r0], C[:r0]), (shape, tensor)
+        rel = np.abs(out.astype(np.float64) - exact) / bound
+        assert rel.max() <= 2.0 ** -20, (shape, tensor, rel.max())
