@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512,
                     help="problems in the batched_sparse workload")
+    ap.add_argument("--autotune", action="store_true",
+                    help="sparse workloads: autotuned launch shapes (tuned during the warm-up)")
     ap.add_argument("--profile-one", action="store_true",
                     help="one solve with per-kernel events, for profilers")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -323,12 +325,14 @@ class SparseOnDevice:
         self.bd = torch.from_numpy(b.astype(np.float64)).to(dev)
         self.xd = torch.zeros(self.d, dtype=torch.float64, device=dev)
 
+    autotune = 0
+
     def solve(self, skl, precision, profile, stream, device, gamma, k):
         return skl.sparse_solve_device(self.n, self.d, self.Ap.data_ptr(), self.Ai.data_ptr(),
                                        self.Ax.data_ptr(), self.bd.data_ptr(), self.xd.data_ptr(),
                                        self.nnz, gamma, k, precision=precision, seed=1,
                                        it_tol=IT_TOL, stream=stream, profile=profile,
-                                       device=device)
+                                       device=device, autotune=self.autotune)
 
     def host_solver(self, skl, torch, opts):
         """Returns (call, x_host, h2d, d2h): call() runs skl_sparse_solve on
@@ -453,6 +457,8 @@ def run_ours(args, rank, world):
     gamma, k = w["gamma"], w["k"]
     hbm_peak, _, peak_kind = load_peaks()
     P = (SparseOnDevice if w["kind"] == "sparse" else DenseOnDevice)(A, b, dev, torch)
+    if args.autotune and P.kind == "sparse":
+        P.autotune = 1
     n, d = P.n, P.d
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.Stream(device=dev)
@@ -566,6 +572,7 @@ def run_ours(args, rank, world):
         o = skl.default_opts()
         o.gamma, o.k, o.it_tol, o.seed_mode, o.seed, o.device = gamma, k, IT_TOL, 1, 1, local
         o.stream = stream.cuda_stream
+        o.autotune = getattr(P, "autotune", 0)
         call, hxo, h2d, d2h = P.host_solver(skl, torch, o)
         times = []
         for q in range(max(3, args.warmup) + args.steps):
@@ -622,6 +629,8 @@ def run_ours(args, rank, world):
                   "rcond_r11": last.rcond_r11, "fp64_fallback": int(last.fp64_fallback),
                   "explicit_residual": last.explicit_residual,
                   "sketch_refine_steps": int(last.sketch_refine_steps),
+                  "tuned_launch_shapes": dict(zip(("sketch_threads", "panel_width", "lanes_Az",
+                                                   "lanes_ATu"), [int(v) for v in last.tuned])),
                   "quality_exact": quality,
                   "phases_ms": phases(last),
                   "qr_substeps_ms": {nm: float(v) for nm, v in zip(

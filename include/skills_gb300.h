@@ -91,6 +91,11 @@ typedef struct {
     int device;              /* CUDA device ordinal                               */
     void* stream;            /* cudaStream_t to run on; NULL = the library's own  */
     int profile;             /* 1: time the LSQR products with CUDA events        */
+    int autotune;            /* sparse path, 1: the first solve of a shape class
+                                times the candidate launch shapes (sketch block
+                                size, CPQR panel width, lanes per row / column of
+                                the two sparse products) on its own data and caches
+                                the fastest for the process; 0: fixed heuristics */
 } skl_opts;
 
 typedef struct {
@@ -132,6 +137,10 @@ typedef struct {
     /* mixed dense path: 1 if A held values outside [2^-100, 2^100] in
        magnitude and the solve ran on the FP64 path instead */
     int fp64_fallback;
+    /* launch shapes this solve used when autotuned (0 = the fixed heuristic):
+       sketch block size, CPQR panel width, lanes per CSR row of A z, lanes per
+       CSC column of A^T u */
+    int64_t tuned[4];
 } skl_info;
 
 /* Defaults of include/bench_config.hpp:7-20 (IT_TOL 1e-6, MAX_IT 10000,

@@ -25,6 +25,7 @@
 // the scalar recurrences stay in FP64.  On the sparse path the pairs hold the
 // equilibrated values A(:, c) / ||A(:, c)||, so no value leaves the float
 // range.  The all-FP64 path uses plain double values and DFMA.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -875,7 +876,7 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
         return;
     }
     const double avg = P.n ? (double)P.nnz / P.n : 0.0;
-    const int L = lanes_for(avg);
+    const int L = P.lanes_n ? P.lanes_n : lanes_for(avg);
     // z staged in shared memory (<= 96 KB); blocks sized to ~4 per SM
     const size_t zbytes = (size_t)P.d * sizeof(V);
     const int stage = zbytes <= 96 * 1024 ? (int)P.d : 0;
@@ -908,7 +909,7 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
         return;
     }
     const double avg = P.d ? (double)P.nnz / P.d : 0.0;
-    const int L = lanes_for(avg);
+    const int L = P.lanes_t ? P.lanes_t : lanes_for(avg);
     const int64_t threads = (int64_t)P.r * L;
     unsigned g = (unsigned)std::min<int64_t>((threads + kLThreads - 1) / kLThreads, 152 * 32);
 #define SPMV_T(LL) k_spmv_t_csc<MIXED, LL><<<g, kLThreads, 0, st>>>(P.cp, P.ri, (const V*)P.rx, P.cols, P.opscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
@@ -1063,6 +1064,60 @@ LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t m
     if (P.precision == SKL_PREC_MIXED)
         return run_impl<true>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
     return run_impl<false>(P, b, tol, max_it, y, work, host_pinned, st, profile, capture_stream);
+}
+
+// ------------------------------------------------------------- tuning --
+// Times the CSR product A z and the CSC product A^T u of this problem's matrix
+// for each lanes-per-row (column) choice, median of three launches after one
+// warm-up, and keeps the fastest in P.lanes_n / P.lanes_t.
+void tune_lsqr_products(LsqrProblem& P, void* work, cudaStream_t st)
+{
+    if (P.Ad || P.n <= 0 || P.r <= 0) return;
+    LsqrBufs B = carve(P, work);
+    LsqrState init{};
+    init.ib = 1.0;
+    const size_t vsz = P.precision == SKL_PREC_MIXED ? sizeof(float2) : sizeof(double);
+    SKL_CUDA(cudaMemcpyAsync(B.S, &init, sizeof(LsqrState), cudaMemcpyHostToDevice, st));
+    SKL_CUDA(cudaMemsetAsync(B.uh, 0, P.n * sizeof(double), st));
+    SKL_CUDA(cudaMemsetAsync(B.us, 0, P.n * vsz, st));
+    SKL_CUDA(cudaMemsetAsync(B.z, 0, P.d * vsz, st));
+    cudaEvent_t e0, e1;
+    SKL_CUDA(cudaEventCreate(&e0));
+    SKL_CUDA(cudaEventCreate(&e1));
+    auto time_it = [&](auto&& launch) {
+        launch();
+        float t[3];
+        for (float& v : t) {
+            SKL_CUDA(cudaEventRecord(e0, st));
+            launch();
+            SKL_CUDA(cudaEventRecord(e1, st));
+            SKL_CUDA(cudaEventSynchronize(e1));
+            SKL_CUDA(cudaEventElapsedTime(&v, e0, e1));
+        }
+        std::sort(t, t + 3);
+        return t[1];
+    };
+    const int cand[4] = {4, 8, 16, 32};
+    float best_n = 1e30f, best_t = 1e30f;
+    int ln = 0, lt = 0;
+    for (int L : cand) {
+        P.lanes_n = L;
+        const float tn = time_it([&] {
+            if (P.precision == SKL_PREC_MIXED) launch_spmv_n<true>(P, B, st);
+            else launch_spmv_n<false>(P, B, st);
+        });
+        if (tn < best_n) { best_n = tn; ln = L; }
+        P.lanes_t = L;
+        const float tt = time_it([&] {
+            if (P.precision == SKL_PREC_MIXED) launch_spmv_t<true>(P, B, st);
+            else launch_spmv_t<false>(P, B, st);
+        });
+        if (tt < best_t) { best_t = tt; lt = L; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    P.lanes_n = ln;
+    P.lanes_t = lt;
 }
 
 // ------------------------------------------------ one product in isolation --

@@ -901,13 +901,14 @@ struct QrPlan {
     int nb, nbp, R;
 };
 
+// nb_cap > 0 caps the panel width (a tuning choice, multiple of 8).
 template <typename T>
-static QrPlan qr_plan(int64_t m, int64_t d)
+static QrPlan qr_plan(int64_t m, int64_t d, int nb_cap = 0)
 {
     QrPlan p;
     p.R = (int)((m + kCluster - 1) / kCluster);
     p.R = (p.R + 3) / 4 * 4;   // whole float4 / double2 row vectors
-    int nb = kMaxNb;
+    int nb = (nb_cap >= 8 && nb_cap < kMaxNb) ? nb_cap / 8 * 8 : kMaxNb;
     const size_t budget = kClusterSmemBudget;
     while (nb > 8 && panel_smem_bytes<T>(p.R, nb) > budget) nb -= 8;
     if (panel_smem_bytes<T>(p.R, nb) > budget)
@@ -1060,10 +1061,11 @@ struct QrTimer {
 
 template <typename T>
 static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
-                    unsigned* status, cudaStream_t st, double* c, bool pivoting, double* qr_prof)
+                    unsigned* status, cudaStream_t st, double* c, bool pivoting, double* qr_prof,
+                    int nb_cap)
 {
     QrTimer tm{qr_prof, {}, {}, 0, st};
-    QrPlan p = qr_plan<T>(m, d);
+    QrPlan p = qr_plan<T>(m, d, nb_cap);
     QrBuffers<T> B = qr_carve<T>(work, m, d, p, nullptr);
     const int nb = p.nb, nbp = p.nbp;
     const int64_t mn = m < d ? m : d;
@@ -1092,10 +1094,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
 
     // Two streams.  The sample work of panel j (Y downdate, the sample QRP of
     // panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs on a
-    // high-priority side stream: the part that needs V and T alone (GU, GUT, B)
-    // overlaps W and R12, the rest overlaps the big trailing update and Q^T c;
-    // panel j+1's permutation waits for the side stream's event.  (R12 is the
-    // first b rows of the trailing update, done ahead of the other rows.)
+    // high-priority side stream: the part that needs V and T alone (GU, GUT, B
+    // and G -= GUT V^T) overlaps W and R12, the rest (Y2 -= B R12, the next
+    // sample QRP) overlaps the big trailing update and Q^T c; panel j+1's
+    // permutation waits for the side stream's events.  (R12 is the first b
+    // rows of the trailing update, done ahead of the other rows.)
     cudaStream_t side = nullptr;
     cudaEvent_t evV = nullptr, evR = nullptr, evY = nullptr, evG = nullptr;
     if (pivoting) {
@@ -1205,6 +1208,12 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             SKL_LAUNCHED();
             gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
                     side);
+            // G(:, j:m) -= GUT V^T needs only GUT and V: done here, it overlaps W and
+            // R12 on the main stream instead of following the next sample QRP (the
+            // next panel, which rewrites V, waits for it through evG)
+            gemm<T>(false, true, nbp, M, b, T(-1), B.GUT, nbp, B.V, m, T(1), Gj, nbp, nullptr, 0,
+                    side);
+            SKL_CUDA(cudaEventRecord(evG, side));
             tms.end(7, t0);
         }
         const int N2 = N - b;
@@ -1234,8 +1243,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
                 gemm<T>(false, false, b, N2, b, T(-1), B.V, m, B.Z, b, T(1), Atr, ld, nullptr, 0, st);
             SKL_CUDA(cudaEventRecord(evR, st));
             SKL_CUDA(cudaStreamWaitEvent(side, evR, 0));
-            // side: Y2 -= B R12 ; the next sample QRP (evY) ; G(:, j:m) -= GUT V^T,
-            // which only the next downdate needs (evG)
+            // side: Y2 -= B R12 and the next sample QRP (evY)
             cudaEvent_t t0 = tms.begin();
             if (N2 > 0)
                 gemm<T>(false, false, nbp, N2, b, T(-1), B.Bm, nbp, Atr, ld, T(1),
@@ -1248,11 +1256,6 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
                 launch_yqrp(jn, bn, (int)(d - jn), side, tms);
             }
             SKL_CUDA(cudaEventRecord(evY, side));
-            t0 = tms.begin();
-            gemm<T>(false, true, nbp, M, b, T(-1), B.GUT, nbp, B.V, m, T(1), Gj, nbp, nullptr, 0,
-                    side);
-            tms.end(7, t0);
-            SKL_CUDA(cudaEventRecord(evG, side));
             side_pending = true;
         }
         if (N2 > 0) {
@@ -1281,22 +1284,30 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             tm.end(3, t0);
         }
     }
-    if (side_pending) SKL_CUDA(cudaStreamWaitEvent(st, evG, 0));
+    if (side_pending) {
+        SKL_CUDA(cudaStreamWaitEvent(st, evG, 0));
+        SKL_CUDA(cudaStreamWaitEvent(st, evY, 0));
+    }
     tms.finish();
     tm.finish();
 }
 
 template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work, unsigned* status,
-          cudaStream_t st, double* c, int pivoting, double* qr_prof)
+          cudaStream_t st, double* c, int pivoting, double* qr_prof, int nb_cap)
 {
-    qr_core<T>(A, m, d, ld, jpvt, tau, work, status, st, c, pivoting != 0, qr_prof);
+    qr_core<T>(A, m, d, ld, jpvt, tau, work, status, st, c, pivoting != 0, qr_prof, nb_cap);
+}
+
+int cpqr_panel_width(int64_t m, int64_t d, int nb_cap)
+{
+    return qr_plan<float>(m, d, nb_cap).nb;
 }
 
 template void cpqr<float>(float*, int64_t, int64_t, int64_t, int*, float*, void*, unsigned*,
-                          cudaStream_t, double*, int, double*);
+                          cudaStream_t, double*, int, double*, int);
 template void cpqr<double>(double*, int64_t, int64_t, int64_t, int*, double*, void*, unsigned*,
-                           cudaStream_t, double*, int, double*);
+                           cudaStream_t, double*, int, double*, int);
 template size_t cpqr_workspace_bytes<float>(int64_t, int64_t);
 template size_t cpqr_workspace_bytes<double>(int64_t, int64_t);
 

@@ -20,15 +20,15 @@ namespace skl {
 
 constexpr int kSketchThreads = 512;
 
-template <typename T>
-__global__ void __launch_bounds__(kSketchThreads)
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT)
 k_sketch_sparse_smem(const int* __restrict__ cp, const int* __restrict__ ri,
                      const double* __restrict__ Ax, const unsigned* __restrict__ hidx, int k,
                      int m, T* __restrict__ SA, int64_t ld, int equilibrate, double inv_sqrt_k,
                      double* __restrict__ colnorm, double* __restrict__ colscale)
 {
     extern __shared__ unsigned long long acc[];   // m entries
-    __shared__ double s_red[kSketchThreads / 32];
+    __shared__ double s_red[NT / 32];
     const int j = blockIdx.x;
     const int p0 = cp[j], p1 = cp[j + 1];
     for (int h = threadIdx.x; h < m; h += blockDim.x) acc[h] = 0ull;
@@ -137,20 +137,40 @@ static size_t smem_optin()
     return v;
 }
 
+template <typename T, int NT>
+static void launch_sketch_smem(const int* cp, const int* ri, const double* Ax, int64_t d,
+                               const unsigned* hidx, int k, int64_t m, T* SA, int64_t ld,
+                               int equilibrate, double isk, double* colnorm, double* colscale,
+                               size_t smem, cudaStream_t st)
+{
+    allow_max_dynamic_smem((const void*)k_sketch_sparse_smem<T, NT>);
+    k_sketch_sparse_smem<T, NT><<<(unsigned)d, NT, smem, st>>>(cp, ri, Ax, hidx, k, (int)m, SA, ld,
+                                                               equilibrate, isk, colnorm, colscale);
+    SKL_LAUNCHED();
+}
+
 template <typename T>
 void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, int64_t d,
                    const unsigned* hidx, int k, int64_t m, T* SA, int64_t ld, int equilibrate,
-                   double* colnorm, double* colscale, cudaStream_t st)
+                   double* colnorm, double* colscale, cudaStream_t st, int threads)
 {
     (void)n;
     if (d <= 0) return;
     const double isk = 1.0 / std::sqrt((double)k);
     size_t smem = (size_t)m * sizeof(unsigned long long);
     if (smem + 1024 <= smem_optin()) {
-        allow_max_dynamic_smem((const void*)k_sketch_sparse_smem<T>);
-        k_sketch_sparse_smem<T><<<(unsigned)d, kSketchThreads, smem, st>>>(
-            cp, ri, Ax, hidx, k, (int)m, SA, ld, equilibrate, isk, colnorm, colscale);
-        SKL_LAUNCHED();
+        // one CTA per column of A; the block size is a tuning choice (S A is
+        // accumulated exactly in fixed point; only the order in which the
+        // column norm's squares are summed depends on it)
+        if (threads == 256)
+            launch_sketch_smem<T, 256>(cp, ri, Ax, d, hidx, k, m, SA, ld, equilibrate, isk, colnorm,
+                                       colscale, smem, st);
+        else if (threads == 1024)
+            launch_sketch_smem<T, 1024>(cp, ri, Ax, d, hidx, k, m, SA, ld, equilibrate, isk, colnorm,
+                                        colscale, smem, st);
+        else
+            launch_sketch_smem<T, kSketchThreads>(cp, ri, Ax, d, hidx, k, m, SA, ld, equilibrate, isk,
+                                                  colnorm, colscale, smem, st);
         return;
     }
     // Bounded global scratch: up to 256 columns in flight per launch.
@@ -169,10 +189,10 @@ void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, in
 
 template void sketch_sparse<float>(const int*, const int*, const double*, int64_t, int64_t,
                                    const unsigned*, int, int64_t, float*, int64_t, int, double*,
-                                   double*, cudaStream_t);
+                                   double*, cudaStream_t, int);
 template void sketch_sparse<double>(const int*, const int*, const double*, int64_t, int64_t,
                                     const unsigned*, int, int64_t, double*, int64_t, int, double*,
-                                    double*, cudaStream_t);
+                                    double*, cudaStream_t, int);
 
 // S*b: Sb[h] = sum over the bucket of h, in increasing source row, of
 // (+-1/sqrt(k)) * b[i] -- the order and arithmetic of cs_dl_gaxpy.

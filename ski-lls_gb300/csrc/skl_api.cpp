@@ -12,7 +12,9 @@
 // Dense pipeline (ls_dense_hashing_blendenpik, src/ls_dense_hashing_blendenpik.cpp:23-149)
 // follows the same steps with the DHT-hashing sketch and dense products.
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -222,6 +224,55 @@ static void check_opts(const skl_opts& o)
         fail(SKL_ERR_INVALID, "unknown precision");
 }
 
+// ------------------------------------------------------------ autotuning --
+// opts.autotune = 1: the first solve of a shape class times the candidates of
+// each tunable launch shape on its own data -- the sketch's block size, the
+// CPQR's panel width (whole factorizations of a copy of the sketch), the lanes
+// per row / column of LSQR's two sparse products -- and caches the fastest
+// for the process (skl_finalize clears the cache).  Shape class: precision
+// and half-octave buckets of n, d, nnz per row and m.
+struct Tuned {
+    int sketch_threads = 0, nb = 0, lanes_n = 0, lanes_t = 0;
+};
+static std::mutex g_tune_mu;
+static std::map<std::array<int, 5>, Tuned> g_tune;
+
+static int octave_bucket(double x) { return (int)std::lround(2.0 * std::log2(std::max(x, 1.0))); }
+
+static std::array<int, 5> tune_key(int prec, int64_t n, int64_t d, int64_t nnz, int64_t m)
+{
+    return {prec, octave_bucket((double)n), octave_bucket((double)d),
+            octave_bucket(16.0 * (double)nnz / (double)std::max<int64_t>(n, 1)), octave_bucket((double)m)};
+}
+
+void tune_cache_clear()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+
+// Median of three timed runs of fn on st after one warm-up.
+template <typename F>
+static float time_median3(cudaStream_t st, F&& fn)
+{
+    cudaEvent_t e0, e1;
+    SKL_CUDA(cudaEventCreate(&e0));
+    SKL_CUDA(cudaEventCreate(&e1));
+    fn();
+    float t[3];
+    for (float& v : t) {
+        SKL_CUDA(cudaEventRecord(e0, st));
+        fn();
+        SKL_CUDA(cudaEventRecord(e1, st));
+        SKL_CUDA(cudaEventSynchronize(e1));
+        SKL_CUDA(cudaEventElapsedTime(&v, e0, e1));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::sort(t, t + 3);
+    return t[1];
+}
+
 // Status bit a QR pivot selection sets when it meets non-finite values.
 constexpr unsigned kQrSelectBit = 8u;
 
@@ -331,8 +382,34 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     build_buckets(hidx, n, (int)k, m, bptr, bent, (int*)work, st);
     trace_phase(st, "buckets");
     SKL_CUDA(cudaEventRecord(ev[2], st));
+    // ---- launch shapes: the tuned ones of this shape class, or tune now ----
+    Tuned tuned;
+    const auto tkey = tune_key(o.precision, n, d, nnz, m);
+    bool have_tuned = false;
+    if (o.autotune) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(tkey);
+        if (it != g_tune.end()) {
+            tuned = it->second;
+            have_tuned = true;
+        }
+    }
+    const bool tuning = o.autotune && !have_tuned;
     // ---- sketch ----
-    sketch_sparse<T>(cp, ri, in.Ax, n, d, hidx, (int)k, m, SA, ld, 1, colnorm, colscale, st);
+    if (tuning) {
+        float best = 1e30f;
+        for (int th : {256, 512, 1024}) {
+            const float t = time_median3(st, [&] {
+                sketch_sparse<T>(cp, ri, in.Ax, n, d, hidx, (int)k, m, SA, ld, 1, colnorm, colscale, st, th);
+            });
+            if (t < best) {
+                best = t;
+                tuned.sketch_threads = th;
+            }
+        }
+    }
+    sketch_sparse<T>(cp, ri, in.Ax, n, d, hidx, (int)k, m, SA, ld, 1, colnorm, colscale, st,
+                     tuned.sketch_threads);
     sketch_rhs(bptr, bent, m, (int)k, in.b, cvec, st);
     if (mixed) {
         // LSQR's float pairs hold the equilibrated values A(:, c) / ||A(:, c)||:
@@ -343,8 +420,34 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     trace_phase(st, "sketch");
     SKL_CUDA(cudaEventRecord(ev[3], st));
     // ---- randomized CPQR, c = Q^T S b ----
+    if (tuning && mixed) {
+        // whole factorizations of a copy of the sketch at each panel width
+        T* SAc = nullptr;
+        double* cc = nullptr;
+        SKL_CUDA(cudaMallocAsync((void**)&SAc, (size_t)ld * d * sizeof(T), st));
+        SKL_CUDA(cudaMallocAsync((void**)&cc, (size_t)m * sizeof(double), st));
+        float best = 1e30f;
+        int last_nb = 0;
+        for (int cap : {64, 48, 32}) {
+            const int nbw = cpqr_panel_width(m, d, cap);
+            if (nbw == last_nb) continue;
+            last_nb = nbw;
+            const float t = time_median3(st, [&] {
+                SKL_CUDA(cudaMemcpyAsync(SAc, SA, (size_t)ld * d * sizeof(T), cudaMemcpyDeviceToDevice, st));
+                SKL_CUDA(cudaMemcpyAsync(cc, cvec, (size_t)m * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                cpqr<T>(SAc, m, d, ld, jpvt, tau, work, C.dev_status, st, cc, 1, nullptr, nbw);
+            });
+            if (t < best) {
+                best = t;
+                tuned.nb = nbw;
+            }
+        }
+        SKL_CUDA(cudaFreeAsync(SAc, st));
+        SKL_CUDA(cudaFreeAsync(cc, st));
+        SKL_CUDA(cudaMemsetAsync(C.dev_status, 0, sizeof(unsigned), st));
+    }
     cpqr<T>(SA, m, d, ld, jpvt, tau, work, C.dev_status, st, cvec, 1,
-            o.profile ? info.qr_prof_ms : nullptr);
+            o.profile ? info.qr_prof_ms : nullptr, tuned.nb);
     {
         const unsigned qs = read_status(C, st);
         if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
@@ -394,6 +497,22 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
     P.cols = jpvt; P.colscale = colscale;
     P.opscale = mixed ? nullptr : colscale;   // the float pairs are already equilibrated
     P.M = Mc; P.Mrow = Mr; P.ldm = ldm; P.r = rank; P.precision = o.precision;
+    if (tuning) {
+        P.r = rank_lsqr;
+        tune_lsqr_products(P, work, st);   // the workspace is idle between the inverse and LSQR
+        P.r = rank;
+        tuned.lanes_n = P.lanes_n;
+        tuned.lanes_t = P.lanes_t;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[tkey] = tuned;
+    } else {
+        P.lanes_n = tuned.lanes_n;
+        P.lanes_t = tuned.lanes_t;
+    }
+    info.tuned[0] = tuned.sketch_threads;
+    info.tuned[1] = tuned.nb;
+    info.tuned[2] = tuned.lanes_n;
+    info.tuned[3] = tuned.lanes_t;
     // ---- explicit sketch solution xs = D P1 M c (resolved columns only) ----
     SKL_CUDA(cudaMemsetAsync(x_dev, 0, d * sizeof(double), st));
     precond_apply(P, cvec, x_dev, ysplit, st);
@@ -543,6 +662,7 @@ static void fill_default(skl_opts* o)
     o->backward_tol = 0.0;
     o->max_refine = 3;
     o->device = 0;
+    o->autotune = 0;
 }
 
 static void validate_csc_header(const skl_csc* A)
@@ -1078,6 +1198,7 @@ void skl_finalize(void)
 {
     release_all_contexts();
     noalloc_forget_scratch();
+    tune_cache_clear();
 }
 
 }  // extern "C"

@@ -86,6 +86,8 @@ skl_status run_guarded(void (*fn)(void*), void* arg);
 void release_all_contexts();
 // Forgets skl_dht_device_noalloc's per-device scratch addresses (k_noalloc.cu).
 void noalloc_forget_scratch();
+// Clears the autotuner's per-shape-class launch choices.
+void tune_cache_clear();
 
 // ---------------------------------------------------------- k_format.cu --
 size_t scan_scratch_ints(int64_t n);
@@ -108,10 +110,13 @@ void build_buckets(const unsigned* hidx, int64_t n, int k, int64_t m, int* bptr,
 // ---------------------------------------------------------- k_sketch.cu --
 // Sparse sketch: SA (m x d, ld) = S*A with column j scaled by colscale[j]
 // (written by the kernel: 1/||A(:,j)|| if equilibrate else 1); Sb = S*b.
+// threads: block size of the one-CTA-per-column kernel (256, 512 or 1024;
+// 0 = 512), a tuning choice (S A itself is exact fixed point; the column
+// norms' summation order follows the block size).
 template <typename T>
 void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, int64_t d,
                    const unsigned* hidx, int k, int64_t m, T* SA, int64_t ld, int equilibrate,
-                   double* colnorm, double* colscale, cudaStream_t st);
+                   double* colnorm, double* colscale, cudaStream_t st, int threads = 0);
 void sketch_rhs(const int* bptr, const unsigned* bent, int64_t m, int k, const double* b,
                 double* Sb, cudaStream_t st);
 // ----------------------------------------------------------- k_dense.cu --
@@ -154,9 +159,14 @@ size_t cpqr_workspace_bytes(int64_t m, int64_t d);
 // QR sub-steps: 0 sample QRP, 1 column moves, 2 panel, 3 Q^T c, 4 W = V^T A,
 // 5 Z = T^T W, 6 A -= V Z, 7 Y/G downdate, 8 initial sample Y = G A.
 constexpr int kQrProfSlots = 9;
+// nb_cap > 0 caps the panel width (a multiple of 8; the workspace of the
+// default plan covers every smaller width).
 template <typename T>
 void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
-          unsigned* status, cudaStream_t st, double* c, int pivoting, double* qr_prof = nullptr);
+          unsigned* status, cudaStream_t st, double* c, int pivoting, double* qr_prof = nullptr,
+          int nb_cap = 0);
+// Panel width the FP32 CPQR uses for m x d under the cap.
+int cpqr_panel_width(int64_t m, int64_t d, int nb_cap);
 
 // --------------------------------------------------------------- k_tc.cu --
 // Status bit of a tensor-core kernel whose bounded mbarrier wait gave up.
@@ -222,6 +232,9 @@ struct LsqrProblem {
     const double* opscale = nullptr;
     const void* M = nullptr; const void* Mrow = nullptr; int64_t ldm = 0; int64_t r = 0;
     int precision = SKL_PREC_MIXED;
+    // lanes per CSR row (A z) and per CSC column (A^T u); 0 = by the average
+    // row / column length
+    int lanes_n = 0, lanes_t = 0;
 };
 
 struct LsqrResult {
@@ -242,6 +255,9 @@ LsqrResult lsqr_run(const LsqrProblem& P, const double* b, double tol, int64_t m
 // own); work holds lsqr_workspace_bytes(P).
 void lsqr_product(const LsqrProblem& P, char trans, const double* x, double* y,
                   const double* vscale, void* work, cudaStream_t st);
+// Autotuning: the fastest lanes-per-row / per-column of the two sparse
+// products on this problem's matrix (P.lanes_n, P.lanes_t).
+void tune_lsqr_products(LsqrProblem& P, void* work, cudaStream_t st);
 // xfull[cols[i]] = colscale[cols[i]] * (M yv)[i]; scratch holds r float2.
 void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* scratch,
                    cudaStream_t st);

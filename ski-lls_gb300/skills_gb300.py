@@ -63,7 +63,8 @@ class SklOpts(ctypes.Structure):
                 ("precision", ctypes.c_int), ("use_cpqr", ctypes.c_int),
                 ("seed_mode", ctypes.c_int), ("seed", ctypes.c_uint32), ("wisdom", ctypes.c_int),
                 ("backward_tol", ctypes.c_double), ("max_refine", ctypes.c_int64),
-                ("device", ctypes.c_int), ("stream", ctypes.c_void_p), ("profile", ctypes.c_int)]
+                ("device", ctypes.c_int), ("stream", ctypes.c_void_p), ("profile", ctypes.c_int),
+                ("autotune", ctypes.c_int)]
 
 
 class SklInfo(ctypes.Structure):
@@ -78,7 +79,7 @@ class SklInfo(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64), ("prof_ms", ctypes.c_double * 4),
                 ("prof_launches", ctypes.c_int64 * 4), ("qr_prof_ms", ctypes.c_double * 9),
                 ("sketch_refine_steps", ctypes.c_int64), ("unresolved_cols", ctypes.c_int64),
-                ("fp64_fallback", ctypes.c_int)]
+                ("fp64_fallback", ctypes.c_int), ("tuned", ctypes.c_int64 * 4)]
 
     def as_dict(self):
         out = {}
@@ -196,7 +197,7 @@ def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=AB
                    ordering=SPQR_ORDERING, it_tol=IT_TOL, max_it=MAX_IT,
                    rcond_threshold=RCOND_THRESHOLD, perturb=PERTURB, debug=0, *,
                    precision="mixed", seed=None, backward_tol=0.0, max_refine=3,
-                   rank_tol=0.0, device=0, stream=None, profile=0) -> Result:
+                   rank_tol=0.0, device=0, stream=None, profile=0, autotune=0) -> Result:
     """GPU counterpart of ls_sparse_spqr (src/ls_sparse_spqr.cpp:79-214).
 
     `ordering` and `debug` are accepted for signature parity (the GPU path
@@ -216,7 +217,7 @@ def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=AB
     o.rcond_threshold, o.perturb, o.precision = rcond_threshold, perturb, PREC[precision]
     o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
     o.backward_tol, o.max_refine, o.rank_tol, o.device = backward_tol, max_refine, rank_tol, device
-    o.stream, o.profile = stream, profile
+    o.stream, o.profile, o.autotune = stream, profile, autotune
     info = SklInfo()
     _check(lib().skl_sparse_solve(ctypes.byref(csc), _ptr(b), _ptr(x), ctypes.byref(o),
                                   ctypes.byref(info)))
@@ -226,7 +227,7 @@ def ls_sparse_spqr(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, abs_tol=AB
 def sparse_solve_device(n, d, p_ptr, i_ptr, x_ptr, b_ptr, xout_ptr, nnz, gamma, k, *,
                         precision="mixed", seed=None, it_tol=IT_TOL, max_it=MAX_IT,
                         abs_tol=ABS_TOL, backward_tol=0.0, stream=None, profile=0,
-                        device=0) -> SklInfo:
+                        device=0, autotune=0) -> SklInfo:
     """skl_sparse_solve_device on device pointers (CSC with int64 indices)."""
     csc = SklCsc(n, d, nnz, p_ptr, i_ptr, x_ptr)
     o = default_opts()
@@ -234,6 +235,7 @@ def sparse_solve_device(n, d, p_ptr, i_ptr, x_ptr, b_ptr, xout_ptr, nnz, gamma, 
     o.precision = PREC[precision]
     o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
     o.backward_tol, o.device, o.stream, o.profile = backward_tol, device, stream, profile
+    o.autotune = autotune
     info = SklInfo()
     _check(lib().skl_sparse_solve_device(ctypes.byref(csc), ctypes.c_void_p(b_ptr),
                                          ctypes.c_void_p(xout_ptr), ctypes.byref(o),
