@@ -315,14 +315,105 @@ SKL_DEV void blk_mul_t(int m, int n, int kk, const T* A, int lda, const T* B, in
     __syncthreads();
 }
 
-// 2 x 2 tiles: 4 x 4 tiles measured slower inside the small kernels (their
-// k ranges trim less under the triangular masks).
+// FP32: the same product on the warps' tensor cores, one 16 x 8 tile of C per
+// warp (mma.sync m16n8k8 TF32; a 64 x 64 result is the CTA's 32 warps), k
+// over the range the masks leave nonzero.  3xTF32 with round-to-nearest
+// splits, hi = rna(a) and lo = rna(a - hi), so hi*hi + hi*lo + lo*hi carries
+// each product to ~2^-24 like an FP32 FMA.  A 64 x 64 x 64 product is ~200
+// instructions per warp instead of ~770 per thread for the 2 x 2 register
+// tiles, and these products are most of the panel's serial b x b algebra.
+// (For a single-CTA product this small the warp-level MMA beats a tcgen05
+// launch: no tensor-memory allocation, descriptors or commit round trip.)
+SKL_DEV unsigned tf32_rna(float a)
+{
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(a));
+    return r;
+}
+
+SKL_DEV void mma_tf32_16x8x8(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2])
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+        "{%8, %9}, {%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool TA, int MA, bool TB, int MB, bool ACC>
+SKL_DEV void blk_mul_tc(int m, int n, int kk, const float* A, int lda, const float* B, int ldb,
+                        const float* __restrict__ sB, float alpha, float* C, int ldc,
+                        float* __restrict__ Cg, int ldg, float* __restrict__ tau)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, tig = lane & 3;
+    const int ntn = (n + 7) >> 3;
+    const bool act = warp < ((m + 15) >> 4) * ntn;
+    const int i0 = (warp / ntn) * 16, c0 = (warp % ntn) * 8;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (act) {
+        int klo, khi;
+        k_range<MA, MB>(i0, c0, 16, 8, kk, klo, khi);
+        klo &= ~7;
+        const int ra0 = i0 + g, ra1 = i0 + g + 8, cb = c0 + g;
+        for (int k0 = klo; k0 < khi; k0 += 8) {
+            const int ka0 = k0 + tig, ka1 = k0 + tig + 4;
+            // fragments: A (g, tig) (g+8, tig) (g, tig+4) (g+8, tig+4); B (tig, g) (tig+4, g)
+            float av[4], bv[2];
+            av[0] = (ra0 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka0) : 0.f;
+            av[1] = (ra1 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka0) : 0.f;
+            av[2] = (ra0 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka1) : 0.f;
+            av[3] = (ra1 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka1) : 0.f;
+            bv[0] = (ka0 < kk && cb < n) ? (sB ? sB[ka0] : 1.f) * op_at<float, TB, MB>(B, ldb, ka0, cb) : 0.f;
+            bv[1] = (ka1 < kk && cb < n) ? (sB ? sB[ka1] : 1.f) * op_at<float, TB, MB>(B, ldb, ka1, cb) : 0.f;
+            unsigned ah[4], al[4], bh[2], bl[2];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                ah[e] = tf32_rna(av[e]);
+                al[e] = tf32_rna(av[e] - __uint_as_float(ah[e]));
+            }
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                bh[e] = tf32_rna(bv[e]);
+                bl[e] = tf32_rna(bv[e] - __uint_as_float(bh[e]));
+            }
+            mma_tf32_16x8x8(acc, al, bh);
+            mma_tf32_16x8x8(acc, ah, bl);
+            mma_tf32_16x8x8(acc, ah, bh);
+        }
+    }
+    __syncthreads();
+    if (act) {
+        // C fragment: (g, 2 tig) (g, 2 tig + 1) (g + 8, 2 tig) (g + 8, 2 tig + 1)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int i = i0 + g + (e >> 1) * 8, c = c0 + 2 * tig + (e & 1);
+            if (i >= m || c >= n) continue;
+            const float v = alpha * acc[e];
+            if (Cg) {
+                Cg[i + (int64_t)c * ldg] = v;
+                if (i == c) tau[i] = v;
+            } else if (ACC) {
+                C[i * ldc + c] += v;
+            } else {
+                C[i * ldc + c] = v;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// 2 x 2 tiles for FP64: 4 x 4 tiles measured slower inside the small kernels
+// (their k ranges trim less under the triangular masks).
 template <typename T, bool TA, int MA, bool TB, int MB, bool ACC = false>
 SKL_DEV void blk_mul(int m, int n, int kk, const T* A, int lda, const T* B, int ldb,
                      const T* __restrict__ sB, T alpha, T* C, int ldc, T* __restrict__ Cg = nullptr,
                      int ldg = 0, T* __restrict__ tau = nullptr)
 {
-    blk_mul_t<T, TA, MA, TB, MB, ACC, 2>(m, n, kk, A, lda, B, ldb, sB, alpha, C, ldc, Cg, ldg, tau);
+    if constexpr (std::is_same<T, float>::value)
+        blk_mul_tc<TA, MA, TB, MB, ACC>(m, n, kk, A, lda, B, ldb, sB, alpha, C, ldc, Cg, ldg, tau);
+    else
+        blk_mul_t<T, TA, MA, TB, MB, ACC, 2>(m, n, kk, A, lda, B, ldb, sB, alpha, C, ldc, Cg, ldg, tau);
 }
 
 // Off-diagonal blocks of X = U^{-1} (np x np upper, np a multiple of 16)

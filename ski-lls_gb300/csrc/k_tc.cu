@@ -5,11 +5,11 @@
 // 547-550): V is the M x b panel of Householder vectors (b <= 64), A the
 // M x N trailing matrix, W is b x N.  FP32 data, 3xTF32 arithmetic on the
 // 5th-generation tensor cores:  a = hi(a) + lo(a) with hi = a rounded to the
-// nearest TF32 value and lo = a - hi (exact), and
+// nearest TF32 value and lo = a - hi rounded to the nearest TF32 value, and
 //     V^T A ~ hi(V)^T hi(A) + lo(V)^T hi(A) + hi(V)^T lo(A)
-// accumulated in FP32 in tensor memory (each product within ~2^-23 of its
-// magnitude: the dropped lo*lo term and the tensor core's truncation of lo,
-// against 2^-24 for an FP32 FMA).
+// accumulated in FP32 in tensor memory (each product within ~2^-24 of its
+// magnitude, like an FP32 FMA: the dropped lo*lo term and lo's own rounding
+// are each at most 2^-24).
 //
 // One CTA owns 128 columns of A and a range of K (rows of A and V); the MMA
 // computes D[128 x 64] = A_tile^T V_tile (M = 128 columns of A, N = 64
@@ -171,10 +171,9 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32])
     for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-// a rounded to the nearest TF32 value (low 13 significand bits zero), so
-// lo = a - hi is exact with |lo| <= 2^-12 |a|: hi and lo carry 2 x 11 bits
-// of a's 24, and the truncation of lo's own low bits by the tensor core
-// costs at most 2^-23 |a| per product.
+// a rounded to the nearest TF32 value (low 13 significand bits zero).  The
+// splits are hi = rna(a) and lo = rna(a - hi): both exact TF32 operands, with
+// |a - hi - lo| <= 2^-24 |a|, so the three products carry ~2^-24 per term.
 __device__ __forceinline__ float tf32_hi(float a)
 {
     unsigned r;
@@ -308,10 +307,10 @@ k_tc_vta(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                 const int e = t + q * 128;
                 const float4 v = h[e];
                 float4 hi, lo;
-                hi.x = tf32_hi(v.x); lo.x = v.x - hi.x;
-                hi.y = tf32_hi(v.y); lo.y = v.y - hi.y;
-                hi.z = tf32_hi(v.z); lo.z = v.z - hi.z;
-                hi.w = tf32_hi(v.w); lo.w = v.w - hi.w;
+                hi.x = tf32_hi(v.x); lo.x = tf32_hi(v.x - hi.x);
+                hi.y = tf32_hi(v.y); lo.y = tf32_hi(v.y - hi.y);
+                hi.z = tf32_hi(v.z); lo.z = tf32_hi(v.z - hi.z);
+                hi.w = tf32_hi(v.w); lo.w = tf32_hi(v.w - hi.w);
                 h[e] = hi;
                 l[e] = lo;
             }
@@ -382,7 +381,7 @@ __global__ void k_tc_split_v(const float* __restrict__ V, int64_t ldv, int M, in
         const float a = V[i + (int64_t)c * ldv];
         const float h = tf32_hi(a);
         Vh[i + (int64_t)c * ldvs] = h;
-        Vl[i + (int64_t)c * ldvs] = a - h;
+        Vl[i + (int64_t)c * ldvs] = tf32_hi(a - h);
     }
 }
 
@@ -594,14 +593,14 @@ __global__ void k_tc_split_vz(const float* __restrict__ V, int64_t ldv, int M, i
             const float a = V[i + (int64_t)c * ldv];
             const float h = tf32_hi(a);
             Vth[(int64_t)i * kTN + c] = h;
-            Vtl[(int64_t)i * kTN + c] = a - h;
+            Vtl[(int64_t)i * kTN + c] = tf32_hi(a - h);
         } else {
             const int64_t f = e - nv;
             const int c = (int)(f % b), n = (int)(f / b);
             const float a = Z[c + (int64_t)n * ldz];
             const float h = tf32_hi(a);
             Zth[c + (int64_t)n * kTN] = h;
-            Ztl[c + (int64_t)n * kTN] = a - h;
+            Ztl[c + (int64_t)n * kTN] = tf32_hi(a - h);
         }
     }
 }
