@@ -595,6 +595,122 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
     }
 }
 
+// ------------------------------------------------ spmv_t by rows (mixed) --
+// t = A^T u on the CSR copy: the columns' dot products of k_spmv_t_csc wait on
+// dependent gathers of u from L2 (27 stall cycles per instruction measured);
+// by rows, u is read once per row and A's row streams in order.  Every block
+// scatters its rows' products a_ij u_i into a shared-memory accumulator over
+// all d columns in 64-bit fixed point, so the sums are exact and do not depend
+// on the order of the atomics; k_spmv_t_finish adds the blocks' accumulators
+// in a fixed order and applies the pivoted column selection.  Scale: the stored
+// values are equilibrated (||A(:, j)|| = 1 on the mixed path) and ||uh|| =
+// beta, so every partial sum is below beta in magnitude (Cauchy-Schwarz) and
+// 2^sh with beta < 2^(60 - sh) keeps it below 2^60; each term is rounded to a
+// multiple of 2^-sh, an error below 2^-61 beta per term, under the float-float
+// products' 2^-48 |a_ij u_i|.
+constexpr int kRowsThreads = 1024;
+
+SKL_DEV int rows_shift(double beta)
+{
+    int e = 0;
+    frexp(beta > 0.0 ? beta : 1.0, &e);
+    return 60 - e;
+}
+
+template <int L>
+__global__ void __launch_bounds__(kRowsThreads, 1)
+k_spmv_t_rows(const int* __restrict__ rp, const int* __restrict__ ci, const float2* __restrict__ cv,
+              int n, int d, int rows_per_block, const float2* __restrict__ us,
+              unsigned long long* __restrict__ acc_out, const LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    extern __shared__ unsigned long long acc[];   // d entries
+    for (int j = threadIdx.x; j < d; j += blockDim.x) acc[j] = 0ull;
+    const int sh = rows_shift(S->beta);
+    __syncthreads();
+    const int lane = threadIdx.x % L, grp = threadIdx.x / L, ngrp = blockDim.x / L;
+    const int r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
+    int i = r0 + grp;
+    // the next row's pointers and u are loaded before the current row's entries are used
+    int p0 = 0, p1 = 0;
+    float2 uu = make_float2(0.f, 0.f);
+    if (i < r1) {
+        p0 = rp[i];
+        p1 = rp[i + 1];
+        uu = us[i];
+    }
+    while (i < r1) {
+        const int ni = i + ngrp;
+        int np0 = 0, np1 = 0;
+        float2 nu = make_float2(0.f, 0.f);
+        if (ni < r1) {
+            np0 = rp[ni];
+            np1 = rp[ni + 1];
+            nu = us[ni];
+        }
+        for (int p = p0 + lane; p < p1; p += 4 * L) {
+            int c[4];
+            float2 a[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = p + k * L;
+                const bool ok = q < p1;
+                c[k] = ok ? ci[q] : -1;
+                a[k] = ok ? cv[q] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (c[k] < 0) continue;
+                // a u as a float pair, then both parts to fixed point
+                const float ph = __fmul_rn(a[k].x, uu.x);
+                const float pe = __fmaf_rn(a[k].x, uu.x, -ph);
+                const float pl = __fmaf_rn(a[k].x, uu.y, __fmaf_rn(a[k].y, uu.x, pe));
+                const long long q = __float2ll_rn(ldexpf(ph, sh)) + __float2ll_rn(ldexpf(pl, sh));
+                atomicAdd(&acc[c[k]], (unsigned long long)q);
+            }
+        }
+        i = ni;
+        p0 = np0;
+        p1 = np1;
+        uu = nu;
+    }
+    __syncthreads();
+    unsigned long long* out = acc_out + (int64_t)blockIdx.x * d;
+    for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = acc[j];
+}
+
+// t[colpos[c]] = opscale(c) (sum over blocks of acc[c]) 2^-sh / beta, columns in
+// natural order (coalesced reads of the blocks' accumulators), blocks summed in
+// order (exact in 64-bit integers).
+__global__ void __launch_bounds__(kLThreads)
+k_spmv_t_finish(const unsigned long long* __restrict__ acc_in, int nblk, int d,
+                const int* __restrict__ colpos, const double* __restrict__ colscale,
+                float2* __restrict__ t, const LsqrState* __restrict__ S)
+{
+    if (S->done) return;
+    const int sh = rows_shift(S->beta);
+    const double ib = S->ib;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d; c += gridDim.x * blockDim.x) {
+        const int i = colpos[c];
+        if (i < 0) continue;
+        long long s = 0;
+        for (int z = 0; z < nblk; ++z) s += (long long)acc_in[(int64_t)z * d + c];
+        const double v = ldexp((double)s, -sh) * ib * (colscale ? colscale[c] : 1.0);
+        t[i] = store_val<true>(v);
+    }
+}
+
+__global__ void k_colpos(int d, int* __restrict__ colpos)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d; c += gridDim.x * blockDim.x)
+        colpos[c] = -1;
+}
+__global__ void k_colpos_set(const int* __restrict__ cols, int r, int* __restrict__ colpos)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x)
+        colpos[cols[i]] = i;
+}
+
 // ------------------------------------------------- dense A (column-major) --
 // spmv_n: uh = A(:, cols) z(cols) - coef uh.  Block = 256 rows x all columns
 // of its column chunk; chunk partials are combined by spmv_n_dense_reduce.
@@ -795,7 +911,43 @@ struct LsqrBufs {
     double *uh, *vh, *w, *y, *partials, *dpart;
     void *us, *vs, *t, *z;
     int nparts;
+    unsigned long long* racc;   // A^T u by rows: per-block column accumulators
+    int* colpos;                // column -> position among the selected columns, or -1
 };
+
+// Blocks of the row-wise A^T u: one 1024-thread block per SM, each with a
+// shared accumulator over all d columns (so d * 8 bytes must fit).
+static int rows_blocks()
+{
+    static const int v = [] {
+        int dev = 0, s = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+        return s > 0 ? s : 148;
+    }();
+    return v;
+}
+
+static bool rows_kernel_fits(int64_t d)
+{
+    static const int optin = [] {
+        int dev = 0, o = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return o;
+    }();
+    return d * 8 + 1024 <= optin;
+}
+
+// A^T u by rows on the mixed sparse path (SKILLS_ATU_ROWS=1; otherwise the CSC kernel)
+static bool use_rows_atu(const LsqrProblem& P)
+{
+    static const bool on = [] {
+        const char* e = getenv("SKILLS_ATU_ROWS");
+        return e && e[0] == '1';
+    }();
+    return on && P.precision == SKL_PREC_MIXED && !P.Ad && P.rp && rows_kernel_fits(P.d);
+}
 
 // lanes per row/column so that each lane handles about four nonzeros
 static int lanes_for(double avg)
@@ -827,6 +979,8 @@ size_t lsqr_workspace_bytes(const LsqrProblem& P)
     int64_t nb = spmv_n_blocks(P);
     b += (nb + 4096) * sizeof(double) + 256;                 // partials
     if (P.Ad) b += (size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double) + 256;
+    b += (size_t)rows_blocks() * P.d * 8 + 256;              // row-wise A^T u accumulators
+    b += P.d * sizeof(int) + 256;                             // colpos
     return b;
 }
 
@@ -855,7 +1009,20 @@ static LsqrBufs carve(const LsqrProblem& P, void* work)
     B.partials = (double*)take(B.nparts * sizeof(double));
     B.dpart = P.Ad ? (double*)take((size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double))
                    : nullptr;
+    B.racc = (unsigned long long*)take((size_t)rows_blocks() * P.d * 8);
+    B.colpos = (int*)take(P.d * sizeof(int));
     return B;
+}
+
+// colpos[c] = i for c = cols[i], i < r; -1 for the other columns
+static void prepare_colpos(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
+{
+    if (P.d <= 0) return;
+    const unsigned g = (unsigned)std::min<int64_t>((P.d + 255) / 256, 152);
+    k_colpos<<<g, 256, 0, st>>>((int)P.d, B.colpos);
+    k_colpos_set<<<g, 256, 0, st>>>(P.cols, (int)P.r, B.colpos);
+    SKL_LAUNCHED();
+    SKL_LAUNCHED();
 }
 
 template <bool MIXED>
@@ -907,6 +1074,30 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
                                                        (V*)B.t, B.S);
         SKL_LAUNCHED();
         return;
+    }
+    if constexpr (MIXED) {
+        if (use_rows_atu(P)) {
+            const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(rows_blocks(), (P.n + 63) / 64));
+            const int rpb = (int)((P.n + nblk - 1) / nblk);
+            const double avgr = P.n ? (double)P.nnz / P.n : 0.0;
+            const int Lr = P.lanes_t ? P.lanes_t : lanes_for(avgr);
+            const size_t smem = (size_t)P.d * 8;
+#define SPMV_TR(LL) do { \
+            if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_spmv_t_rows<LL>); \
+            k_spmv_t_rows<LL><<<nblk, kRowsThreads, smem, st>>>(P.rp, P.ci, (const float2*)P.cx, (int)P.n, (int)P.d, rpb, (const float2*)B.us, B.racc, B.S); \
+        } while (0)
+            if (Lr == 32) SPMV_TR(32);
+            else if (Lr == 16) SPMV_TR(16);
+            else if (Lr == 8) SPMV_TR(8);
+            else SPMV_TR(4);
+#undef SPMV_TR
+            const unsigned gf = (unsigned)std::min<int64_t>((P.d + kLThreads - 1) / kLThreads, 152 * 4);
+            k_spmv_t_finish<<<gf, kLThreads, 0, st>>>(B.racc, nblk, (int)P.d, B.colpos, P.opscale,
+                                                      (float2*)B.t, B.S);
+            SKL_LAUNCHED();
+            SKL_LAUNCHED();
+            return;
+        }
     }
     const double avg = P.d ? (double)P.nnz / P.d : 0.0;
     const int L = P.lanes_t ? P.lanes_t : lanes_for(avg);
@@ -968,6 +1159,7 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     using V = ValT<MIXED>;
     using MT = MatT<MIXED>;
     LsqrBufs B = carve(P, work);
+    prepare_colpos(P, B, st);
     LsqrState init{};
     init.tol = tol;
     init.max_it = max_it;
@@ -1074,8 +1266,10 @@ void tune_lsqr_products(LsqrProblem& P, void* work, cudaStream_t st)
 {
     if (P.Ad || P.n <= 0 || P.r <= 0) return;
     LsqrBufs B = carve(P, work);
+    prepare_colpos(P, B, st);
     LsqrState init{};
     init.ib = 1.0;
+    init.beta = 1.0;
     const size_t vsz = P.precision == SKL_PREC_MIXED ? sizeof(float2) : sizeof(double);
     SKL_CUDA(cudaMemcpyAsync(B.S, &init, sizeof(LsqrState), cudaMemcpyHostToDevice, st));
     SKL_CUDA(cudaMemsetAsync(B.uh, 0, P.n * sizeof(double), st));
@@ -1147,14 +1341,27 @@ __global__ void k_prod_out(const ValT<MIXED>* __restrict__ v, const double* __re
     }
 }
 
+// S->beta = ||x|| (one block): the scale of the row-wise A^T u
+__global__ void __launch_bounds__(kLThreads)
+k_beta_norm(const double* __restrict__ x, int64_t n, LsqrState* __restrict__ S)
+{
+    __shared__ double red[kLThreads / 32];
+    double ss = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss += x[i] * x[i];
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) S->beta = sqrt(ss);
+}
+
 template <bool MIXED>
 static void product_impl(const LsqrProblem& P, char trans, const double* x, double* y,
                          const double* vscale, void* work, cudaStream_t st)
 {
     using V = ValT<MIXED>;
     LsqrBufs B = carve(P, work);
+    prepare_colpos(P, B, st);
     LsqrState init{};
     init.ib = 1.0;   // t = A^T u / beta with beta = 1; coef_n = 0: u = A z
+    init.beta = 1.0;
     SKL_CUDA(cudaMemcpyAsync(B.S, &init, sizeof(LsqrState), cudaMemcpyHostToDevice, st));
     SKL_CUDA(cudaMemsetAsync(B.uh, 0, P.n * sizeof(double), st));
     SKL_CUDA(cudaMemsetAsync(B.us, 0, P.n * sizeof(V), st));
@@ -1165,6 +1372,8 @@ static void product_impl(const LsqrProblem& P, char trans, const double* x, doub
         k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.us, MIXED ? nullptr : B.uh, P.n, nullptr, y);
     } else {
         k_prod_in<MIXED><<<g, 256, 0, st>>>(x, P.n, nullptr, (V*)B.us);
+        k_beta_norm<<<1, kLThreads, 0, st>>>(x, P.n, B.S);
+        SKL_LAUNCHED();
         launch_spmv_t<MIXED>(P, B, st);
         k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.t, nullptr, P.r, vscale, y);
     }
