@@ -12,6 +12,7 @@
 // Fisher-Yates shuffle of a permutation array that persists across columns;
 // all n*k signs are drawn after all rows.  The shuffle is inherently serial,
 // so it runs on the host while the device copies and converts A.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -136,37 +137,19 @@ void rng_srand(uint32_t seed)
     g_seeded = true;
 }
 
-// Caller holds the lock (rng_lock).  The n*k sign draws follow the n*k row
-// draws in the stream; they are drawn on a second thread from the state
-// jumped n*k draws ahead while this thread runs the (serial) row shuffle.
+// Caller holds the lock (rng_lock).  The stream gives n*k row draws, then
+// n*k sign draws.  Only the Fisher-Yates swaps are serial; the draws
+// themselves are not, so for large n*k worker threads start from the state
+// jumped to their chunk of the stream and turn its words into swap targets
+// t = word % (m - j) + j and sign bits, and this thread then runs the swaps
+// over the precomputed targets.
 void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
 {
     const int64_t nk = n * k;
-    std::vector<uint8_t> neg;
-    Rng after_rows = g_rng;
-    std::thread signs;
-    const bool split = nk >= (int64_t)1 << 15;
-    if (split) {
-        after_rows = g_rng.jumped((uint64_t)nk);
-        neg.resize((size_t)nk);
-        signs = std::thread([&neg, &after_rows, nk]() {
-            for (int64_t q = 0; q < nk; ++q)
-                neg[(size_t)q] = (after_rows.next() & 1u) == 0u;   // rand()%2 == 0 -> -1
-        });
-    }
     std::vector<uint32_t> perm((size_t)m);
     for (int64_t i = 0; i < m; ++i) perm[(size_t)i] = (uint32_t)i;
     uint32_t* pa = perm.data();
-    if (k == 1) {
-        const uint32_t mm = (uint32_t)m;
-        for (int64_t i = 0; i < n; ++i) {
-            uint32_t t = g_rng.next() % mm;
-            uint32_t a = pa[t];
-            pa[t] = pa[0];
-            pa[0] = a;
-            hidx[i] = a;
-        }
-    } else {
+    if (nk < ((int64_t)1 << 15)) {
         for (int64_t i = 0; i < n; ++i) {
             uint32_t* out = hidx + i * k;
             for (int64_t j = 0; j < k; ++j) {
@@ -177,16 +160,54 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
                 out[j] = a;
             }
         }
-    }
-    if (split) {
-        signs.join();
-        for (int64_t q = 0; q < nk; ++q)
-            if (neg[(size_t)q]) hidx[q] |= 0x80000000u;
-        g_rng = after_rows;   // the stream continues after both draw sequences
-    } else {
         for (int64_t q = 0; q < nk; ++q)
             if ((g_rng.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
+        return;
     }
+    // tt[s]: swap target of draw s, with the sign in bit 31 (set = -1)
+    std::vector<uint32_t> tt((size_t)nk);
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t nthr = std::max<int64_t>(1, std::min<int64_t>({(int64_t)(hw ? hw : 4), 16, nk >> 14}));
+    const int64_t chunk = (nk + nthr - 1) / nthr;
+    const Rng base = g_rng;
+    auto work = [&](int64_t c) {
+        const int64_t s0 = c * chunk, s1 = std::min(nk, s0 + chunk);
+        if (s0 >= s1) return;
+        Rng rows = base.jumped((uint64_t)s0);
+        int64_t j = s0 % k;
+        for (int64_t s = s0; s < s1; ++s) {
+            tt[(size_t)s] = (uint32_t)(rows.next() % (uint32_t)(m - j)) + (uint32_t)j;
+            if (++j == k) j = 0;
+        }
+        Rng signs = base.jumped((uint64_t)(nk + s0));
+        for (int64_t s = s0; s < s1; ++s)
+            if ((signs.next() & 1u) == 0u) tt[(size_t)s] |= 0x80000000u;   // rand()%2 == 0 -> -1
+    };
+    std::vector<std::thread> pool;
+    for (int64_t c = 1; c < nthr; ++c) pool.emplace_back(work, c);
+    work(0);
+    for (auto& t : pool) t.join();
+    const uint32_t* tp = tt.data();
+    if (k == 1) {
+        for (int64_t s = 0; s < nk; ++s) {
+            const uint32_t w = tp[s], t = w & 0x7fffffffu;
+            const uint32_t a = pa[t];
+            pa[t] = pa[0];
+            pa[0] = a;
+            hidx[s] = a | (w & 0x80000000u);
+        }
+    } else {
+        int64_t j = 0;
+        for (int64_t s = 0; s < nk; ++s) {
+            const uint32_t w = tp[s], t = w & 0x7fffffffu;
+            const uint32_t a = pa[t];
+            pa[t] = pa[j];
+            pa[j] = a;
+            hidx[s] = a | (w & 0x80000000u);
+            if (++j == k) j = 0;
+        }
+    }
+    g_rng = base.jumped((uint64_t)(2 * nk));   // the stream continues after both draw sequences
 }
 
 // Caller holds the lock.

@@ -69,9 +69,9 @@ def test_hash_stream_continues_like_global_rand():
 
 
 def test_hash_stream_large_draws_split_across_threads():
-    # n*k >= 2^15: the sign draws run on a second thread from the generator
-    # state jumped n*k draws ahead; rows, signs and the continuing stream must
-    # stay identical to one sequential stream
+    # n*k >= 2^15: worker threads draw the swap targets and signs from the
+    # generator state jumped to their chunk of the stream; rows, signs and the
+    # continuing stream must stay identical to one sequential stream
     skl.srand(7)
     a_rows, a_vals = skl.hash_generate(8500, 30000, 2)
     b_rows, b_vals = skl.hash_generate(900, 40000, 1)
@@ -82,6 +82,20 @@ def test_hash_stream_large_draws_split_across_threads():
     np.testing.assert_array_equal(a_vals, v1)
     np.testing.assert_array_equal(b_rows, r2)
     np.testing.assert_array_equal(b_vals, v2)
+
+
+def test_hash_stream_chunked_draws_k3():
+    # n*k = 300,009: up to 16 worker chunks whose starts fall inside a column
+    # (chunk start not a multiple of k), then the stream continues
+    skl.srand(11)
+    a_rows, a_vals = skl.hash_generate(15000, 100003, 3)
+    c_rows, _ = skl.hash_generate(40, 25, 3)
+    g = orc.Rng(11)
+    r1, v1 = orc.gen_hashing(g, 15000, 100003, 3)
+    r3, _ = orc.gen_hashing(g, 40, 25, 3)
+    np.testing.assert_array_equal(a_rows, r1)
+    np.testing.assert_array_equal(a_vals, v1)
+    np.testing.assert_array_equal(c_rows, r3)
 
 
 def test_hash_rejects_bad_sizes():
