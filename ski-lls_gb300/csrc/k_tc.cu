@@ -370,223 +370,6 @@ k_tc_vta(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
     }
 }
 
-// ---- W = V^T A, six stages: A's lo part in tensor memory --------------------
-// The same product as k_tc_vta with a deeper pipeline: a stage in shared memory
-// holds only the TMA'd A tile (split to hi in place) and V's hi / lo tiles
-// (32 KB instead of 48), because the converter warps store A's lo part in a
-// TMEM ring (tcgen05.st) and the lo(A)^T hi(V) MMA reads its A operand from
-// tensor memory.  Six stages keep 96 KB of A per SM in flight instead of 64.
-// Converter warp w splits rows (columns of A) 32 (w & 3) .. +31 of the tile,
-// one row per thread: the row's 8 16-byte chunks sit at chunk position
-// j ^ (row & 7) of its 128 bytes (the TMA's 128-byte swizzle).
-constexpr int kStages6 = 6;
-constexpr int kStage6Bytes = kABytes + 2 * kVBytes;
-constexpr int kSmem6Bytes = kStages6 * kStage6Bytes + 1024 + 1024;
-constexpr unsigned kTmem6Cols = 512;     // accumulators: columns 0..127; lo ring: 128 + 32 s
-constexpr unsigned kLoCol0 = 2 * kTN;
-
-__device__ __forceinline__ void tmem_st32(unsigned taddr, const float (&v)[32])
-{
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
-        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
-        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
-        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])),
-        "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])),
-        "r"(__float_as_uint(v[20])), "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
-        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])), "r"(__float_as_uint(v[27])),
-        "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])), "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
-        : "memory");
-    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-}
-
-// D += A B with A (M x K) read from tensor memory, B from shared memory
-__device__ __forceinline__ void mma_tf32_tmem_a(unsigned d_tmem, unsigned a_tmem, uint64_t b, uint32_t idesc,
-                                                unsigned accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__global__ void __launch_bounds__(kTcThreads, 1)
-k_tc_vta6(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapVh,
-          const __grid_constant__ CUtensorMap mapVl, int N, int b, int kb_per, int kb_total,
-          float* __restrict__ partial, unsigned* __restrict__ status)
-{
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages6 * kStage6Bytes);
-    // bars: full[6], conv[6], empty[6], tfull[2], tempty[2], done; then the TMEM address
-    unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + 3 * kStages6 + 5);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int col0 = blockIdx.x * kTM;
-    const int kb0 = blockIdx.y * kb_per;
-    const int nkb = min(kb_per, kb_total - kb0);
-    const int ngroups = (nkb + kGroup - 1) / kGroup;
-    auto full = [&](int s) { return smem_u32(bars + s); };
-    auto conv = [&](int s) { return smem_u32(bars + kStages6 + s); };
-    auto empty = [&](int s) { return smem_u32(bars + 2 * kStages6 + s); };
-    auto tfull = [&](int q) { return smem_u32(bars + 3 * kStages6 + q); };
-    auto tempty = [&](int q) { return smem_u32(bars + 3 * kStages6 + 2 + q); };
-    const unsigned done = smem_u32(bars + 3 * kStages6 + 4);
-    auto a_hi = [&](int s) { return smem + s * kStage6Bytes; };
-    auto v_hi = [&](int s) { return smem + s * kStage6Bytes + kABytes; };
-    auto v_lo = [&](int s) { return smem + s * kStage6Bytes + kABytes + kVBytes; };
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages6; ++s) {
-            mbar_init(full(s), 1);
-            mbar_init(conv(s), 128);
-            mbar_init(empty(s), 1);
-        }
-        for (int q = 0; q < 2; ++q) {
-            mbar_init(tfull(q), 1);
-            mbar_init(tempty(q), 256);
-        }
-        mbar_init(done, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(kTmem6Cols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const unsigned tmem = *tmem_slot;
-
-    if (warp == 0) {
-        if (lane == 0) {
-            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
-            bool ok = true;
-            int issued = 0;
-            for (int kb = 0; kb < nkb && ok; ++kb) {
-                const int s = kb % kStages6;
-                if (kb >= kStages6) ok = mbar_wait(empty(s), ((kb / kStages6) - 1) & 1, status);
-                if (!ok) break;
-                mbar_expect_tx(full(s), kTxBytes);
-                const int krow = (kb0 + kb) * kBK;
-                tma_load_2d(smem_u32(a_hi(s)), &mapA, krow, col0, full(s));
-                tma_load_2d(smem_u32(v_hi(s)), &mapVh, krow, 0, full(s));
-                tma_load_2d(smem_u32(v_lo(s)), &mapVl, krow, 0, full(s));
-                ++issued;
-            }
-            for (int kb = std::max(0, issued - kStages6); kb < issued; ++kb)
-                mbar_wait(full(kb % kStages6), (kb / kStages6) & 1, status);
-        }
-    } else if (warp == 1) {
-        if (lane == 0) {
-            constexpr uint32_t idesc = tf32_idesc(kTM, kTN);
-            bool ok = true;
-            for (int kb = 0; kb < nkb && ok; ++kb) {
-                const int s = kb % kStages6;
-                const int g = kb / kGroup, buf = g & 1;
-                const bool first = (kb % kGroup) == 0;
-                if (first && g >= 2) ok = mbar_wait(tempty(buf), ((g >> 1) - 1) & 1, status);
-                if (ok) ok = mbar_wait(conv(s), (kb / kStages6) & 1, status);
-                if (!ok) break;
-                tc_fence_after();
-                const unsigned d = tmem + (unsigned)(buf * kTN);
-                const unsigned lo = tmem + kLoCol0 + (unsigned)(s * kBK);
-                const unsigned ah = smem_u32(a_hi(s));
-                const unsigned vh = smem_u32(v_hi(s)), vl = smem_u32(v_lo(s));
-#pragma unroll
-                for (int k8 = 0; k8 < kBK / 8; ++k8) {
-                    const unsigned off = k8 * 32;
-                    mma_tf32_tmem_a(d, lo + (unsigned)(k8 * 8), sw128_desc(vh + off), idesc,
-                                    (first && k8 == 0) ? 0u : 1u);
-                    mma_tf32(d, sw128_desc(ah + off), sw128_desc(vl + off), idesc, 1u);
-                    mma_tf32(d, sw128_desc(ah + off), sw128_desc(vh + off), idesc, 1u);
-                }
-                mma_commit(empty(s));
-                if ((kb % kGroup) == kGroup - 1 || kb == nkb - 1) mma_commit(tfull(buf));
-            }
-            mma_commit(done);
-            mbar_wait(done, 0, status);
-        }
-    } else if (warp < 6) {
-        // warps 2..5: row r of the stage's A tile -> hi in place, lo to the TMEM ring
-        const int quad = warp & 3;
-        const int r = quad * 32 + lane;
-        bool ok = true;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kStages6;
-            ok = __all_sync(0xffffffffu, mbar_wait(full(s), (kb / kStages6) & 1, status));
-            if (!ok) break;   // warp-uniform: tcgen05.st is warp-collective
-            float4* row = reinterpret_cast<float4*>(a_hi(s) + r * 128);
-            float lo[32];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                float4* p = row + (j ^ (r & 7));
-                const float4 v = *p;
-                float4 hi;
-                hi.x = tf32_hi(v.x); lo[4 * j + 0] = tf32_hi(v.x - hi.x);
-                hi.y = tf32_hi(v.y); lo[4 * j + 1] = tf32_hi(v.y - hi.y);
-                hi.z = tf32_hi(v.z); lo[4 * j + 2] = tf32_hi(v.z - hi.z);
-                hi.w = tf32_hi(v.w); lo[4 * j + 3] = tf32_hi(v.w - hi.w);
-                *p = hi;
-            }
-            tmem_st32(tmem + ((unsigned)(quad * 32) << 16) + kLoCol0 + (unsigned)(s * kBK), lo);
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            tc_fence_before();
-            mbar_arrive(conv(s));
-        }
-    } else {
-        // warps 6..13: drain the accumulators, as in k_tc_vta
-        const int quad = warp & 3;
-        const int half = (warp - 6) >> 2;
-        float sum[32], comp[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) sum[q] = comp[q] = 0.f;
-        bool ok = true;
-        for (int g = 0; g < ngroups; ++g) {
-            const int buf = g & 1;
-            ok = __all_sync(0xffffffffu, mbar_wait(tfull(buf), (g >> 1) & 1, status));
-            if (!ok) break;
-            tc_fence_after();
-            float v[32];
-            tmem_ld32(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(buf * kTN + half * 32), v);
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                const float y = __fsub_rn(v[q], comp[q]);
-                const float t2 = __fadd_rn(sum[q], y);
-                comp[q] = __fsub_rn(__fsub_rn(t2, sum[q]), y);
-                sum[q] = t2;
-            }
-            tc_fence_before();
-            mbar_arrive(tempty(buf));
-        }
-        const int col = col0 + quad * 32 + lane;
-        if (ok && nkb > 0 && col < N) {
-            float* out = partial + (int64_t)blockIdx.y * b * N + (int64_t)col * b + half * 32;
-            if (b == kTN) {
-#pragma unroll
-                for (int q = 0; q < 32; q += 4)
-                    *reinterpret_cast<float4*>(out + q) = make_float4(sum[q], sum[q + 1], sum[q + 2], sum[q + 3]);
-            } else {
-#pragma unroll
-                for (int q = 0; q < 32; ++q)
-                    if (half * 32 + q < b) out[q] = sum[q];
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 1) {
-        __syncwarp();
-        tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmem6Cols)
-                     : "memory");
-    }
-}
-
 // V (M x b, ldv) -> hi / lo (M x b, ldvs)
 __global__ void k_tc_split_v(const float* __restrict__ V, int64_t ldv, int M, int b,
                              float* __restrict__ Vh, float* __restrict__ Vl, int64_t ldvs)
@@ -914,18 +697,9 @@ void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, in
     static std::once_flag attr_once;
     std::call_once(attr_once, [] {
         cudaFuncSetAttribute((const void*)k_tc_vta, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        cudaFuncSetAttribute((const void*)k_tc_vta6, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem6Bytes);
     });
-    static const bool six = [] {
-        const char* e = getenv("SKILLS_TC_VTA6");
-        return e && e[0] == '1';
-    }();
-    if (six)
-        k_tc_vta6<<<dim3(ntile, splits), kTcThreads, kSmem6Bytes, st>>>(mA, mVh, mVl, N, b, kb_per,
-                                                                      kb_total, out, status);
-    else
-        k_tc_vta<<<dim3(ntile, splits), kTcThreads, kSmemBytes, st>>>(mA, mVh, mVl, N, b, kb_per, kb_total,
-                                                                    out, status);
+    k_tc_vta<<<dim3(ntile, splits), kTcThreads, kSmemBytes, st>>>(mA, mVh, mVl, N, b, kb_per, kb_total,
+                                                                out, status);
     SKL_LAUNCHED();
     if (splits > 1) splitk_reduce_launch<float>(b, N, splits, 1.0f, partial, 0.0f, W, b, st);
 }
