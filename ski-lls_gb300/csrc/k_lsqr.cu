@@ -595,141 +595,62 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
     }
 }
 
-// ------------------------------------------------ spmv_t by rows (mixed) --
-// t = A^T u on the CSR copy: the columns' dot products of k_spmv_t_csc wait on
-// dependent gathers of u from L2 (27 stall cycles per instruction measured);
-// by rows, u is read once per row and A's row streams in order.  Every block
-// scatters its rows' products a_ij u_i into a shared-memory accumulator over
-// all d columns in 64-bit fixed point, so the sums are exact and do not depend
-// on the order of the atomics; k_spmv_t_finish adds the blocks' accumulators
-// in a fixed order and applies the pivoted column selection.  Scale: the stored
-// values are equilibrated (||A(:, j)|| = 1 on the mixed path) and ||uh|| =
-// beta, so every partial sum is below beta in magnitude (Cauchy-Schwarz) and
-// 2^sh with beta < 2^(60 - sh) keeps it below 2^60; each term is rounded to a
-// multiple of 2^-sh, an error below 2^-61 beta per term, under the float-float
-// products' 2^-48 |a_ij u_i|.
-constexpr int kRowsThreads = 1024;
-
-SKL_DEV int rows_shift(double beta)
-{
-    int e = 0;
-    frexp(beta > 0.0 ? beta : 1.0, &e);
-    return 60 - e;
-}
-
-template <int L>
-__global__ void __launch_bounds__(kRowsThreads, 1)
-k_spmv_t_rows(const int* __restrict__ rp, const int* __restrict__ ci, const float2* __restrict__ cv,
-              int n, int d, int rows_per_block, const float2* __restrict__ us,
-              unsigned long long* __restrict__ acc_out, const LsqrState* __restrict__ S)
-{
-    if (S->done) return;
-    extern __shared__ unsigned long long acc[];   // d entries
-    for (int j = threadIdx.x; j < d; j += blockDim.x) acc[j] = 0ull;
-    const int sh = rows_shift(S->beta);
-    __syncthreads();
-    const int lane = threadIdx.x % L, grp = threadIdx.x / L, ngrp = blockDim.x / L;
-    const int r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
-    int i = r0 + grp;
-    // the next row's pointers and u are loaded before the current row's entries are used
-    int p0 = 0, p1 = 0;
-    float2 uu = make_float2(0.f, 0.f);
-    if (i < r1) {
-        p0 = rp[i];
-        p1 = rp[i + 1];
-        uu = us[i];
-    }
-    while (i < r1) {
-        const int ni = i + ngrp;
-        int np0 = 0, np1 = 0;
-        float2 nu = make_float2(0.f, 0.f);
-        if (ni < r1) {
-            np0 = rp[ni];
-            np1 = rp[ni + 1];
-            nu = us[ni];
-        }
-        for (int p = p0 + lane; p < p1; p += 4 * L) {
-            int c[4];
-            float2 a[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int q = p + k * L;
-                const bool ok = q < p1;
-                c[k] = ok ? ci[q] : -1;
-                a[k] = ok ? cv[q] : make_float2(0.f, 0.f);
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (c[k] < 0) continue;
-                // a u as a float pair, then both parts to fixed point
-                const float ph = __fmul_rn(a[k].x, uu.x);
-                const float pe = __fmaf_rn(a[k].x, uu.x, -ph);
-                const float pl = __fmaf_rn(a[k].x, uu.y, __fmaf_rn(a[k].y, uu.x, pe));
-                const long long q = __float2ll_rn(ldexpf(ph, sh)) + __float2ll_rn(ldexpf(pl, sh));
-                atomicAdd(&acc[c[k]], (unsigned long long)q);
-            }
-        }
-        i = ni;
-        p0 = np0;
-        p1 = np1;
-        uu = nu;
-    }
-    __syncthreads();
-    unsigned long long* out = acc_out + (int64_t)blockIdx.x * d;
-    for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = acc[j];
-}
-
-// t[colpos[c]] = opscale(c) (sum over blocks of acc[c]) 2^-sh / beta, columns in
-// natural order (coalesced reads of the blocks' accumulators), blocks summed in
-// order (exact in 64-bit integers).
-__global__ void __launch_bounds__(kLThreads)
-k_spmv_t_finish(const unsigned long long* __restrict__ acc_in, int nblk, int d,
-                const int* __restrict__ colpos, const double* __restrict__ colscale,
-                float2* __restrict__ t, const LsqrState* __restrict__ S)
-{
-    if (S->done) return;
-    const int sh = rows_shift(S->beta);
-    const double ib = S->ib;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d; c += gridDim.x * blockDim.x) {
-        const int i = colpos[c];
-        if (i < 0) continue;
-        long long s = 0;
-        for (int z = 0; z < nblk; ++z) s += (long long)acc_in[(int64_t)z * d + c];
-        const double v = ldexp((double)s, -sh) * ib * (colscale ? colscale[c] : 1.0);
-        t[i] = store_val<true>(v);
-    }
-}
-
-__global__ void k_colpos(int d, int* __restrict__ colpos)
-{
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d; c += gridDim.x * blockDim.x)
-        colpos[c] = -1;
-}
-__global__ void k_colpos_set(const int* __restrict__ cols, int r, int* __restrict__ colpos)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x)
-        colpos[cols[i]] = i;
-}
-
 // ------------------------------------------------- dense A (column-major) --
-// spmv_n: uh = A(:, cols) z(cols) - coef uh.  Block = 256 rows x all columns
-// of its column chunk; chunk partials are combined by spmv_n_dense_reduce.
+// spmv_n: uh = A(:, cols) z(cols) - coef uh.  A block covers 512 rows (two
+// per thread, 256 apart, so each column's loads stay warp-contiguous) and the
+// columns of one chunk (at most kDenseChunk), whose indices and z entries it
+// first stages in shared memory; four columns per step keep eight independent
+// loads in flight per thread.  Chunk partials are combined by
+// spmv_n_dense_reduce.
+constexpr int kDnRows = 2 * kLThreads;
+constexpr int kDenseChunk = 512;
+
 template <bool MIXED>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_n_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int* __restrict__ cols,
                int r, int chunk, const ValT<MIXED>* __restrict__ z, double* __restrict__ part,
                const LsqrState* __restrict__ S)
 {
+    using V = ValT<MIXED>;
     if (S->done) return;
-    const int i = blockIdx.x * kLThreads + threadIdx.x;
-    const int c0 = blockIdx.y * chunk, c1 = min(r, c0 + chunk);
-    if (i >= n) return;
-    Acc<MIXED> acc;
-    for (int c = c0; c < c1; ++c) {
-        const int col = cols[c];
-        acc.fma_mv(A[i + (int64_t)col * lda], z[col]);
+    __shared__ int scol[kDenseChunk];
+    __shared__ V sz[kDenseChunk];
+    const int c0 = blockIdx.y * chunk, nc = min(r - c0, chunk);
+    for (int k = threadIdx.x; k < nc; k += kLThreads) {
+        const int col = cols[c0 + k];
+        scol[k] = col;
+        sz[k] = z[col];
     }
-    part[(int64_t)blockIdx.y * n + i] = acc.value();
+    __syncthreads();
+    const int i0 = blockIdx.x * kDnRows + threadIdx.x, i1 = i0 + kLThreads;
+    if (i0 >= n) return;
+    const int j1 = i1 < n ? i1 : i0;   // a row past the end re-reads row i0; its sum is not stored
+    Acc<MIXED> a0, a1;
+    int k = 0;
+    for (; k + 4 <= nc; k += 4) {
+        V x0[4], x1[4], zz[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const V* col = A + (int64_t)scol[k + u] * lda;
+            x0[u] = col[i0];
+            x1[u] = col[j1];
+            zz[u] = sz[k + u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0.fma_mv(x0[u], zz[u]);
+            a1.fma_mv(x1[u], zz[u]);
+        }
+    }
+    for (; k < nc; ++k) {
+        const V* col = A + (int64_t)scol[k] * lda;
+        const V zz = sz[k];
+        a0.fma_mv(col[i0], zz);
+        a1.fma_mv(col[j1], zz);
+    }
+    double* out = part + (int64_t)blockIdx.y * n;
+    out[i0] = a0.value();
+    if (i1 < n) out[i1] = a1.value();
 }
 
 template <bool MIXED>
@@ -761,29 +682,63 @@ k_spmv_n_dense_reduce(const double* __restrict__ part, int nchunks, int n, doubl
     }
 }
 
-// spmv_t: one block per selected column, contiguous dot over n rows.
+// spmv_t: t(i) = colscale(c) A(:, c)^T u / beta for c = cols[i], four
+// columns per block: each thread reads u once per row pair for all four
+// columns, so u costs a quarter of A's bytes; two rows per step keep ten
+// independent loads in flight per thread.
+constexpr int kDtCols = 4;
+
 template <bool MIXED>
 __global__ void __launch_bounds__(kLThreads)
 k_spmv_t_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int* __restrict__ cols,
                const double* __restrict__ colscale, int r, const ValT<MIXED>* __restrict__ us,
                ValT<MIXED>* __restrict__ t, const LsqrState* __restrict__ S)
 {
+    using V = ValT<MIXED>;
     if (S->done) return;
-    __shared__ Acc<MIXED> red[kLThreads / 32];
+    __shared__ Acc<MIXED> red[kDtCols][kLThreads / 32];
     const double ib = S->ib;
-    for (int i = blockIdx.x; i < r; i += gridDim.x) {
-        const int c = cols[i];
-        const ValT<MIXED>* col = A + (int64_t)c * lda;
-        Acc<MIXED> acc;
-        for (int q = threadIdx.x; q < n; q += kLThreads) acc.fma_mv(col[q], us[q]);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int g = blockIdx.x; g * kDtCols < r; g += gridDim.x) {
+        const int i0 = g * kDtCols;
+        const int nc = min(kDtCols, r - i0);
+        const V* colp[kDtCols];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc.add(acc.shfl_xor(o));
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        for (int u = 0; u < kDtCols; ++u) colp[u] = A + (int64_t)cols[i0 + min(u, nc - 1)] * lda;
+        Acc<MIXED> acc[kDtCols];
+        int q = threadIdx.x;
+        for (; q + kLThreads < n; q += 2 * kLThreads) {
+            const V u0 = us[q], u1 = us[q + kLThreads];
+            V x0[kDtCols], x1[kDtCols];
+#pragma unroll
+            for (int u = 0; u < kDtCols; ++u) {
+                x0[u] = colp[u][q];
+                x1[u] = colp[u][q + kLThreads];
+            }
+#pragma unroll
+            for (int u = 0; u < kDtCols; ++u) {
+                acc[u].fma_mv(x0[u], u0);
+                acc[u].fma_mv(x1[u], u1);
+            }
+        }
+        if (q < n) {
+            const V u0 = us[q];
+#pragma unroll
+            for (int u = 0; u < kDtCols; ++u) acc[u].fma_mv(colp[u][q], u0);
+        }
+#pragma unroll
+        for (int u = 0; u < kDtCols; ++u) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc[u].add(acc[u].shfl_xor(o));
+            if (lane == 0) red[u][warp] = acc[u];
+        }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            Acc<MIXED> s = red[0];
-            for (int q = 1; q < kLThreads / 32; ++q) s.add(red[q]);
-            t[i] = store_val<MIXED>((colscale ? colscale[c] : 1.0) * s.value() * ib);
+        if (threadIdx.x < nc) {
+            const int u = threadIdx.x;
+            Acc<MIXED> s = red[u][0];
+            for (int w = 1; w < kLThreads / 32; ++w) s.add(red[u][w]);
+            const int c = cols[i0 + u];
+            t[i0 + u] = store_val<MIXED>((colscale ? colscale[c] : 1.0) * s.value() * ib);
         }
         __syncthreads();
     }
@@ -911,13 +866,10 @@ struct LsqrBufs {
     double *uh, *vh, *w, *y, *partials, *dpart;
     void *us, *vs, *t, *z;
     int nparts;
-    unsigned long long* racc;   // A^T u by rows: per-block column accumulators
-    int* colpos;                // column -> position among the selected columns, or -1
+    int dense_chunk;            // columns per block of the dense A z
 };
 
-// Blocks of the row-wise A^T u: one 1024-thread block per SM, each with a
-// shared accumulator over all d columns (so d * 8 bytes must fit).
-static int rows_blocks()
+static int sm_count_lsqr()
 {
     static const int v = [] {
         int dev = 0, s = 0;
@@ -926,27 +878,6 @@ static int rows_blocks()
         return s > 0 ? s : 148;
     }();
     return v;
-}
-
-static bool rows_kernel_fits(int64_t d)
-{
-    static const int optin = [] {
-        int dev = 0, o = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        return o;
-    }();
-    return d * 8 + 1024 <= optin;
-}
-
-// A^T u by rows on the mixed sparse path (SKILLS_ATU_ROWS=1; otherwise the CSC kernel)
-static bool use_rows_atu(const LsqrProblem& P)
-{
-    static const bool on = [] {
-        const char* e = getenv("SKILLS_ATU_ROWS");
-        return e && e[0] == '1';
-    }();
-    return on && P.precision == SKL_PREC_MIXED && !P.Ad && P.rp && rows_kernel_fits(P.d);
 }
 
 // lanes per row/column so that each lane handles about four nonzeros
@@ -959,11 +890,28 @@ static int lanes_for(double avg)
 }
 
 static const int kRowsPerBlock = 64;
-static const int kDenseChunk = 128;
+
+// Columns per block of the dense A z: as many column chunks as keep the grid
+// (row blocks x chunks) within one wave of resident blocks, so no second,
+// mostly idle wave trails the product; a multiple of 4, at most kDenseChunk.
+static int dense_n_chunk(const LsqrProblem& P)
+{
+    static const int per_sm = [] {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_n_dense<true>, kLThreads, 0);
+        return b > 0 ? b : 4;
+    }();
+    const int64_t rb = (P.n + kDnRows - 1) / kDnRows;
+    const int64_t slots = (int64_t)sm_count_lsqr() * per_sm;
+    const int64_t nch = std::max<int64_t>(1, slots / std::max<int64_t>(rb, 1));
+    int64_t c = (P.r + nch - 1) / nch;
+    c = (c + 3) & ~(int64_t)3;
+    return (int)std::max<int64_t>(4, std::min<int64_t>(c, kDenseChunk));
+}
 
 static int64_t spmv_n_blocks(const LsqrProblem& P)
 {
-    if (P.Ad) return (P.n + kLThreads - 1) / kLThreads;
+    if (P.Ad) return (P.n + kDnRows - 1) / kDnRows;
     return (P.n + kRowsPerBlock - 1) / kRowsPerBlock;   // upper bound on the grid
 }
 
@@ -978,9 +926,10 @@ size_t lsqr_workspace_bytes(const LsqrProblem& P)
     b += P.d * vs + 256;                                     // z
     int64_t nb = spmv_n_blocks(P);
     b += (nb + 4096) * sizeof(double) + 256;                 // partials
-    if (P.Ad) b += (size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double) + 256;
-    b += (size_t)rows_blocks() * P.d * 8 + 256;              // row-wise A^T u accumulators
-    b += P.d * sizeof(int) + 256;                             // colpos
+    if (P.Ad) {
+        const int c = dense_n_chunk(P);
+        b += (size_t)((P.r + c - 1) / c) * P.n * sizeof(double) + 256;
+    }
     return b;
 }
 
@@ -1007,22 +956,10 @@ static LsqrBufs carve(const LsqrProblem& P, void* work)
     int64_t nb = spmv_n_blocks(P);
     B.nparts = (int)(nb + 4096);
     B.partials = (double*)take(B.nparts * sizeof(double));
-    B.dpart = P.Ad ? (double*)take((size_t)((P.r + kDenseChunk - 1) / kDenseChunk) * P.n * sizeof(double))
+    B.dense_chunk = P.Ad ? dense_n_chunk(P) : 0;
+    B.dpart = P.Ad ? (double*)take((size_t)((P.r + B.dense_chunk - 1) / B.dense_chunk) * P.n * sizeof(double))
                    : nullptr;
-    B.racc = (unsigned long long*)take((size_t)rows_blocks() * P.d * 8);
-    B.colpos = (int*)take(P.d * sizeof(int));
     return B;
-}
-
-// colpos[c] = i for c = cols[i], i < r; -1 for the other columns
-static void prepare_colpos(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
-{
-    if (P.d <= 0) return;
-    const unsigned g = (unsigned)std::min<int64_t>((P.d + 255) / 256, 152);
-    k_colpos<<<g, 256, 0, st>>>((int)P.d, B.colpos);
-    k_colpos_set<<<g, 256, 0, st>>>(P.cols, (int)P.r, B.colpos);
-    SKL_LAUNCHED();
-    SKL_LAUNCHED();
 }
 
 template <bool MIXED>
@@ -1030,11 +967,11 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
 {
     using V = ValT<MIXED>;
     if (P.Ad) {
-        const int nchunks = (int)((P.r + kDenseChunk - 1) / kDenseChunk);
-        dim3 g((unsigned)((P.n + kLThreads - 1) / kLThreads), nchunks);
+        const int chunk = B.dense_chunk;
+        const int nchunks = (int)((P.r + chunk - 1) / chunk);
+        dim3 g((unsigned)((P.n + kDnRows - 1) / kDnRows), nchunks);
         k_spmv_n_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
-                                                       (int)P.r, kDenseChunk, (const V*)B.z, B.dpart,
-                                                       B.S);
+                                                       (int)P.r, chunk, (const V*)B.z, B.dpart, B.S);
         k_spmv_n_dense_reduce<MIXED><<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 1024), kLThreads,
                                        0, st>>>(B.dpart, nchunks, (int)P.n, B.uh, (V*)B.us, B.S,
                                                 B.partials);
@@ -1068,36 +1005,12 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
 {
     using V = ValT<MIXED>;
     if (P.Ad) {
-        unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
+        unsigned g = (unsigned)std::min<int64_t>((P.r + kDtCols - 1) / kDtCols, 152 * 16);
         k_spmv_t_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
                                                        P.opscale, (int)P.r, (const V*)B.us,
                                                        (V*)B.t, B.S);
         SKL_LAUNCHED();
         return;
-    }
-    if constexpr (MIXED) {
-        if (use_rows_atu(P)) {
-            const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(rows_blocks(), (P.n + 63) / 64));
-            const int rpb = (int)((P.n + nblk - 1) / nblk);
-            const double avgr = P.n ? (double)P.nnz / P.n : 0.0;
-            const int Lr = P.lanes_t ? P.lanes_t : lanes_for(avgr);
-            const size_t smem = (size_t)P.d * 8;
-#define SPMV_TR(LL) do { \
-            if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_spmv_t_rows<LL>); \
-            k_spmv_t_rows<LL><<<nblk, kRowsThreads, smem, st>>>(P.rp, P.ci, (const float2*)P.cx, (int)P.n, (int)P.d, rpb, (const float2*)B.us, B.racc, B.S); \
-        } while (0)
-            if (Lr == 32) SPMV_TR(32);
-            else if (Lr == 16) SPMV_TR(16);
-            else if (Lr == 8) SPMV_TR(8);
-            else SPMV_TR(4);
-#undef SPMV_TR
-            const unsigned gf = (unsigned)std::min<int64_t>((P.d + kLThreads - 1) / kLThreads, 152 * 4);
-            k_spmv_t_finish<<<gf, kLThreads, 0, st>>>(B.racc, nblk, (int)P.d, B.colpos, P.opscale,
-                                                      (float2*)B.t, B.S);
-            SKL_LAUNCHED();
-            SKL_LAUNCHED();
-            return;
-        }
     }
     const double avg = P.d ? (double)P.nnz / P.d : 0.0;
     const int L = P.lanes_t ? P.lanes_t : lanes_for(avg);
@@ -1159,7 +1072,6 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     using V = ValT<MIXED>;
     using MT = MatT<MIXED>;
     LsqrBufs B = carve(P, work);
-    prepare_colpos(P, B, st);
     LsqrState init{};
     init.tol = tol;
     init.max_it = max_it;
@@ -1266,7 +1178,6 @@ void tune_lsqr_products(LsqrProblem& P, void* work, cudaStream_t st)
 {
     if (P.Ad || P.n <= 0 || P.r <= 0) return;
     LsqrBufs B = carve(P, work);
-    prepare_colpos(P, B, st);
     LsqrState init{};
     init.ib = 1.0;
     init.beta = 1.0;
@@ -1358,7 +1269,6 @@ static void product_impl(const LsqrProblem& P, char trans, const double* x, doub
 {
     using V = ValT<MIXED>;
     LsqrBufs B = carve(P, work);
-    prepare_colpos(P, B, st);
     LsqrState init{};
     init.ib = 1.0;   // t = A^T u / beta with beta = 1; coef_n = 0: u = A z
     init.beta = 1.0;

@@ -1130,8 +1130,11 @@ static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t 
         double* Ad = C.staging.alloc<double>(n * d);
         double* bd = C.staging.alloc<double>(n);
         double* xd = C.staging.alloc<double>(d);
-        SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double),
-                                   d, cudaMemcpyHostToDevice, st));
+        if (lda == n)   // one contiguous copy: a pitched copy of d columns runs far below the link rate
+            SKL_CUDA(cudaMemcpyAsync(Ad, A, (size_t)n * d * sizeof(double), cudaMemcpyHostToDevice, st));
+        else
+            SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double),
+                                       d, cudaMemcpyHostToDevice, st));
         SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
         dense_pipeline_any(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
         SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
