@@ -458,6 +458,209 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
     cluster_sync();   // keep shared memory alive until every CTA finished reading it
 }
 
+// ------------------------------------------- Y-QRP, registers (FP32) -----
+// The same pivot selection as k_yqrp with the sample block held in registers
+// instead of shared memory: the quad (4 lanes) of column slot q owns local
+// columns q, q + 128, ... (NCQ of them) and lane l4 of the quad holds rows
+// 2 (l4 + 4 j) and 2 (l4 + 4 j) + 1, j < 10, of each, so a column's dot
+// product is a quad reduction.  Only the selections leave the kernel (the
+// sample's own R is discarded), so a finished row is set to zero when its
+// step ends; with rows < s zero, the step's reflector v (v_s = 1, v_r =
+// scale Y(r, winner) below, zero above) makes the update y -= (tau v^T y) v
+// and the next norms ||y||^2 uniform over all 20 rows, in packed FP32x2
+// FMAs, with no shared-memory traffic for the block.
+// The CTA's candidate column is staged by its owner quad, and the owner warp
+// pushes it (rows from s, 16-byte remote stores) with its norm, index, alpha
+// = y_s and sigma2 = ||y_{>s}||^2 to every CTA before the cluster barrier.
+constexpr int kYRegPairs = 10;                 // row pairs per lane: 80 rows per quad
+constexpr int kYRegRows = 8 * kYRegPairs;      // = kMaxNb + kPP
+
+SKL_DEV float2 ffma2(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+SKL_DEV float2 fmul2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+SKL_DEV float quad_sum(float x)
+{
+    x += __shfl_xor_sync(0xffffffffu, x, 1);
+    x += __shfl_xor_sync(0xffffffffu, x, 2);
+    return x;
+}
+
+template <int NCQ>
+__global__ void __launch_bounds__(kYThreads, 1)
+k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel,
+           int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
+           unsigned* __restrict__ status)
+{
+    constexpr int kQuads = kYThreads / 4;
+    __shared__ float s_red_v[kYWarps];
+    __shared__ int s_red_i[kYWarps];
+    __shared__ __align__(16) float4 s_cand[2][kCluster];               // norm, index, sigma2, alpha
+    __shared__ __align__(16) float s_col[2][kCluster][kYRegRows];      // candidates' columns
+    __shared__ __align__(16) float s_stage[kYRegRows];                  // this CTA's candidate
+    __shared__ int s_sel[kMaxNb];
+    __shared__ int s_inlow[kMaxNb];
+    __shared__ int s_lowpos[kMaxNb];
+
+    const unsigned crank = cluster_ctarank();
+    const int cn = (N + kCluster - 1) / kCluster;
+    const int c0 = (int)crank * cn;
+    const int ncols = max(0, min(cn, N - c0));
+    const int nslot = (ncols + kQuads - 1) / kQuads;   // CTA-uniform
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int q4 = tid & 3, quad = tid >> 2;
+
+    float2 y[NCQ][kYRegPairs];
+    unsigned taken = 0;   // bit jj: slot jj taken or past the CTA's columns
+#pragma unroll
+    for (int jj = 0; jj < NCQ; ++jj) {
+        const int lc = jj * kQuads + quad;
+        const bool ok = lc < ncols;
+        if (!ok) taken |= 1u << jj;
+        const float* col = Y + (int64_t)(j0 + c0 + (ok ? lc : 0)) * ldy;
+#pragma unroll
+        for (int j = 0; j < kYRegPairs; ++j) {
+            const int r = 2 * (q4 + 4 * j);
+            y[jj][j] = (ok && r < nbp) ? *reinterpret_cast<const float2*>(col + r) : make_float2(0.f, 0.f);
+        }
+    }
+    // this quad's best untaken column (largest norm, ties -> smallest index)
+    float bv = -1.f;
+    int bi = -1;
+#pragma unroll
+    for (int jj = 0; jj < NCQ; ++jj) {
+        float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < kYRegPairs; ++j) a = ffma2(y[jj][j], y[jj][j], a);
+        const float ss = quad_sum(a.x + a.y);
+        const float nv = ss == ss ? ss : -0.5f;   // a NaN norm ranks below every real one
+        if (!((taken >> jj) & 1u) && nv > bv) { bv = nv; bi = jj * kQuads + quad; }
+    }
+
+    for (int s = 0; s < b; ++s) {
+        const int p = s & 1;
+        // (a) the CTA's candidate, known to every warp
+        warp_argmax(bv, bi);
+        if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
+        __syncthreads();
+        float ov = s_red_v[lane & (kYWarps - 1)];
+        int oi = s_red_i[lane & (kYWarps - 1)];
+        warp_argmax(ov, oi);
+        // (b) the owner warp stages the column and pushes it with its message
+        const int owner_warp = oi >= 0 ? (oi % kQuads) >> 3 : 0;
+        if (wid == owner_warp) {
+            float sg = 0.f;
+            if (oi >= 0 && (lane >> 2) == ((oi % kQuads) & 7)) {
+                const int jo = oi / kQuads;
+#pragma unroll
+                for (int jj = 0; jj < NCQ; ++jj) {
+                    if (jj != jo) continue;
+#pragma unroll
+                    for (int j = 0; j < kYRegPairs; ++j) {
+                        const int r = 2 * (q4 + 4 * j);
+                        *reinterpret_cast<float2*>(s_stage + r) = y[jj][j];
+                        if (r > s) sg = fmaf(y[jj][j].x, y[jj][j].x, sg);
+                        if (r + 1 > s) sg = fmaf(y[jj][j].y, y[jj][j].y, sg);
+                    }
+                }
+            }
+            sg = quad_sum(sg);   // the owner quad's lanes hold sigma2, the others 0
+            sg = __shfl_sync(0xffffffffu, sg, oi >= 0 ? ((oi % kQuads) & 7) * 4 : 0);
+            __syncwarp();
+            const float alpha = oi >= 0 ? s_stage[s] : 0.f;
+            if (lane < kCluster) {
+                float4* dst = &s_cand[p][crank];
+                const float4 msg = make_float4(ov, __int_as_float(oi >= 0 ? c0 + oi : -1), sg, alpha);
+                dsmem_st_v4f32(reinterpret_cast<float*>(dst), (unsigned)lane, msg);
+            }
+            if (oi >= 0) {
+                const int g0 = s >> 2, ng = kYRegRows / 4 - g0;
+                for (int e = lane; e < ng * kCluster; e += 32) {
+                    const int g = g0 + e / kCluster, dstc = e % kCluster;
+                    const float4 v = *reinterpret_cast<const float4*>(s_stage + 4 * g);
+                    dsmem_st_v4f32(&s_col[p][crank][4 * g], (unsigned)dstc, v);
+                }
+            }
+        }
+        // (c) every CTA's pushes visible
+        cluster_sync();
+        // (d) the winner and its reflector, in every thread
+        float4 cm = s_cand[p][lane & (kCluster - 1)];
+        float wv = cm.x;
+        int wi = __float_as_int(cm.y);
+        const int orank = warp_argmax_lane(wv, wi) & (kCluster - 1);
+        cm = s_cand[p][orank];
+        float beta, tau, scale;
+        householder(cm.w, cm.z, beta, tau, scale);
+        const int win_local = (wi >= c0 && wi < c0 + ncols) ? wi - c0 : -1;
+        if (tid == 0) {
+            if (crank == 0) {
+                sel[s] = wi;
+                s_sel[s] = wi;
+            }
+        }
+        if (win_local >= 0 && (win_local % kQuads) == quad) taken |= 1u << (win_local / kQuads);
+        const float* wc = s_col[p][orank];
+        float2 v[kYRegPairs];
+#pragma unroll
+        for (int j = 0; j < kYRegPairs; ++j) {
+            const int r = 2 * (q4 + 4 * j);
+            const float2 c = *reinterpret_cast<const float2*>(wc + r);   // rows < 4 (s / 4): stale, not used
+            v[j].x = r > s ? scale * c.x : (r == s ? 1.f : 0.f);
+            v[j].y = r + 1 > s ? scale * c.y : (r + 1 == s ? 1.f : 0.f);
+        }
+        // rows < s are zero in y and v, so the update keeps them zero; row s
+        // (pair s / 8 of lane (s / 2) mod 4) is the one row to clear
+        const unsigned zbit = q4 == ((s >> 1) & 3) ? 1u << (s >> 3) : 0u;
+        const float2 keep = (s & 1) ? make_float2(1.f, 0.f) : make_float2(0.f, 1.f);
+        // (e) y -= (tau v^T y) v on the untaken columns; row s -> 0; next norms
+        bv = -1.f;
+        bi = -1;
+#pragma unroll
+        for (int jj = 0; jj < NCQ; ++jj) {
+            if (jj >= nslot) break;   // CTA-uniform
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < kYRegPairs; ++j) a = ffma2(v[j], y[jj][j], a);
+            const float w = tau * quad_sum(a.x + a.y);
+            const float2 nw = make_float2(-w, -w);
+            float2 q = make_float2(0.f, 0.f);
+            const bool live = !((taken >> jj) & 1u);
+#pragma unroll
+            for (int j = 0; j < kYRegPairs; ++j) {
+                float2 t = ffma2(nw, v[j], y[jj][j]);
+                if (zbit & (1u << j)) t = fmul2(t, keep);
+                if (live) y[jj][j] = t;
+                q = ffma2(t, t, q);
+            }
+            const float ss = quad_sum(q.x + q.y);
+            if (live) {   // columns ascend with jj
+                const float nv = ss == ss ? ss : -0.5f;
+                if (nv > bv) { bv = nv; bi = jj * kQuads + quad; }
+            }
+        }
+        // no barrier here: the next step's block barrier orders the staging
+        // buffer's reuse, and the candidate buffers alternate by step
+    }
+    __syncthreads();   // the selections written by thread 0, for the move plan
+    if (crank == 0) perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
+    cluster_sync();   // keep shared memory alive until every CTA finished reading it
+}
+
 // -------------------------------------------------- column permutation --
 // Moves the selected columns (sel, relative to j0) to positions j0..j0+b-1;
 // the columns they displace fill the vacated positions in increasing order.
@@ -1016,6 +1219,22 @@ static void launch_cluster(const void* fn, dim3 block, size_t smem, cudaStream_t
     SKL_LAUNCHED();
 }
 
+// Column slots per quad of the register sample QRP for a launch over N
+// columns (FP32, at most 80 sample rows, at most 3 x 128 columns per CTA), or
+// 0 for the shared-memory kernel.  SKILLS_YQRP_REG=0 keeps the latter.
+template <typename T>
+static int yqrp_reg_slots(int nbp, int N)
+{
+    static const bool off = [] {
+        const char* e = getenv("SKILLS_YQRP_REG");
+        return e && e[0] == '0';
+    }();
+    if (!std::is_same<T, float>::value || off || nbp > kYRegRows || (nbp & 1)) return 0;
+    const int cn = (N + kCluster - 1) / kCluster;
+    const int ncq = (cn + kYThreads / 4 - 1) / (kYThreads / 4);
+    return ncq <= 3 ? std::max(ncq, 1) : 0;
+}
+
 // Event pairs around QR sub-steps (profiling only).
 struct QrTimer {
     double* acc;
@@ -1137,7 +1356,16 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &ldpv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
                         &pdst, &pn, &stp};
         cudaEvent_t t0 = t.begin();
-        launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
+        const int ncq = yqrp_reg_slots<T>(nbp, N);
+        if (ncq > 0) {
+            void* rargs[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
+                             &pdst, &pn, &stp};
+            const void* fn = ncq == 1 ? (const void*)k_yqrp_reg<1>
+                           : ncq == 2 ? (const void*)k_yqrp_reg<2> : (const void*)k_yqrp_reg<3>;
+            launch_cluster<T>(fn, dim3(kYThreads), 0, s, rargs);
+        } else {
+            launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
+        }
         t.end(0, t0);
     };
 
