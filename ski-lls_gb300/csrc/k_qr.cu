@@ -322,6 +322,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
         const T nv = nrm[c] == nrm[c] ? nrm[c] : T(-0.5);
         if (!taken[c] && nv > bv) { bv = nv; bi = c; }
     }
+    // every CTA of the cluster has started before the first remote store
+    cluster_sync();
     for (int s = 0; s < b; ++s) {
         const int p = s & 1;
         // (a) local argmax
@@ -469,9 +471,9 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
 // scale Y(r, winner) below, zero above) makes the update y -= (tau v^T y) v
 // and the next norms ||y||^2 uniform over all 20 rows, in packed FP32x2
 // FMAs, with no shared-memory traffic for the block.
-// The CTA's candidate column is staged by its owner quad, and the owner warp
-// pushes it (rows from s, 16-byte remote stores) with its norm, index, alpha
-// = y_s and sigma2 = ||y_{>s}||^2 to every CTA before the cluster barrier.
+// Each warp's best column is staged in shared memory by its quad before the
+// block barrier; after it, warp q pushes the CTA candidate's column
+// (16-byte remote stores) and its norm, index, tau and scale to CTA q.
 constexpr int kYRegPairs = 10;                 // row pairs per lane: 80 rows per quad
 constexpr int kYRegRows = 8 * kYRegPairs;      // = kMaxNb + kPP
 
@@ -507,11 +509,12 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
            unsigned* __restrict__ status)
 {
     constexpr int kQuads = kYThreads / 4;
-    __shared__ float s_red_v[kYWarps];
-    __shared__ int s_red_i[kYWarps];
-    __shared__ __align__(16) float4 s_cand[2][kCluster];               // norm, index, sigma2, alpha
-    __shared__ __align__(16) float s_col[2][kCluster][kYRegRows];      // candidates' columns
-    __shared__ __align__(16) float s_stage[kYRegRows];                  // this CTA's candidate
+    constexpr int kGran = kYRegRows / 4;                                // 16-byte row groups
+    __shared__ float s_wv[kYWarps];                                     // each warp's candidate
+    __shared__ int s_wi[kYWarps];
+    __shared__ __align__(16) float s_wstage[kYWarps][kYRegRows];       // ... and its column
+    __shared__ __align__(16) float4 s_cand[2][kCluster];               // norm, index, tau, scale
+    __shared__ __align__(16) float s_col[2][kCluster][kYRegRows];      // the CTAs' candidates
     __shared__ int s_sel[kMaxNb];
     __shared__ int s_inlow[kMaxNb];
     __shared__ int s_lowpos[kMaxNb];
@@ -520,7 +523,6 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
     const int cn = (N + kCluster - 1) / kCluster;
     const int c0 = (int)crank * cn;
     const int ncols = max(0, min(cn, N - c0));
-    const int nslot = (ncols + kQuads - 1) / kQuads;   // CTA-uniform
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int q4 = tid & 3, quad = tid >> 2;
 
@@ -531,7 +533,7 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         const int lc = jj * kQuads + quad;
         const bool ok = lc < ncols;
         if (!ok) taken |= 1u << jj;
-        const float* col = Y + (int64_t)(j0 + c0 + (ok ? lc : 0)) * ldy;
+        const float* col = Y + (int64_t)(ok ? j0 + c0 + lc : j0) * ldy;
 #pragma unroll
         for (int j = 0; j < kYRegPairs; ++j) {
             const int r = 2 * (q4 + 4 * j);
@@ -550,68 +552,68 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         const float nv = ss == ss ? ss : -0.5f;   // a NaN norm ranks below every real one
         if (!((taken >> jj) & 1u) && nv > bv) { bv = nv; bi = jj * kQuads + quad; }
     }
+    // every CTA of the cluster has started before the first remote store
+    cluster_sync();
 
     for (int s = 0; s < b; ++s) {
         const int p = s & 1;
-        // (a) the CTA's candidate, known to every warp
+        // (a) each warp's candidate: its quad stages the column (rows < s are
+        // zero); bv = ||y_{>=s}||^2 from the previous update
         warp_argmax(bv, bi);
-        if (lane == 0) { s_red_v[wid] = bv; s_red_i[wid] = bi; }
+        if (bi >= 0 && (lane >> 2) == ((bi % kQuads) & 7)) {
+            const int jo = bi / kQuads;
+#pragma unroll
+            for (int jj = 0; jj < NCQ; ++jj) {
+                if (jj != jo) continue;
+#pragma unroll
+                for (int j = 0; j < kYRegPairs; ++j)
+                    *reinterpret_cast<float2*>(&s_wstage[wid][2 * (q4 + 4 * j)]) = y[jj][j];
+            }
+        }
+        if (lane == 0) { s_wv[wid] = bv; s_wi[wid] = bi; }
         __syncthreads();
-        float ov = s_red_v[lane & (kYWarps - 1)];
-        int oi = s_red_i[lane & (kYWarps - 1)];
+        // (b) the CTA's candidate.  Its reflector comes from alpha = y_s and
+        // the norm the argmax used, ||y_{>=s}||: beta = -sign(alpha) ||y||,
+        // tau = (beta - alpha) / beta, v_{>s} = y_{>s} / (alpha - beta).  (Any
+        // reflector onto e_s serves: the sample's own R is discarded.)  Warp
+        // q pushes the column and the message to CTA q of the cluster.
+        float ov = s_wv[lane & (kYWarps - 1)];
+        int oi = s_wi[lane & (kYWarps - 1)];
         warp_argmax(ov, oi);
-        // (b) the owner warp stages the column and pushes it with its message
-        const int owner_warp = oi >= 0 ? (oi % kQuads) >> 3 : 0;
-        if (wid == owner_warp) {
-            float sg = 0.f;
-            if (oi >= 0 && (lane >> 2) == ((oi % kQuads) & 7)) {
-                const int jo = oi / kQuads;
-#pragma unroll
-                for (int jj = 0; jj < NCQ; ++jj) {
-                    if (jj != jo) continue;
-#pragma unroll
-                    for (int j = 0; j < kYRegPairs; ++j) {
-                        const int r = 2 * (q4 + 4 * j);
-                        *reinterpret_cast<float2*>(s_stage + r) = y[jj][j];
-                        if (r > s) sg = fmaf(y[jj][j].x, y[jj][j].x, sg);
-                        if (r + 1 > s) sg = fmaf(y[jj][j].y, y[jj][j].y, sg);
-                    }
+        if (oi >= 0) {
+            const int ow = (oi % kQuads) >> 3;
+            if (lane < kGran) {
+                const float4 g = *reinterpret_cast<const float4*>(&s_wstage[ow][4 * lane]);
+                dsmem_st_v4f32(&s_col[p][crank][4 * lane], (unsigned)wid, g);
+            } else if (lane == kGran) {
+                const float alpha = s_wstage[ow][s];
+                float tau = 0.f, scale = 0.f;
+                if (ov > 0.f) {
+                    const float nrm = sqrtf(ov);
+                    const float beta = alpha >= 0.f ? -nrm : nrm;
+                    tau = (beta - alpha) / beta;
+                    scale = 1.f / (alpha - beta);
                 }
+                const float4 msg = make_float4(ov, __int_as_float(c0 + oi), tau, scale);
+                dsmem_st_v4f32(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg);
             }
-            sg = quad_sum(sg);   // the owner quad's lanes hold sigma2, the others 0
-            sg = __shfl_sync(0xffffffffu, sg, oi >= 0 ? ((oi % kQuads) & 7) * 4 : 0);
-            __syncwarp();
-            const float alpha = oi >= 0 ? s_stage[s] : 0.f;
-            if (lane < kCluster) {
-                float4* dst = &s_cand[p][crank];
-                const float4 msg = make_float4(ov, __int_as_float(oi >= 0 ? c0 + oi : -1), sg, alpha);
-                dsmem_st_v4f32(reinterpret_cast<float*>(dst), (unsigned)lane, msg);
-            }
-            if (oi >= 0) {
-                const int g0 = s >> 2, ng = kYRegRows / 4 - g0;
-                for (int e = lane; e < ng * kCluster; e += 32) {
-                    const int g = g0 + e / kCluster, dstc = e % kCluster;
-                    const float4 v = *reinterpret_cast<const float4*>(s_stage + 4 * g);
-                    dsmem_st_v4f32(&s_col[p][crank][4 * g], (unsigned)dstc, v);
-                }
-            }
+        } else if (lane == kGran) {
+            const float4 msg = make_float4(-1.f, __int_as_float(-1), 0.f, 0.f);
+            dsmem_st_v4f32(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg);
         }
         // (c) every CTA's pushes visible
         cluster_sync();
-        // (d) the winner and its reflector, in every thread
-        float4 cm = s_cand[p][lane & (kCluster - 1)];
+        // (d) the winner and its reflector v (v_s = 1, scale y_{>s} below, 0 above)
+        const float4 cm = s_cand[p][lane & (kCluster - 1)];
         float wv = cm.x;
         int wi = __float_as_int(cm.y);
         const int orank = warp_argmax_lane(wv, wi) & (kCluster - 1);
-        cm = s_cand[p][orank];
-        float beta, tau, scale;
-        householder(cm.w, cm.z, beta, tau, scale);
+        const float4 wm = s_cand[p][orank];
+        const float tau = wm.z, scale = wm.w;
         const int win_local = (wi >= c0 && wi < c0 + ncols) ? wi - c0 : -1;
-        if (tid == 0) {
-            if (crank == 0) {
-                sel[s] = wi;
-                s_sel[s] = wi;
-            }
+        if (tid == 0 && crank == 0) {
+            sel[s] = wi;
+            s_sel[s] = wi;
         }
         if (win_local >= 0 && (win_local % kQuads) == quad) taken |= 1u << (win_local / kQuads);
         const float* wc = s_col[p][orank];
@@ -619,42 +621,63 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
 #pragma unroll
         for (int j = 0; j < kYRegPairs; ++j) {
             const int r = 2 * (q4 + 4 * j);
-            const float2 c = *reinterpret_cast<const float2*>(wc + r);   // rows < 4 (s / 4): stale, not used
+            const float2 c = *reinterpret_cast<const float2*>(wc + r);
             v[j].x = r > s ? scale * c.x : (r == s ? 1.f : 0.f);
             v[j].y = r + 1 > s ? scale * c.y : (r + 1 == s ? 1.f : 0.f);
         }
-        // rows < s are zero in y and v, so the update keeps them zero; row s
-        // (pair s / 8 of lane (s / 2) mod 4) is the one row to clear
-        const unsigned zbit = q4 == ((s >> 1) & 3) ? 1u << (s >> 3) : 0u;
-        const float2 keep = (s & 1) ? make_float2(1.f, 0.f) : make_float2(0.f, 1.f);
-        // (e) y -= (tau v^T y) v on the untaken columns; row s -> 0; next norms
+        // (e) w = tau v^T y per slot (independent chains, interleaved)
+        float w[NCQ];
+#pragma unroll
+        for (int jj = 0; jj < NCQ; ++jj) {
+            float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < kYRegPairs; j += 2) {
+                a0 = ffma2(v[j], y[jj][j], a0);
+                a1 = ffma2(v[j + 1], y[jj][j + 1], a1);
+            }
+            w[jj] = (a0.x + a0.y) + (a1.x + a1.y);
+        }
+#pragma unroll
+        for (int jj = 0; jj < NCQ; ++jj) w[jj] = tau * quad_sum(w[jj]);
+        // row s leaves the sample: zero it in y and in v (the lane holding row
+        // s, pair s / 8), so y -= w v keeps it zero and the norms need no mask
+        if (q4 == ((s >> 1) & 3)) {
+            const int js = s >> 3;
+            const float2 keep = (s & 1) ? make_float2(1.f, 0.f) : make_float2(0.f, 1.f);
+#pragma unroll
+            for (int j = 0; j < kYRegPairs; ++j) {
+                if (j != js) continue;
+                v[j] = fmul2(v[j], keep);
+#pragma unroll
+                for (int jj = 0; jj < NCQ; ++jj) y[jj][j] = fmul2(y[jj][j], keep);
+            }
+        }
+        // y -= w v and the next norms ||y_{>s}||^2; taken slots update too
+        // (their values are never read again)
+        float ss[NCQ];
+#pragma unroll
+        for (int jj = 0; jj < NCQ; ++jj) {
+            const float2 nw = make_float2(-w[jj], -w[jj]);
+            float2 q0 = make_float2(0.f, 0.f), q1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < kYRegPairs; j += 2) {
+                y[jj][j] = ffma2(nw, v[j], y[jj][j]);
+                y[jj][j + 1] = ffma2(nw, v[j + 1], y[jj][j + 1]);
+                q0 = ffma2(y[jj][j], y[jj][j], q0);
+                q1 = ffma2(y[jj][j + 1], y[jj][j + 1], q1);
+            }
+            ss[jj] = (q0.x + q0.y) + (q1.x + q1.y);
+        }
         bv = -1.f;
         bi = -1;
 #pragma unroll
-        for (int jj = 0; jj < NCQ; ++jj) {
-            if (jj >= nslot) break;   // CTA-uniform
-            float2 a = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int j = 0; j < kYRegPairs; ++j) a = ffma2(v[j], y[jj][j], a);
-            const float w = tau * quad_sum(a.x + a.y);
-            const float2 nw = make_float2(-w, -w);
-            float2 q = make_float2(0.f, 0.f);
-            const bool live = !((taken >> jj) & 1u);
-#pragma unroll
-            for (int j = 0; j < kYRegPairs; ++j) {
-                float2 t = ffma2(nw, v[j], y[jj][j]);
-                if (zbit & (1u << j)) t = fmul2(t, keep);
-                if (live) y[jj][j] = t;
-                q = ffma2(t, t, q);
-            }
-            const float ss = quad_sum(q.x + q.y);
-            if (live) {   // columns ascend with jj
-                const float nv = ss == ss ? ss : -0.5f;
-                if (nv > bv) { bv = nv; bi = jj * kQuads + quad; }
-            }
+        for (int jj = 0; jj < NCQ; ++jj) {   // columns ascend with jj
+            const float sq = quad_sum(ss[jj]);
+            const float nv = sq == sq ? sq : -0.5f;
+            if (!((taken >> jj) & 1u) && nv > bv) { bv = nv; bi = jj * kQuads + quad; }
         }
         // no barrier here: the next step's block barrier orders the staging
-        // buffer's reuse, and the candidate buffers alternate by step
+        // buffers' reuse, and the candidate buffers alternate by step
     }
     __syncthreads();   // the selections written by thread 0, for the move plan
     if (crank == 0) perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
