@@ -502,7 +502,25 @@ SKL_DEV float quad_sum(float x)
     return x;
 }
 
-template <int NCQ>
+// Candidate exchange, ASYNC = true: each step's pushes are st.async stores
+// that complete bytes on an mbarrier of the receiving CTA (armed once per
+// step with the 16 senders' bytes, alternating by step parity), so a CTA waits
+// for its own incoming data instead of a cluster-wide barrier.  Every sender
+// always sends its 20 granules and message (zeros without a candidate), so
+// the byte count is fixed.  The wait is bounded: past the limit the kernel
+// sets kStatusTcTimeout, plans no column moves and leaves the step loop.
+constexpr unsigned kYSendBytes = (kYRegRows / 4) * 16 + 16;
+constexpr unsigned kYWaitLimit = 1u << 22;
+
+SKL_DEV void st_async_v4(float* local_dst, unsigned rank, float4 v, uint64_t* local_bar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                     dsmem_addr(local_dst, rank)),
+                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(dsmem_addr(local_bar, rank))
+                 : "memory");
+}
+
+template <int NCQ, bool ASYNC>
 __global__ void __launch_bounds__(kYThreads, 1)
 k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel,
            int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
@@ -513,8 +531,9 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
     __shared__ float s_wv[kYWarps];                                     // each warp's candidate
     __shared__ int s_wi[kYWarps];
     __shared__ __align__(16) float s_wstage[kYWarps][kYRegRows];       // ... and its column
-    __shared__ __align__(16) float4 s_cand[2][kCluster];               // norm, index, tau, scale
-    __shared__ __align__(16) float s_col[2][kCluster][kYRegRows];      // the CTAs' candidates
+    __shared__ __align__(16) float4 s_cand[2][kCluster];               // norm, index, tau
+    __shared__ __align__(16) float s_col[2][kCluster][kYRegRows];      // the CTAs' candidates' v
+    __shared__ __align__(8) uint64_t s_full[2];
     __shared__ int s_sel[kMaxNb];
     __shared__ int s_inlow[kMaxNb];
     __shared__ int s_lowpos[kMaxNb];
@@ -552,9 +571,16 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         const float nv = ss == ss ? ss : -0.5f;   // a NaN norm ranks below every real one
         if (!((taken >> jj) & 1u) && nv > bv) { bv = nv; bi = jj * kQuads + quad; }
     }
-    // every CTA of the cluster has started before the first remote store
+    if (ASYNC && tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_full[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_full[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // every CTA of the cluster has started (and initialised its barriers)
+    // before the first remote store
     cluster_sync();
 
+    bool failed = false;
     for (int s = 0; s < b; ++s) {
         const int p = s & 1;
         // (a) each warp's candidate: its quad stages the column (rows < s are
@@ -572,44 +598,71 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         }
         if (lane == 0) { s_wv[wid] = bv; s_wi[wid] = bi; }
         __syncthreads();
-        // (b) the CTA's candidate.  Its reflector comes from alpha = y_s and
-        // the norm the argmax used, ||y_{>=s}||: beta = -sign(alpha) ||y||,
-        // tau = (beta - alpha) / beta, v_{>s} = y_{>s} / (alpha - beta).  (Any
-        // reflector onto e_s serves: the sample's own R is discarded.)  Warp
-        // q pushes the column and the message to CTA q of the cluster.
+        if (ASYNC && tid == 0)
+            asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
+                             smem_u32(&s_full[p])),
+                         "r"(kYSendBytes * kCluster)
+                         : "memory");
+        // (b) the CTA's candidate and its reflector, from alpha = y_s and the
+        // norm the argmax used, ||y_{>=s}||: beta = -sign(alpha) ||y||, tau =
+        // (beta - alpha) / beta, v_s = 1, v_{>s} = y_{>s} / (alpha - beta), zero
+        // above.  (Any reflector onto e_s serves: the sample's own R is
+        // discarded.)  Warp q sends v and the message to CTA q of the cluster.
         float ov = s_wv[lane & (kYWarps - 1)];
         int oi = s_wi[lane & (kYWarps - 1)];
         warp_argmax(ov, oi);
-        if (oi >= 0) {
-            const int ow = (oi % kQuads) >> 3;
-            if (lane < kGran) {
-                const float4 g = *reinterpret_cast<const float4*>(&s_wstage[ow][4 * lane]);
-                dsmem_st_v4f32(&s_col[p][crank][4 * lane], (unsigned)wid, g);
-            } else if (lane == kGran) {
-                const float alpha = s_wstage[ow][s];
-                float tau = 0.f, scale = 0.f;
-                if (ov > 0.f) {
-                    const float nrm = sqrtf(ov);
-                    const float beta = alpha >= 0.f ? -nrm : nrm;
-                    tau = (beta - alpha) / beta;
-                    scale = 1.f / (alpha - beta);
-                }
-                const float4 msg = make_float4(ov, __int_as_float(c0 + oi), tau, scale);
-                dsmem_st_v4f32(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg);
-            }
-        } else if (lane == kGran) {
-            const float4 msg = make_float4(-1.f, __int_as_float(-1), 0.f, 0.f);
-            dsmem_st_v4f32(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg);
+        const int ow = oi >= 0 ? (oi % kQuads) >> 3 : 0;
+        const float alpha = s_wstage[ow][s];
+        float tau = 0.f, scale = 0.f;
+        if (oi >= 0 && ov > 0.f) {
+            const float nrm = ov * rsqrtf(ov);
+            const float beta = alpha >= 0.f ? -nrm : nrm;
+            tau = (beta - alpha) * __frcp_rn(beta);
+            scale = __frcp_rn(alpha - beta);
         }
-        // (c) every CTA's pushes visible
-        cluster_sync();
-        // (d) the winner and its reflector v (v_s = 1, scale y_{>s} below, 0 above)
+        if (lane < kGran) {
+            const int r = 4 * lane;
+            float4 g = *reinterpret_cast<const float4*>(&s_wstage[ow][r]);
+            g.x = r > s ? scale * g.x : (r == s ? 1.f : 0.f);
+            g.y = r + 1 > s ? scale * g.y : (r + 1 == s ? 1.f : 0.f);
+            g.z = r + 2 > s ? scale * g.z : (r + 2 == s ? 1.f : 0.f);
+            g.w = r + 3 > s ? scale * g.w : (r + 3 == s ? 1.f : 0.f);
+            if (oi < 0) g = make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (ASYNC)
+                st_async_v4(&s_col[p][crank][r], (unsigned)wid, g, &s_full[p]);
+            else if (oi >= 0)
+                dsmem_st_v4f32(&s_col[p][crank][r], (unsigned)wid, g);
+        } else if (lane == kGran) {
+            const float4 msg = oi >= 0 ? make_float4(ov, __int_as_float(c0 + oi), tau, 0.f)
+                                       : make_float4(-1.f, __int_as_float(-1), 0.f, 0.f);
+            if constexpr (ASYNC)
+                st_async_v4(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg, &s_full[p]);
+            else
+                dsmem_st_v4f32(reinterpret_cast<float*>(&s_cand[p][crank]), (unsigned)wid, msg);
+        }
+        // (c) every CTA's data for this step in this CTA's shared memory
+        if constexpr (ASYNC) {
+            const unsigned bar = smem_u32(&s_full[p]), par = (unsigned)(s >> 1) & 1u;
+            unsigned done = 0;
+            for (unsigned it = 0; it < kYWaitLimit && !done; ++it)
+                asm volatile("{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 P, [%1], %2;\n\t"
+                             "selp.u32 %0, 1, 0, P;\n\t}"
+                             : "=r"(done)
+                             : "r"(bar), "r"(par)
+                             : "memory");
+            if (__syncthreads_or(!done)) {
+                failed = true;
+                break;
+            }
+        } else {
+            cluster_sync();
+        }
+        // (d) the winner and its reflector
         const float4 cm = s_cand[p][lane & (kCluster - 1)];
         float wv = cm.x;
         int wi = __float_as_int(cm.y);
         const int orank = warp_argmax_lane(wv, wi) & (kCluster - 1);
-        const float4 wm = s_cand[p][orank];
-        const float tau = wm.z, scale = wm.w;
+        const float wtau = s_cand[p][orank].z;
         const int win_local = (wi >= c0 && wi < c0 + ncols) ? wi - c0 : -1;
         if (tid == 0 && crank == 0) {
             sel[s] = wi;
@@ -619,12 +672,7 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         const float* wc = s_col[p][orank];
         float2 v[kYRegPairs];
 #pragma unroll
-        for (int j = 0; j < kYRegPairs; ++j) {
-            const int r = 2 * (q4 + 4 * j);
-            const float2 c = *reinterpret_cast<const float2*>(wc + r);
-            v[j].x = r > s ? scale * c.x : (r == s ? 1.f : 0.f);
-            v[j].y = r + 1 > s ? scale * c.y : (r + 1 == s ? 1.f : 0.f);
-        }
+        for (int j = 0; j < kYRegPairs; ++j) v[j] = *reinterpret_cast<const float2*>(wc + 2 * (q4 + 4 * j));
         // (e) w = tau v^T y per slot (independent chains, interleaved)
         float w[NCQ];
 #pragma unroll
@@ -638,7 +686,7 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
             w[jj] = (a0.x + a0.y) + (a1.x + a1.y);
         }
 #pragma unroll
-        for (int jj = 0; jj < NCQ; ++jj) w[jj] = tau * quad_sum(w[jj]);
+        for (int jj = 0; jj < NCQ; ++jj) w[jj] = wtau * quad_sum(w[jj]);
         // row s leaves the sample: zero it in y and in v (the lane holding row
         // s, pair s / 8), so y -= w v keeps it zero and the norms need no mask
         if (q4 == ((s >> 1) & 3)) {
@@ -677,10 +725,17 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
             if (!((taken >> jj) & 1u) && nv > bv) { bv = nv; bi = jj * kQuads + quad; }
         }
         // no barrier here: the next step's block barrier orders the staging
-        // buffers' reuse, and the candidate buffers alternate by step
+        // buffer's reuse, and the candidate buffers alternate by step
     }
     __syncthreads();   // the selections written by thread 0, for the move plan
-    if (crank == 0) perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(status, kStatusTcTimeout);
+            if (crank == 0) *plan_n = 0;
+        }
+    } else if (crank == 0) {
+        perm_plan_block(s_sel, s_inlow, s_lowpos, b, N, plan_src, plan_dst, plan_n, status);
+    }
     cluster_sync();   // keep shared memory alive until every CTA finished reading it
 }
 
@@ -1258,6 +1313,17 @@ static int yqrp_reg_slots(int nbp, int N)
     return ncq <= 3 ? std::max(ncq, 1) : 0;
 }
 
+// The register sample QRP's exchange: mbarrier-completed remote stores
+// (default) or remote stores plus a cluster barrier (SKILLS_YQRP_ASYNC=0).
+static bool yqrp_async()
+{
+    static const bool v = [] {
+        const char* e = getenv("SKILLS_YQRP_ASYNC");
+        return !(e && e[0] == '0');
+    }();
+    return v;
+}
+
 // Event pairs around QR sub-steps (profiling only).
 struct QrTimer {
     double* acc;
@@ -1383,8 +1449,13 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         if (ncq > 0) {
             void* rargs[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
                              &pdst, &pn, &stp};
-            const void* fn = ncq == 1 ? (const void*)k_yqrp_reg<1>
-                           : ncq == 2 ? (const void*)k_yqrp_reg<2> : (const void*)k_yqrp_reg<3>;
+            const void* fn;
+            if (yqrp_async())
+                fn = ncq == 1 ? (const void*)k_yqrp_reg<1, true>
+                   : ncq == 2 ? (const void*)k_yqrp_reg<2, true> : (const void*)k_yqrp_reg<3, true>;
+            else
+                fn = ncq == 1 ? (const void*)k_yqrp_reg<1, false>
+                   : ncq == 2 ? (const void*)k_yqrp_reg<2, false> : (const void*)k_yqrp_reg<3, false>;
             launch_cluster<T>(fn, dim3(kYThreads), 0, s, rargs);
         } else {
             launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);

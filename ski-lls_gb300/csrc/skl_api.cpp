@@ -450,7 +450,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
             o.profile ? info.qr_prof_ms : nullptr, tuned.nb);
     {
         const unsigned qs = read_status(C, st);
-        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a kernel's bounded wait gave up (tensor-core product or sample QRP exchange)");
         if (qs & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
     }
     trace_phase(st, "cpqr");
@@ -942,7 +942,7 @@ static bool dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
             cpqr_on ? 1 : 0, o.profile ? info.qr_prof_ms : nullptr);
     {
         const unsigned qs = read_status(C, st);
-        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+        if (qs & kStatusTcTimeout) fail(SKL_ERR_TIMEOUT, "a kernel's bounded wait gave up (tensor-core product or sample QRP exchange)");
         if (qs & kQrSelectBit) fail(SKL_ERR_NONFINITE, "non-finite values in the sketch factorization");
     }
     trace_phase(st, "dense qr");

@@ -169,7 +169,8 @@ void cpqr(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, void* work,
 int cpqr_panel_width(int64_t m, int64_t d, int nb_cap);
 
 // --------------------------------------------------------------- k_tc.cu --
-// Status bit of a tensor-core kernel whose bounded mbarrier wait gave up.
+// Status bit of a kernel whose bounded mbarrier wait gave up (the tensor-core
+// products, the sample QRP's candidate exchange).
 constexpr unsigned kStatusTcTimeout = 64u;
 // W (b x N, ld b) = V^T A on the tensor cores (tcgen05, 3xTF32): V is M x b
 // (ldv, b <= 64), A is M x N (lda); both 16-byte aligned with ld*4 a multiple
