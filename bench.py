@@ -42,6 +42,7 @@ import numpy as np  # noqa: E402
 METRIC = "time-to-solve @ backward err <=1e-10: mixed vs FP64 path on 1 GB300 (s, %HBM)"
 DEFAULT_WORKLOAD = "sparse_illcond_120000x5000"
 IT_TOL = 1e-10
+BATCH_BACKWARD_TOL = 1e-10   # batched problems: restarts until the metric's bound holds
 
 
 def parse_args():
@@ -659,14 +660,16 @@ def run_batched(args, rank, world):
     gen_s = time.perf_counter() - t0
     total = int(ranks.sum(len(probs)))
     warm = probs[: min(8, len(probs))]
-    skl.batched_sparse_spqr(warm, 1.7, 2, it_tol=IT_TOL, seed=1, device=local)
+    # the metric's backward-error condition holds for every problem: LSQR
+    # restarts from the FP64 residual until it is met
+    bopts = dict(it_tol=IT_TOL, seed=1, backward_tol=BATCH_BACKWARD_TOL, device=local)
+    skl.batched_sparse_spqr(warm, 1.7, 2, **bopts)
     batched_s = []
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         ranks.barrier()
         t0 = time.perf_counter()
-        xs, infos, status = skl.batched_sparse_spqr(probs, 1.7, 2, it_tol=IT_TOL, seed=1,
-                                                    device=local)
+        xs, infos, status = skl.batched_sparse_spqr(probs, 1.7, 2, **bopts)
         batched_s.append(ranks.max(time.perf_counter() - t0))   # the slowest rank's time
     # a loop of single solves (one pass; it is the slow reference point)
     torch.cuda.synchronize()
@@ -674,7 +677,7 @@ def run_batched(args, rank, world):
     t0 = time.perf_counter()
     same = True
     for p, (A, b) in enumerate(probs):
-        r = skl.ls_sparse_spqr(A, b, 1.7, 2, it_tol=IT_TOL, seed=1, device=local)
+        r = skl.ls_sparse_spqr(A, b, 1.7, 2, **bopts)
         same = same and np.array_equal(r.x, xs[p])
     loop_s = ranks.max(time.perf_counter() - t0)
     same = ranks.sum(0 if same else 1) == 0
@@ -691,7 +694,7 @@ def run_batched(args, rank, world):
                    "problems_per_rank": len(probs),
                    "d_range": [50, 500], "n_rule": "n ~ U[2000, 50000], n >= 20 d",
                    "streams": int(os.environ.get("SKILLS_BATCH_STREAMS", "8")), "gamma": 1.7,
-                   "k": 2, "it_tol": IT_TOL, "inputs": "host buffers (H2D inside the timing)"},
+                   "k": 2, "it_tol": IT_TOL, "backward_tol": BATCH_BACKWARD_TOL, "inputs": "host buffers (H2D inside the timing)"},
         "e2e": {"value": total / best, "unit": "problems/s",
                 "h2d_bytes_per_step": int(sum(16 * A.nnz + 8 * (A.shape[1] + 1) + 8 * A.shape[0]
                                               for A, _ in probs)),

@@ -261,7 +261,7 @@ def dense_solve_device(n, d, a_ptr, lda, b_ptr, xout_ptr, gamma, k, *, precision
 
 def batched_sparse_spqr(problems, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, *,
                         abs_tol=ABS_TOL, it_tol=IT_TOL, max_it=MAX_IT, precision="mixed",
-                        seed=None, device=0):
+                        seed=None, backward_tol=0.0, max_refine=3, device=0):
     """skl_batched_sparse_solve over [(A, b), ...] (scipy CSC, host arrays).
     Returns (list of x, list of SklInfo, list of status codes)."""
     nprob = len(problems)
@@ -287,6 +287,7 @@ def batched_sparse_spqr(problems, gamma=OVER_SAMPLING_RATIO, k=NNZ_PER_COLUMN, *
     o.gamma, o.k, o.abs_tol, o.it_tol, o.max_it = gamma, k, abs_tol, it_tol, max_it
     o.precision = PREC[precision]
     o.seed_mode, o.seed = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    o.backward_tol, o.max_refine = backward_tol, max_refine
     o.device = device
     infos = (SklInfo * max(nprob, 1))()
     status = (ctypes.c_int * max(nprob, 1))()
