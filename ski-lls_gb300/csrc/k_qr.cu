@@ -474,8 +474,8 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
 // Each warp's best column is staged in shared memory by its quad before the
 // block barrier; after it, warp q pushes the CTA candidate's column
 // (16-byte remote stores) and its norm, index, tau and scale to CTA q.
-constexpr int kYRegPairs = 10;                 // row pairs per lane: 80 rows per quad
-constexpr int kYRegRows = 8 * kYRegPairs;      // = kMaxNb + kPP
+constexpr int kYRegPairsMax = 10;              // row pairs per lane: 80 rows per quad
+constexpr int kYRegRows = 8 * kYRegPairsMax;   // = kMaxNb + kPP
 
 SKL_DEV float2 ffma2(float2 a, float2 b, float2 c)
 {
@@ -509,7 +509,6 @@ SKL_DEV float quad_sum(float x)
 // always sends its 20 granules and message (zeros without a candidate), so
 // the byte count is fixed.  The wait is bounded: past the limit the kernel
 // sets kStatusTcTimeout, plans no column moves and leaves the step loop.
-constexpr unsigned kYSendBytes = (kYRegRows / 4) * 16 + 16;
 constexpr unsigned kYWaitLimit = 1u << 22;
 
 SKL_DEV void st_async_v4(float* local_dst, unsigned rank, float4 v, uint64_t* local_bar)
@@ -520,14 +519,16 @@ SKL_DEV void st_async_v4(float* local_dst, unsigned rank, float4 v, uint64_t* lo
                  : "memory");
 }
 
-template <int NCQ, bool ASYNC>
+template <int NCQ, int NP, bool ASYNC>
 __global__ void __launch_bounds__(kYThreads, 1)
 k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, int* __restrict__ sel,
            int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
            unsigned* __restrict__ status)
 {
     constexpr int kQuads = kYThreads / 4;
-    constexpr int kGran = kYRegRows / 4;                                // 16-byte row groups
+    constexpr int kYRegPairs = NP;                                      // row pairs per lane
+    constexpr int kGran = 2 * NP;                                       // 16-byte row groups
+    constexpr unsigned kYSendBytes = kGran * 16 + 16;                   // per sender and step
     __shared__ float s_wv[kYWarps];                                     // each warp's candidate
     __shared__ int s_wi[kYWarps];
     __shared__ __align__(16) float s_wstage[kYWarps][kYRegRows];       // ... and its column
@@ -673,6 +674,7 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
         float2 v[kYRegPairs];
 #pragma unroll
         for (int j = 0; j < kYRegPairs; ++j) v[j] = *reinterpret_cast<const float2*>(wc + 2 * (q4 + 4 * j));
+        static_assert(kYRegPairs % 2 == 0, "row pairs are consumed two at a time");
         // (e) w = tau v^T y per slot (independent chains, interleaved)
         float w[NCQ];
 #pragma unroll
@@ -1297,20 +1299,26 @@ static void launch_cluster(const void* fn, dim3 block, size_t smem, cudaStream_t
     SKL_LAUNCHED();
 }
 
-// Column slots per quad of the register sample QRP for a launch over N
-// columns (FP32, at most 80 sample rows, at most 3 x 128 columns per CTA), or
-// 0 for the shared-memory kernel.  SKILLS_YQRP_REG=0 keeps the latter.
+// Launch shape of the register sample QRP for nbp sample rows and N columns:
+// row pairs per lane np (8: nbp <= 64, 10: nbp <= 80) and column slots per
+// quad ncq (at most 3 with 10 pairs, 5 with 8: what 128 registers a thread
+// hold), or ncq = 0 for the shared-memory kernel (FP64, wider samples).
+// SKILLS_YQRP_REG=0 keeps the latter.
+struct YRegShape {
+    int ncq, np;
+};
 template <typename T>
-static int yqrp_reg_slots(int nbp, int N)
+static YRegShape yqrp_reg_shape(int nbp, int N)
 {
     static const bool off = [] {
         const char* e = getenv("SKILLS_YQRP_REG");
         return e && e[0] == '0';
     }();
-    if (!std::is_same<T, float>::value || off || nbp > kYRegRows || (nbp & 1)) return 0;
+    if (!std::is_same<T, float>::value || off || nbp > kYRegRows || (nbp & 1)) return {0, 0};
+    const int np = nbp <= 64 ? 8 : 10;
     const int cn = (N + kCluster - 1) / kCluster;
-    const int ncq = (cn + kYThreads / 4 - 1) / (kYThreads / 4);
-    return ncq <= 3 ? std::max(ncq, 1) : 0;
+    const int ncq = std::max(1, (cn + kYThreads / 4 - 1) / (kYThreads / 4));
+    return {ncq <= (np == 8 ? 5 : 3) ? ncq : 0, np};
 }
 
 // The register sample QRP's exchange: mbarrier-completed remote stores
@@ -1322,6 +1330,26 @@ static bool yqrp_async()
         return !(e && e[0] == '0');
     }();
     return v;
+}
+
+static const void* yqrp_reg_kernel(YRegShape sh, bool async)
+{
+#define YREG(C, P) (async ? (const void*)k_yqrp_reg<C, P, true> : (const void*)k_yqrp_reg<C, P, false>)
+    if (sh.np == 8) {
+        switch (sh.ncq) {
+        case 1: return YREG(1, 8);
+        case 2: return YREG(2, 8);
+        case 3: return YREG(3, 8);
+        case 4: return YREG(4, 8);
+        default: return YREG(5, 8);
+        }
+    }
+    switch (sh.ncq) {
+    case 1: return YREG(1, 10);
+    case 2: return YREG(2, 10);
+    default: return YREG(3, 10);
+    }
+#undef YREG
 }
 
 // Event pairs around QR sub-steps (profiling only).
@@ -1445,18 +1473,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         void* args[] = {(void*)&Yc, &ldy, (void*)&nbv, &ldpv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
                         &pdst, &pn, &stp};
         cudaEvent_t t0 = t.begin();
-        const int ncq = yqrp_reg_slots<T>(nbp, N);
-        if (ncq > 0) {
+        const YRegShape sh = yqrp_reg_shape<T>(nbp, N);
+        if (sh.ncq > 0) {
             void* rargs[] = {(void*)&Yc, &ldy, (void*)&nbv, &jj, (void*)&N, (void*)&b, &sel, &psrc,
                              &pdst, &pn, &stp};
-            const void* fn;
-            if (yqrp_async())
-                fn = ncq == 1 ? (const void*)k_yqrp_reg<1, true>
-                   : ncq == 2 ? (const void*)k_yqrp_reg<2, true> : (const void*)k_yqrp_reg<3, true>;
-            else
-                fn = ncq == 1 ? (const void*)k_yqrp_reg<1, false>
-                   : ncq == 2 ? (const void*)k_yqrp_reg<2, false> : (const void*)k_yqrp_reg<3, false>;
-            launch_cluster<T>(fn, dim3(kYThreads), 0, s, rargs);
+            launch_cluster<T>(yqrp_reg_kernel(sh, yqrp_async()), dim3(kYThreads), 0, s, rargs);
         } else {
             launch_cluster<T>((const void*)k_yqrp<T>, dim3(kYThreads), ysm_max, s, args);
         }
