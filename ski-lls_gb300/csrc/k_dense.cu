@@ -46,11 +46,12 @@ template <typename C> SKL_DEV C cmul(C a, C b)
     return r;
 }
 
-// exp(-2 pi i * num / den) in the working precision
+// exp(-2 pi i * num / den) in the working precision, 0 <= num < den < 2^31
+// (32-bit operands: a 64-bit remainder or division per twiddle is a long
+// emulated sequence).
 template <typename T>
-SKL_DEV typename Cplx<T>::type twiddle(long long num, long long den)
+SKL_DEV typename Cplx<T>::type twiddle(int num, int den)
 {
-    num %= den;
     if constexpr (std::is_same<T, float>::value) {
         float s, c;
         sincospif(-2.0f * (float)num / (float)den, &s, &c);
@@ -60,6 +61,55 @@ SKL_DEV typename Cplx<T>::type twiddle(long long num, long long den)
         sincospi(-2.0 * (double)num / (double)den, &s, &c);
         return make_double2(c, s);
     }
+}
+
+// The R-th roots of unity of the small DFTs, exp(-2 pi i j / R), as compile-
+// time constants: cos and sin by their Taylor series (the argument reduced to
+// [-pi, pi], 30 terms: far below double rounding there), so the radix-3/5/7
+// butterflies carry no runtime trigonometry.
+constexpr double kPiD = 3.14159265358979323846;
+constexpr double cx_sin(double x)
+{
+    double term = x, sum = x;
+    for (int n = 1; n < 30; ++n) {
+        term *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double cx_cos(double x)
+{
+    double term = 1.0, sum = 1.0;
+    for (int n = 1; n < 30; ++n) {
+        term *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double root_angle(int j, int R)
+{
+    const double a = -2.0 * kPiD * (double)(j % R) / (double)R;
+    return a < -kPiD ? a + 2.0 * kPiD : a;
+}
+template <int R>
+struct Roots {
+    double re[R], im[R];
+    constexpr Roots() : re(), im()
+    {
+        for (int j = 0; j < R; ++j) {
+            re[j] = cx_cos(root_angle(j, R));
+            im[j] = cx_sin(root_angle(j, R));
+        }
+    }
+};
+template <typename T, int R>
+SKL_DEV typename Cplx<T>::type small_root(int j)
+{
+    constexpr Roots<R> w{};
+    typename Cplx<T>::type r;
+    r.x = (T)w.re[j % R];
+    r.y = (T)w.im[j % R];
+    return r;
 }
 
 // In-register R-point DFT (forward) of v[0..R).
@@ -88,7 +138,7 @@ SKL_DEV void dft_small(typename Cplx<T>::type* v)
         for (int q = 0; q < R; ++q) {
             C acc = v[0];
 #pragma unroll
-            for (int t = 1; t < R; ++t) acc = cadd(acc, cmul(v[t], twiddle<T>((long long)q * t, R)));
+            for (int t = 1; t < R; ++t) acc = cadd(acc, cmul(v[t], small_root<T, R>(q * t)));
             out[q] = acc;
         }
 #pragma unroll
@@ -107,9 +157,15 @@ SKL_DEV void butterfly_load(const typename Cplx<T>::type* x, int L, int p, int i
     const int k = i % p;
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = x[i + q * T_];
-    if (p > 1) {
+    if (p > 1 && k > 0) {
+        // w^q for w = exp(-2 pi i k / (pR)): one sincospi, then powers
+        const typename Cplx<T>::type w = twiddle<T>(k, p * R);
+        typename Cplx<T>::type wq = w;
 #pragma unroll
-        for (int q = 1; q < R; ++q) v[q] = cmul(v[q], twiddle<T>((long long)q * k, (long long)p * R));
+        for (int q = 1; q < R; ++q) {
+            v[q] = cmul(v[q], wq);
+            if (q + 1 < R) wq = cmul(wq, w);
+        }
     }
     dft_small<T, R>(v);
 }
@@ -235,7 +291,7 @@ SKL_DEV typename Cplx<T>::type* dht_column(const FftPlan& P, const double* __res
         const C zc = Z[(L - kk) % L];
         const T er = (zk.x + zc.x) * T(0.5), ei = (zk.y - zc.y) * T(0.5);   // even part
         const T or_ = (zk.y + zc.y) * T(0.5), oi = -(zk.x - zc.x) * T(0.5); // odd part
-        const C w = twiddle<T>(kk, 2LL * L);
+        const C w = twiddle<T>(kk, 2 * L);
         const T xr = er + (w.x * or_ - w.y * oi);
         const T xi = ei + (w.x * oi + w.y * or_);
         hk = xr - xi;
