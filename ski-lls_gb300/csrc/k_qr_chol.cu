@@ -340,67 +340,180 @@ SKL_DEV void mma_tf32_16x8x8(float (&d)[4], const unsigned (&a)[4], const unsign
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// One warp's 16 x 8 tile w of C = op(A) op(B) (m x n, k over the masks'
+// range), accumulated in acc; false when the product has no tile w.
+template <bool TA, int MA, bool TB, int MB>
+SKL_DEV bool tc_tile(int w, int m, int n, int kk, const float* A, int lda, const float* B, int ldb,
+                     const float* __restrict__ sB, float (&acc)[4], int& i0, int& c0)
+{
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2, tig = lane & 3;
+    const int ntn = (n + 7) >> 3;
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+    if (w < 0 || w >= ((m + 15) >> 4) * ntn) return false;
+    i0 = (w / ntn) * 16;
+    c0 = (w % ntn) * 8;
+    int klo, khi;
+    k_range<MA, MB>(i0, c0, 16, 8, kk, klo, khi);
+    klo &= ~7;
+    const int ra0 = i0 + g, ra1 = i0 + g + 8, cb = c0 + g;
+    for (int k0 = klo; k0 < khi; k0 += 8) {
+        const int ka0 = k0 + tig, ka1 = k0 + tig + 4;
+        // fragments: A (g, tig) (g+8, tig) (g, tig+4) (g+8, tig+4); B (tig, g) (tig+4, g)
+        float av[4], bv[2];
+        av[0] = (ra0 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka0) : 0.f;
+        av[1] = (ra1 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka0) : 0.f;
+        av[2] = (ra0 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka1) : 0.f;
+        av[3] = (ra1 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka1) : 0.f;
+        bv[0] = (ka0 < kk && cb < n) ? (sB ? sB[ka0] : 1.f) * op_at<float, TB, MB>(B, ldb, ka0, cb) : 0.f;
+        bv[1] = (ka1 < kk && cb < n) ? (sB ? sB[ka1] : 1.f) * op_at<float, TB, MB>(B, ldb, ka1, cb) : 0.f;
+        unsigned ah[4], al[4], bh[2], bl[2];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            ah[e] = tf32_rna(av[e]);
+            al[e] = tf32_rna(av[e] - __uint_as_float(ah[e]));
+        }
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            bh[e] = tf32_rna(bv[e]);
+            bl[e] = tf32_rna(bv[e] - __uint_as_float(bh[e]));
+        }
+        mma_tf32_16x8x8(acc, al, bh);
+        mma_tf32_16x8x8(acc, ah, bl);
+        mma_tf32_16x8x8(acc, ah, bh);
+    }
+    return true;
+}
+
+// C fragment: (g, 2 tig) (g, 2 tig + 1) (g + 8, 2 tig) (g + 8, 2 tig + 1)
+template <bool ACC>
+SKL_DEV void tc_tile_store(int m, int n, int i0, int c0, const float (&acc)[4], float alpha, float* C, int ldc,
+                           float* __restrict__ Cg, int ldg, float* __restrict__ tau)
+{
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int i = i0 + g + (e >> 1) * 8, c = c0 + 2 * tig + (e & 1);
+        if (i >= m || c >= n) continue;
+        const float v = alpha * acc[e];
+        if (Cg) {
+            Cg[i + (int64_t)c * ldg] = v;
+            if (i == c) tau[i] = v;
+        } else if (ACC) {
+            C[i * ldc + c] += v;
+        } else {
+            C[i * ldc + c] = v;
+        }
+    }
+}
+
 template <bool TA, int MA, bool TB, int MB, bool ACC>
 SKL_DEV void blk_mul_tc(int m, int n, int kk, const float* A, int lda, const float* B, int ldb,
                         const float* __restrict__ sB, float alpha, float* C, int ldc,
                         float* __restrict__ Cg, int ldg, float* __restrict__ tau)
 {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, tig = lane & 3;
-    const int ntn = (n + 7) >> 3;
-    const bool act = warp < ((m + 15) >> 4) * ntn;
-    const int i0 = (warp / ntn) * 16, c0 = (warp % ntn) * 8;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    if (act) {
-        int klo, khi;
-        k_range<MA, MB>(i0, c0, 16, 8, kk, klo, khi);
-        klo &= ~7;
-        const int ra0 = i0 + g, ra1 = i0 + g + 8, cb = c0 + g;
-        for (int k0 = klo; k0 < khi; k0 += 8) {
-            const int ka0 = k0 + tig, ka1 = k0 + tig + 4;
-            // fragments: A (g, tig) (g+8, tig) (g, tig+4) (g+8, tig+4); B (tig, g) (tig+4, g)
-            float av[4], bv[2];
-            av[0] = (ra0 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka0) : 0.f;
-            av[1] = (ra1 < m && ka0 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka0) : 0.f;
-            av[2] = (ra0 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra0, ka1) : 0.f;
-            av[3] = (ra1 < m && ka1 < kk) ? op_at<float, TA, MA>(A, lda, ra1, ka1) : 0.f;
-            bv[0] = (ka0 < kk && cb < n) ? (sB ? sB[ka0] : 1.f) * op_at<float, TB, MB>(B, ldb, ka0, cb) : 0.f;
-            bv[1] = (ka1 < kk && cb < n) ? (sB ? sB[ka1] : 1.f) * op_at<float, TB, MB>(B, ldb, ka1, cb) : 0.f;
-            unsigned ah[4], al[4], bh[2], bl[2];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                ah[e] = tf32_rna(av[e]);
-                al[e] = tf32_rna(av[e] - __uint_as_float(ah[e]));
+    float acc[4];
+    int i0 = 0, c0 = 0;
+    const bool act = tc_tile<TA, MA, TB, MB>(threadIdx.x >> 5, m, n, kk, A, lda, B, ldb, sB, acc, i0, c0);
+    __syncthreads();
+    if (act) tc_tile_store<ACC>(m, n, i0, c0, acc, alpha, C, ldc, Cg, ldg, tau);
+    __syncthreads();
+}
+
+// Tiles of a product: the warps a phase gives it.
+SKL_DEV int tc_tiles(int m, int n) { return ((m + 15) >> 4) * ((n + 7) >> 3); }
+
+// Off-diagonal blocks of X = U^{-1} (upper) and, when L is given, of Y =
+// L^{-1} (unit lower), np x np (np a multiple of 16, at most 64), once the
+// 16 x 16 diagonal blocks hold the inverses: recursive doubling,
+//   [A B; 0 C]^{-1} = [A^{-1}, -A^{-1} B C^{-1}; 0, C^{-1}],
+//   [A 0; B C]^{-1} = [A^{-1}, 0; -C^{-1} B A^{-1}, C^{-1}],
+// with every pair of a level (and the U and L pairs) in one phase of warp
+// tiles: two block barriers per product level instead of two per product.
+// tmp holds 64 x 36 (ldt = 36): U pairs in rows 0..31, L pairs in 32..63,
+// pair q of a level at column 16 q.
+SKL_DEV void inv_offdiag_tc(const float* U, int ldu, float* X, int ldx, const float* L, int ldl, float* Y,
+                            int ldy, int np, float* tmp, int ldt)
+{
+    const int warp = threadIdx.x >> 5;
+    for (int w = kDB; w < np; w *= 2) {
+        // phase 1: tmp_U = U_12 X_22, tmp_L = L_21 Y_11 for every pair
+        {
+            float acc[4];
+            int i0 = 0, c0 = 0, m = 0, n = 0;
+            float* C = nullptr;
+            bool act = false;
+            int base = 0;
+            for (int p0 = 0; p0 + w < np; p0 += 2 * w) {
+                const int n2 = min(w, np - p0 - w), q = p0 / (2 * w);
+                const int tU = tc_tiles(w, n2);
+                if (warp >= base && warp < base + tU) {
+                    act = tc_tile<false, kMFull, false, kMUpper>(warp - base, w, n2, n2, U + p0 * ldu + p0 + w,
+                                                                 ldu, X + (p0 + w) * ldx + p0 + w, ldx,
+                                                                 nullptr, acc, i0, c0);
+                    C = tmp + 16 * q;
+                    m = w;
+                    n = n2;
+                }
+                base += tU;
+                if (L) {
+                    const int tL = tc_tiles(n2, w);
+                    if (warp >= base && warp < base + tL) {
+                        act = tc_tile<false, kMFull, false, kMLowerUnit>(warp - base, n2, w, w,
+                                                                         L + (p0 + w) * ldl + p0, ldl,
+                                                                         Y + p0 * ldy + p0, ldy, nullptr, acc,
+                                                                         i0, c0);
+                        C = tmp + 32 * ldt + 16 * q;
+                        m = n2;
+                        n = w;
+                    }
+                    base += tL;
+                }
             }
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                bh[e] = tf32_rna(bv[e]);
-                bl[e] = tf32_rna(bv[e] - __uint_as_float(bh[e]));
+            __syncthreads();
+            if (act) tc_tile_store<false>(m, n, i0, c0, acc, 1.f, C, ldt, nullptr, 0, nullptr);
+            __syncthreads();
+        }
+        // phase 2: X_12 = -X_11 tmp_U, Y_21 = -Y_22 tmp_L
+        {
+            float acc[4];
+            int i0 = 0, c0 = 0, m = 0, n = 0, ldc = 0;
+            float* C = nullptr;
+            bool act = false;
+            int base = 0;
+            for (int p0 = 0; p0 + w < np; p0 += 2 * w) {
+                const int n2 = min(w, np - p0 - w), q = p0 / (2 * w);
+                const int tU = tc_tiles(w, n2);
+                if (warp >= base && warp < base + tU) {
+                    act = tc_tile<false, kMUpper, false, kMFull>(warp - base, w, n2, w, X + p0 * ldx + p0, ldx,
+                                                                 tmp + 16 * q, ldt, nullptr, acc, i0, c0);
+                    C = X + p0 * ldx + p0 + w;
+                    ldc = ldx;
+                    m = w;
+                    n = n2;
+                }
+                base += tU;
+                if (L) {
+                    const int tL = tc_tiles(n2, w);
+                    if (warp >= base && warp < base + tL) {
+                        act = tc_tile<false, kMLowerUnit, false, kMFull>(warp - base, n2, w, n2,
+                                                                         Y + (p0 + w) * ldy + p0 + w, ldy,
+                                                                         tmp + 32 * ldt + 16 * q, ldt, nullptr,
+                                                                         acc, i0, c0);
+                        C = Y + (p0 + w) * ldy + p0;
+                        ldc = ldy;
+                        m = n2;
+                        n = w;
+                    }
+                    base += tL;
+                }
             }
-            mma_tf32_16x8x8(acc, al, bh);
-            mma_tf32_16x8x8(acc, ah, bl);
-            mma_tf32_16x8x8(acc, ah, bh);
+            __syncthreads();
+            if (act) tc_tile_store<false>(m, n, i0, c0, acc, -1.f, C, ldc, nullptr, 0, nullptr);
+            __syncthreads();
         }
     }
-    __syncthreads();
-    if (act) {
-        // C fragment: (g, 2 tig) (g, 2 tig + 1) (g + 8, 2 tig) (g + 8, 2 tig + 1)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int i = i0 + g + (e >> 1) * 8, c = c0 + 2 * tig + (e & 1);
-            if (i >= m || c >= n) continue;
-            const float v = alpha * acc[e];
-            if (Cg) {
-                Cg[i + (int64_t)c * ldg] = v;
-                if (i == c) tau[i] = v;
-            } else if (ACC) {
-                C[i * ldc + c] += v;
-            } else {
-                C[i * ldc + c] = v;
-            }
-        }
-    }
-    __syncthreads();
 }
 
 // 2 x 2 tiles for FP64: 4 x 4 tiles measured slower inside the small kernels
@@ -486,7 +599,10 @@ SKL_DEV void chol_inv_small(T* G, int ldx, int np, const T* __restrict__ mass, T
         if (c < i) G[i * ldx + c] = T(0);
     }
     __syncthreads();
-    inv_upper_offdiag<T>(G, ldx, Xs, ldx, np, tmp, ldt);
+    if constexpr (std::is_same<T, float>::value)
+        inv_offdiag_tc(G, ldx, Xs, ldx, nullptr, 0, nullptr, 0, np, tmp, ldt);
+    else
+        inv_upper_offdiag<T>(G, ldx, Xs, ldx, np, tmp, ldt);
 }
 
 // Modified LU of A (np x np) in place (L strict lower, U upper), signs to
@@ -509,27 +625,51 @@ SKL_DEV void mlu_inv_small(T* A, int ldx, int np, T* sg, T* Z, T* tmp, int ldt)
         if (rest > 0) {
             T* A12 = A11 + kDB;
             T* A21 = A11 + kDB * ldx;
-            blk_mul<T, false, kMLowerUnit, false, kMFull>(kDB, rest, kDB, Z11, ldx, A12, ldx, nullptr,
-                                                         T(1), A12, ldx);
-            blk_mul<T, false, kMFull, false, kMUpper>(rest, kDB, kDB, A21, ldx, Z11, ldx, nullptr, T(1),
-                                                     A21, ldx);
+            if constexpr (std::is_same<T, float>::value) {
+                // U12 = L11^{-1} A12 and L21 = A21 U11^{-1} in one phase
+                const int warp = threadIdx.x >> 5, t12 = tc_tiles(kDB, rest);
+                float acc[4];
+                int i0 = 0, c0 = 0;
+                bool act;
+                if (warp < t12)
+                    act = tc_tile<false, kMLowerUnit, false, kMFull>(warp, kDB, rest, kDB, Z11, ldx, A12, ldx,
+                                                                     nullptr, acc, i0, c0);
+                else
+                    act = tc_tile<false, kMFull, false, kMUpper>(warp - t12, rest, kDB, kDB, A21, ldx, Z11,
+                                                                 ldx, nullptr, acc, i0, c0);
+                __syncthreads();
+                if (act) {
+                    if (warp < t12) tc_tile_store<false>(kDB, rest, i0, c0, acc, 1.f, A12, ldx, nullptr, 0, nullptr);
+                    else tc_tile_store<false>(rest, kDB, i0, c0, acc, 1.f, A21, ldx, nullptr, 0, nullptr);
+                }
+                __syncthreads();
+            } else {
+                blk_mul<T, false, kMLowerUnit, false, kMFull>(kDB, rest, kDB, Z11, ldx, A12, ldx, nullptr,
+                                                             T(1), A12, ldx);
+                blk_mul<T, false, kMFull, false, kMUpper>(rest, kDB, kDB, A21, ldx, Z11, ldx, nullptr, T(1),
+                                                         A21, ldx);
+            }
             blk_mul<T, false, kMFull, false, kMFull, true>(rest, rest, kDB, A21, ldx, A12, ldx, nullptr,
                                                            T(-1), A11 + kDB * ldx + kDB, ldx);
         }
     }
-    inv_upper_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
-    inv_unit_lower_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
+    if constexpr (std::is_same<T, float>::value) {
+        inv_offdiag_tc(A, ldx, Z, ldx, A, ldx, Z, ldx, np, tmp, ldt);
+    } else {
+        inv_upper_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
+        inv_unit_lower_offdiag<T>(A, ldx, Z, ldx, np, tmp, ldt);
+    }
 }
 
 // Padded size of the b x b algebra and the workspace layout of the small
-// kernels: four np x np blocks (row-major, ld = np + 4), a 32 x 36 product
+// kernels: four np x np blocks (row-major, ld = np + 4), a 64 x 36 product
 // scratch, and 3 np entries.
 __host__ __device__ inline int small_np(int b) { return (b + kDB - 1) / kDB * kDB; }
 template <typename T>
 size_t chol_small_smem_bytes(int b)
 {
     const size_t np = (size_t)small_np(b);
-    return (4 * np * (np + 4) + 32 * 36 + 3 * np) * sizeof(T) + 256;
+    return (4 * np * (np + 4) + 64 * 36 + 3 * np) * sizeof(T) + 256;
 }
 
 // Pass 1: R1 and X1 = R1^{-1} from G1 (column-major b x b, ldg = b).  Sets
@@ -545,7 +685,7 @@ k_chol_small1(const T* __restrict__ G, int b, T* __restrict__ R1, T* __restrict_
     T* S0 = (T*)smem_raw;
     T* S1 = S0 + (size_t)np * LDX;
     T* tmp = S1 + (size_t)np * LDX;
-    T* mass = tmp + 32 * 36;
+    T* mass = tmp + 64 * 36;
     __shared__ int s_bad;
     const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
     if (threadIdx.x == 0) s_bad = 0;
@@ -586,8 +726,8 @@ k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T
     T* S1 = S0 + (size_t)np * LDX;               // G2 -> R2 -> L^{-1} \ U^{-1}
     T* S2 = S1 + (size_t)np * LDX;               // X2 -> W
     T* S3 = S2 + (size_t)np * LDX;               // Q(0:b,:) -> Q1 -> L \ U
-    T* tmp = S3 + (size_t)np * LDX;              // 32 x 36 product scratch
-    T* Sg = tmp + 32 * 36;
+    T* tmp = S3 + (size_t)np * LDX;              // 64 x 36 product scratch
+    T* Sg = tmp + 64 * 36;
     T* mass = Sg + np;
     __shared__ int s_bad;
     const T eps = std::is_same<T, float>::value ? T(5.9604645e-08) : T(1.1102230246251565e-16);
