@@ -526,10 +526,12 @@ def run_ours(args, rank, world):
             kernels[name] = {"launches": int(prof_n[q]), "ms_per_launch": per,
                              "total_ms": float(prof_ms[q]), "alg_bytes": int(nbytes),
                              "achieved_gbs": ach, "frac": ach / hbm_peak}
-    # the sample QRP (k_yqrp, one launch per panel but the last): live event
-    # time per launch from the QR sub-step events; algorithmic bytes = one read
-    # of the (nb+16) x (d-j) FP32 sample block per launch (nb = 64)
-    nb, nbp = 64, 80
+    # the sample QRP (k_yqrp_reg, one launch per panel but the last): live
+    # event time per launch from the QR sub-step events; algorithmic bytes =
+    # one read of the (nb+16) x (d-j) FP32 sample block per launch, nb the
+    # panel width the solve used
+    nb = int(last.tuned[1]) or 64
+    nbp = nb + 16
     mrows = int(last.sketch_rows)
     mn = min(mrows, d)
     yq_js = [j for j in range(0, mn, nb) if j + nb < mrows and j + nb < d]
@@ -539,10 +541,10 @@ def run_ours(args, rank, world):
         yq_bytes = int(np.mean([4 * nbp * (d - j) for j in yq_js]))
         per = yq_ms / yq_n
         ach = yq_bytes / (per * 1e-3) / 1e9
-        kernels["k_yqrp"] = {"launches": yq_n, "ms_per_launch": per, "total_ms": yq_ms,
-                             "alg_bytes": yq_bytes, "achieved_gbs": ach, "frac": ach / hbm_peak,
-                             "note": "latency-bound: 64 dependent pivot steps per launch, each a "
-                                     "16-CTA cluster barrier"}
+        kernels["k_yqrp_reg"] = {"launches": yq_n, "ms_per_launch": per, "total_ms": yq_ms,
+                                 "alg_bytes": yq_bytes, "achieved_gbs": ach, "frac": ach / hbm_peak,
+                                 "note": "latency-bound: %d dependent pivot steps per launch, each an "
+                                         "mbarrier-completed candidate exchange among 16 CTAs" % nb}
     if P.kind == "dense":
         # DHT + hash: read A once (FP64), write the m x d FP32 sketch
         sk_ms = float(np.sum([i.t_sketch_ms for i in infos]))

@@ -137,9 +137,10 @@ typedef struct {
     /* mixed dense path: 1 if A held values outside [2^-100, 2^100] in
        magnitude and the solve ran on the FP64 path instead */
     int fp64_fallback;
-    /* launch shapes this solve used when autotuned (0 = the fixed heuristic):
-       sketch block size, CPQR panel width, lanes per CSR row of A z, lanes per
-       CSC column of A^T u */
+    /* launch shapes this solve used: sketch block size, CPQR panel width,
+       lanes per CSR row of A z, lanes per CSC column of A^T u.  The panel width
+       is always reported on the mixed path (0 on the FP64 path); the others
+       are 0 unless autotuned (0 = the fixed heuristic) */
     int64_t tuned[4];
 } skl_info;
 

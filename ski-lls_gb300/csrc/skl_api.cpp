@@ -510,7 +510,7 @@ static void sparse_pipeline(Context& C, cudaStream_t st, const SparseDev& in, do
         P.lanes_t = tuned.lanes_t;
     }
     info.tuned[0] = tuned.sketch_threads;
-    info.tuned[1] = tuned.nb;
+    info.tuned[1] = mixed ? cpqr_panel_width(m, d, tuned.nb) : 0;   // the width the FP32 CPQR used
     info.tuned[2] = tuned.lanes_n;
     info.tuned[3] = tuned.lanes_t;
     // ---- explicit sketch solution xs = D P1 M c (resolved columns only) ----
