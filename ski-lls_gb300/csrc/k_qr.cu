@@ -1436,7 +1436,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     // permutation waits for the side stream's events.  (R12 is the first b
     // rows of the trailing update, done ahead of the other rows.)
     cudaStream_t side = nullptr;
-    cudaEvent_t evV = nullptr, evR = nullptr, evY = nullptr, evG = nullptr;
+    cudaEvent_t evV = nullptr, evR = nullptr, evY = nullptr, evG = nullptr, evD = nullptr;
     if (pivoting) {
         int lo = 0, hi = 0;
         SKL_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
@@ -1445,17 +1445,18 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         SKL_CUDA(cudaEventCreateWithFlags(&evR, cudaEventDisableTiming));
         SKL_CUDA(cudaEventCreateWithFlags(&evY, cudaEventDisableTiming));
         SKL_CUDA(cudaEventCreateWithFlags(&evG, cudaEventDisableTiming));
+        SKL_CUDA(cudaEventCreateWithFlags(&evD, cudaEventDisableTiming));
     }
     struct StreamGuard {
         cudaStream_t s;
-        cudaEvent_t ev[4];
+        cudaEvent_t ev[5];
         ~StreamGuard()
         {
             for (cudaEvent_t e : ev)
                 if (e) cudaEventDestroy(e);
             if (s) cudaStreamDestroy(s);
         }
-    } guard{side, {evV, evR, evY, evG}};
+    } guard{side, {evV, evR, evY, evG, evD}};
     QrTimer tms{qr_prof, {}, {}, 0, side};
     bool side_pending = false;
 
@@ -1596,7 +1597,14 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             const bool next_last = (jn + nb >= m) || (jn + nb >= d);
             if (jn < mn && !next_last) {
                 const int bn = (int)std::min<int64_t>(nb, std::min<int64_t>(d - jn, m - jn));
+                // evD: the sample is downdated and the sample QRP is next on the
+                // (high-priority) side stream.  The trailing update waits for it:
+                // launched first, the update's CTAs would fill every GPC and the
+                // QRP's 16-CTA cluster could start only after the update drained;
+                // launched after it, the QRP holds one GPC and the two overlap.
+                SKL_CUDA(cudaEventRecord(evD, side));
                 launch_yqrp(jn, bn, (int)(d - jn), side, tms);
+                SKL_CUDA(cudaStreamWaitEvent(st, evD, 0));
             }
             SKL_CUDA(cudaEventRecord(evY, side));
             side_pending = true;
