@@ -12,7 +12,8 @@ sparse problem, s = 2, m = 1.7 d, LSQR tolerance 1e-10, mixed precision.
 
 Workloads: sparse_uniform_20000x1000, dense_kappa1e6_40000x4000,
 sparse_illcond_120000x5000 (default), sparse_zipf_1000000x10000,
-batched_sparse.  Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): every
+batched_sparse, and dense_blendenpik_40000x4000 (the Blendenpik comparison
+solver on the dense matrix).  Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): every
 rank solves its own replica (the single-problem path does not shard); the
 reported time is the max over ranks.  The reference arm (--impl reference)
 times the CPU oracle, a restatement of the reference algorithm, on the host
@@ -188,8 +189,15 @@ def make_workload(name):
     return w, A, b, time.perf_counter() - t0
 
 
+def oracle_kind(w):
+    """Which oracle solver a workload runs: "sparse", "dense" or "blendenpik"."""
+    return "blendenpik" if w.get("solver") == "blendenpik" else w["kind"]
+
+
 def oracle_solve(kind, A, b, gamma, k):
     import ski_lls_oracle as orc
+    if kind == "blendenpik":
+        return orc.ls_dense_blendenpik(A, b, gamma, it_tol=IT_TOL, seed=1)
     if kind == "sparse":
         return orc.ls_sparse_spqr(A.shape[0], A.shape[1], A.indptr, A.indices, A.data, b, gamma,
                                   k, it_tol=IT_TOL, rng=orc.Rng(1))
@@ -279,12 +287,12 @@ def run_reference(args, rank):
     warm = min(args.warmup, 1)
     steps = max(1, min(args.steps, 5))
     for _ in range(warm):
-        oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
+        oracle_solve(oracle_kind(w), A, b, w["gamma"], w["k"])
     times = []
     out = None
     for _ in range(steps):
         t0 = time.perf_counter()
-        out = oracle_solve(w["kind"], A, b, w["gamma"], w["k"])
+        out = oracle_solve(oracle_kind(w), A, b, w["gamma"], w["k"])
         times.append(time.perf_counter() - t0)
     v = statistics.median(times)
     cores = os.cpu_count()
@@ -379,14 +387,20 @@ class SparseOnDevice:
 class DenseOnDevice:
     kind = "dense"
 
-    def __init__(self, A, b, dev, torch):
+    def __init__(self, A, b, dev, torch, blendenpik=False):
         self.A, self.b = A, b
         self.n, self.d = A.shape
+        self.blendenpik = blendenpik   # ls_dense_blendenpik instead of the hashing solver
         self.Ad = torch.from_numpy(np.asfortranarray(A).ravel(order="F")).to(dev)
         self.bd = torch.from_numpy(b.astype(np.float64)).to(dev)
         self.xd = torch.zeros(self.d, dtype=torch.float64, device=dev)
 
     def solve(self, skl, precision, profile, stream, device, gamma, k):
+        if self.blendenpik:
+            return skl.dense_blendenpik_device(self.n, self.d, self.Ad.data_ptr(), self.n,
+                                               self.bd.data_ptr(), self.xd.data_ptr(), gamma,
+                                               precision=precision, seed=1, it_tol=IT_TOL,
+                                               stream=stream, profile=profile, device=device)
         return skl.dense_solve_device(self.n, self.d, self.Ad.data_ptr(), self.n,
                                       self.bd.data_ptr(), self.xd.data_ptr(), gamma, k,
                                       precision=precision, seed=1, it_tol=IT_TOL, stream=stream,
@@ -398,10 +412,11 @@ class DenseOnDevice:
         hb = torch.from_numpy(self.b.astype(np.float64)).pin_memory()
         hxo = torch.zeros(self.d, dtype=torch.float64).pin_memory()
         n, d = self.n, self.d
+        entry = skl.lib().skl_dense_blendenpik_solve if self.blendenpik else skl.lib().skl_dense_solve
 
         def call():
             info = skl.SklInfo()
-            rc = skl.lib().skl_dense_solve(ctypes.c_void_p(hA.data_ptr()), n, n, d,
+            rc = entry(ctypes.c_void_p(hA.data_ptr()), n, n, d,
                                            ctypes.c_void_p(hb.data_ptr()),
                                            ctypes.c_void_p(hxo.data_ptr()), ctypes.byref(opts),
                                            ctypes.byref(info))
@@ -427,6 +442,12 @@ class DenseOnDevice:
                       "256 MB buffer written between steps"}
 
 
+def on_device(w, A, b, dev, torch):
+    if w["kind"] == "sparse":
+        return SparseOnDevice(A, b, dev, torch)
+    return DenseOnDevice(A, b, dev, torch, blendenpik=w.get("solver") == "blendenpik")
+
+
 def profile_one(args):
     """--profile-one: ONE solve of the workload on device-resident inputs with
     the library's per-kernel events on, no warm-up: a short, fixed command for
@@ -436,7 +457,7 @@ def profile_one(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     w, A, b, _ = make_workload(args.workload)
-    P = (SparseOnDevice if w["kind"] == "sparse" else DenseOnDevice)(A, b, dev, torch)
+    P = on_device(w, A, b, dev, torch)
     info = None
     for _ in range(max(1, args.repeats)):
         info = P.solve(skl, args.precision, 1, None, 0, w["gamma"], w["k"])
@@ -457,7 +478,7 @@ def run_ours(args, rank, world):
     w, A, b, gen_s = make_workload(args.workload)
     gamma, k = w["gamma"], w["k"]
     hbm_peak, _, peak_kind = load_peaks()
-    P = (SparseOnDevice if w["kind"] == "sparse" else DenseOnDevice)(A, b, dev, torch)
+    P = on_device(w, A, b, dev, torch)
     if args.autotune and P.kind == "sparse":
         P.autotune = 1
     n, d = P.n, P.d
@@ -535,8 +556,8 @@ def run_ours(args, rank, world):
     mrows = int(last.sketch_rows)
     mn = min(mrows, d)
     yq_js = [j for j in range(0, mn, nb) if j + nb < mrows and j + nb < d]
-    if yq_js:
-        yq_ms = float(np.sum([i.qr_prof_ms[0] for i in infos]))
+    yq_ms = float(np.sum([i.qr_prof_ms[0] for i in infos]))
+    if yq_js and yq_ms > 0:   # no sample QRP on the unpivoted (Blendenpik) path
         yq_n = len(yq_js) * len(infos)
         yq_bytes = int(np.mean([4 * nbp * (d - j) for j in yq_js]))
         per = yq_ms / yq_n
@@ -592,7 +613,7 @@ def run_ours(args, rank, world):
     cpu = None
     oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, oracle = cpu_baseline_run(P.kind, args.workload, A, b, gamma, k)
+        cpu, oracle = cpu_baseline_run(oracle_kind(w), args.workload, A, b, gamma, k)
 
     if rank != 0:
         return

@@ -13,6 +13,10 @@
  *                                                        src/ls_dense_hashing_blendenpik.cpp:23-149
  *   skl_dense_solve with opts.use_cpqr = 0
  *                     <- ls_dense_hashing_blendenpik_noCPQR  include/ski-lls.h:19-21
+ *   skl_dense_blendenpik_solve
+ *                     <- ls_dense_blendenpik            include/blendenpik.hpp:31-33,
+ *                                                        src/ls_dense_blendenpik.cpp:21-70
+ *   skl_subsample_rows <- random_sample's row draw      src/dense_helpers.cpp:19-39
  *   skl_srand / skl_hash_generate
  *                     <- srand() + gen_hashing_matrix   src/sparse_helpers.cpp:66-116
  *   skl_sketch_sparse <- sparse_sketch(A,k,gamma,b,bs)  src/sketching.cpp:90-112
@@ -193,7 +197,29 @@ skl_status skl_dense_solve_device(const double* A_dev, int64_t lda, int64_t n, i
                                   const double* b_dev, double* x_dev, const skl_opts* opts,
                                   skl_info* info);
 
+/* Blendenpik (Avron, Maymounkov and Toledo's solver, the reference's comparison
+ * solver): the sketch keeps m = ceil(gamma*d) rows of the randomized DHT of A
+ * (random signs D, orthonormal DHT, rows drawn without replacement) instead of
+ * hashing them; unpivoted QR of the sample; LSQR preconditioned by R from
+ * x = 0; x = R^{-1} y; rank = d.  Uses opts->gamma, it_tol, max_it, wisdom,
+ * seed, precision, device and stream; k, use_cpqr, abs_tol and rcond do not
+ * apply.  Seeding as the reference's: the signs and the row draw each start
+ * from the same reseeded stream (srand(time(NULL)) before each, or opts->seed). */
+skl_status skl_dense_blendenpik_solve(const double* A, int64_t lda, int64_t n, int64_t d,
+                                      const double* b, double* x, const skl_opts* opts,
+                                      skl_info* info);
+
+/* Same with A, b, x in device memory. */
+skl_status skl_dense_blendenpik_solve_device(const double* A_dev, int64_t lda, int64_t n,
+                                             int64_t d, const double* b_dev, double* x_dev,
+                                             const skl_opts* opts, skl_info* info);
+
 /* ------------------------------------------------------- building blocks */
+
+/* The m rows (of N) random_sample keeps, drawn from the library stream
+ * (seed_mode/seed as in skl_opts): rows[i], i < m, distinct, in draw order.
+ * Bit-exact with select_k_from_n over 0..N-1 for the same stream. */
+skl_status skl_subsample_rows(int64_t N, int64_t m, int seed_mode, uint32_t seed, int64_t* rows);
 
 /* Hash rows and values of an m x n s-hashing matrix drawn from the library
  * stream (seed_mode/seed as in skl_opts): rows[i*k+j], vals[i*k+j] =

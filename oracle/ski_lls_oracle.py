@@ -26,6 +26,11 @@ Pieces and the reference code they follow:
                                 HQRRP (d >= 1000) is replaced by dgeqp3, which
                                 is what the reference itself calls for d < 1000
                                 (hqrrp/.../NoFLA_HQRRP_WY_blk_var4_skint.c:205-208).
+* ``ls_dense_blendenpik``       src/ls_dense_blendenpik.cpp:21-70 with
+                                rand_subsampled_dct / random_sample
+                                (src/dense_helpers.cpp:19-59); dense_qr is
+                                numpy's QR (LAPACK dgeqrf, as the reference)
+* ``random_sample_rows``        select_k_from_n, src/sparse_helpers.cpp:74-86
 * ``lsqr``                      src/IterSolver.cpp:160-305 (C)
 """
 from __future__ import annotations
@@ -371,6 +376,50 @@ def ls_dense_hashing_blendenpik_noCPQR(A, b, gamma, k, it_tol=1e-6, max_it=10000
                        dense=A)
     x = usolve(R, y, 1, 0.0)
     return dict(m=m, rank=d, x=x, flag=flag, it=it, SA=SA)
+
+
+def random_sample_rows(rng: Rng, N: int, m: int) -> np.ndarray:
+    """Rows random_sample keeps (src/dense_helpers.cpp:19-39): gen_0_to_n(N),
+    then select_k_from_n(N, m) (src/sparse_helpers.cpp:74-86), the first m
+    entries of the partially shuffled array."""
+    if not 0 <= m <= N:
+        raise ValueError("random_sample: need 0 <= m <= N")
+    idx = np.arange(N, dtype=np.int64)
+    for i in range(m):
+        j = rng.next() % (N - i) + i
+        idx[i], idx[j] = idx[j], idx[i]
+    return idx[:m].copy()
+
+
+def ls_dense_blendenpik(A, b, gamma, it_tol=1e-6, max_it=10000, seed=1, N=None):
+    """Restates ls_dense_blendenpik (src/ls_dense_blendenpik.cpp:21-70):
+    rand_subsampled_dct (src/dense_helpers.cpp:42-59) -- signs from the stream
+    seeded with `seed`, the orthonormal DHT, then m = ceil(gamma d) rows drawn
+    from the stream seeded again with the same value (the reference calls
+    srand(time(NULL)) before each) --, unpivoted QR (dense_qr), LSQR on (A, b)
+    from zero preconditioned by R, x = R^{-1} y, rank = d."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, d = A.shape
+    if n < d:
+        raise RuntimeError("Matrix is not overdetermined.")
+    m = int(math.ceil(d * gamma))
+    N = n if N is None else N
+    t0 = time.perf_counter()
+    rng = Rng(seed)
+    D = rand_signs(rng, n)
+    Y = unitary_dht(A, D, N)
+    rng.seed(seed)
+    rows = random_sample_rows(rng, N, m)
+    SA = np.asfortranarray(Y[rows, :])
+    t1 = time.perf_counter()
+    R = np.asfortranarray(np.linalg.qr(SA, mode="r")[:d, :d])
+    t2 = time.perf_counter()
+    y, flag, it = lsqr(n, d, np.asarray(b, dtype=np.float64), np.arange(d), R, it_tol, max_it,
+                       dense=A)
+    x = usolve(R, y, 1, 0.0)
+    t3 = time.perf_counter()
+    return dict(m=m, rank=d, x=x, flag=flag, it=it, SA=SA, rows=rows,
+                phases_s={"sketch": t1 - t0, "qr": t2 - t1, "lsqr": t3 - t2})
 
 
 def backward_error(A_mv, A_rmv, fro, x, b):

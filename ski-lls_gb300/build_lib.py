@@ -53,7 +53,7 @@ def build(verbose=False, jobs=None):
 
 
 CLI_DIR = os.path.join(HERE, "cli")
-CLI_TOOLS = ("ls_qr", "ls_blendenpik_hashing")
+CLI_TOOLS = ("ls_qr", "ls_blendenpik_hashing", "ls_blendenpik")
 
 
 def build_cli():

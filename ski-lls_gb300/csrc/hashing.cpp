@@ -216,6 +216,21 @@ void gen_signs(int64_t n, double* D)
     for (int64_t i = 0; i < n; ++i) D[i] = (g_rng.next() & 1u) ? 1.0 : -1.0;
 }
 
+// Caller holds the lock.  Step i draws t = rand() % (N - i) + i and swaps
+// entries i and t of the index array; entry i is final after step i.
+void gen_subsample(int64_t N, int64_t m, uint32_t* rows)
+{
+    std::vector<uint32_t> idx((size_t)N);
+    for (int64_t i = 0; i < N; ++i) idx[(size_t)i] = (uint32_t)i;
+    for (int64_t i = 0; i < m; ++i) {
+        const uint32_t t = (uint32_t)(g_rng.next() % (uint32_t)(N - i)) + (uint32_t)i;
+        const uint32_t a = idx[t];
+        idx[t] = idx[(size_t)i];
+        idx[(size_t)i] = a;
+        rows[i] = a;
+    }
+}
+
 // NoFLA_Normal_random_matrix / NoFLA_Normal_random_number
 // (hqrrp/lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4_skint.c:584-624):
 // pairs (c1, c2) uniform in (-1,1)^2 are drawn until 0 < c1^2+c2^2 < 1; each
@@ -242,6 +257,19 @@ void rng_hqrrp_advance(int64_t rows, int64_t cols)
 }  // namespace skl
 
 extern "C" void skl_srand(uint32_t seed) { skl::rng_srand(seed); }
+
+extern "C" skl_status skl_subsample_rows(int64_t N, int64_t m, int seed_mode, uint32_t seed,
+                                         int64_t* rows)
+{
+    if (N <= 0 || m < 0 || m > N || N > 0x7fffffff || (m > 0 && !rows)) return SKL_ERR_INVALID;
+    std::vector<uint32_t> r((size_t)m);
+    if (seed_mode) skl::rng_srand(seed);
+    skl::rng_lock();
+    skl::gen_subsample(N, m, r.data());
+    skl::rng_unlock();
+    for (int64_t i = 0; i < m; ++i) rows[i] = (int64_t)r[(size_t)i];
+    return SKL_OK;
+}
 
 extern "C" skl_status skl_hash_generate(int64_t m, int64_t n, int64_t k, int seed_mode,
                                         uint32_t seed, int64_t* rows, double* vals)

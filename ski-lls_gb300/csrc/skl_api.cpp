@@ -853,9 +853,14 @@ static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double*
 }
 
 // --------------------------------------------------------- dense solve ---
-// ls_dense_hashing_blendenpik (src/ls_dense_hashing_blendenpik.cpp:23-149) and,
-// with use_cpqr = 0, ls_dense_hashing_blendenpik_noCPQR
-// (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-59).
+// ls_dense_hashing_blendenpik (src/ls_dense_hashing_blendenpik.cpp:23-149),
+// with use_cpqr = 0 ls_dense_hashing_blendenpik_noCPQR
+// (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-59), and with sample_rows
+// ls_dense_blendenpik (src/ls_dense_blendenpik.cpp:21-70), whose sketch
+// rand_subsampled_dct (src/dense_helpers.cpp:42-59) keeps m rows of the
+// transform instead of hashing them: hh then holds those m rows, each row its
+// own bucket with sign + and k = 1 (so the gather's 1/k is 1), and the rest is
+// the noCPQR pipeline.
 
 // Returns false (nothing solved) when the mixed path meets values outside its
 // range; the caller then runs the FP64 pipeline.
@@ -864,7 +869,7 @@ static bool dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
                            int64_t d, const double* b, double* x_dev, const skl_opts& o,
                            skl_info& info, bool timing_upload, std::thread* host_thread,
                            const std::vector<double>* hD, const std::vector<uint32_t>* hh,
-                           int64_t N)
+                           int64_t N, bool sample_rows)
 {
     const bool mixed = std::is_same<T, float>::value;
     const bool cpqr_on = o.use_cpqr != 0;
@@ -928,8 +933,15 @@ static bool dense_pipeline(Context& C, cudaStream_t st, const double* A, int64_t
     if (mixed && (read_status(C, st) & kStatusRange)) return false;
     if (host_thread->joinable()) host_thread->join();
     SKL_CUDA(cudaMemcpyAsync(Dd, hD->data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
-    SKL_CUDA(cudaMemcpyAsync(hidx, hh->data(), N * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
-    build_buckets(hidx, N, (int)k, m, bptr, bent, (int*)work, st);
+    if (sample_rows) {
+        std::vector<int> bp((size_t)m + 1);
+        for (int64_t h = 0; h <= m; ++h) bp[(size_t)h] = (int)h;
+        SKL_CUDA(cudaMemcpyAsync(bptr, bp.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+        SKL_CUDA(cudaMemcpyAsync(bent, hh->data(), m * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    } else {
+        SKL_CUDA(cudaMemcpyAsync(hidx, hh->data(), N * k * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+        build_buckets(hidx, N, (int)k, m, bptr, bent, (int*)work, st);
+    }
     SKL_CUDA(cudaEventRecord(ev[2], st));
     // ---- sketch: DHT + hash of A (and b) ----
     dht_hash<T>(A, lda, n, d, Dd, N, bptr, bent, (int)k, m, SA, ld, nullptr, 0, work, work_bytes, st);
@@ -1060,11 +1072,11 @@ static void dense_pipeline_any(Context& C, cudaStream_t st, const double* A, int
                                int64_t n, int64_t d, const double* b, double* x_dev,
                                const skl_opts& o, skl_info& info, bool timing_upload,
                                std::thread* host_thread, const std::vector<double>* hD,
-                               const std::vector<uint32_t>* hh, int64_t N)
+                               const std::vector<uint32_t>* hh, int64_t N, bool sample_rows)
 {
     if (o.precision == SKL_PREC_MIXED &&
         dense_pipeline<float>(C, st, A, lda, n, d, b, x_dev, o, info, timing_upload, host_thread,
-                              hD, hh, N))
+                              hD, hh, N, sample_rows))
         return;
     const bool fell_back = o.precision == SKL_PREC_MIXED;
     if (fell_back) {
@@ -1074,15 +1086,22 @@ static void dense_pipeline_any(Context& C, cudaStream_t st, const double* A, int
     skl_opts o64 = o;
     o64.precision = SKL_PREC_FP64;
     dense_pipeline<double>(C, st, A, lda, n, d, b, x_dev, o64, info, timing_upload, host_thread,
-                           hD, hh, N);
+                           hD, hh, N, sample_rows);
 }
 
 static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t d, const double* b,
-                               double* x, const skl_opts* opts, skl_info* info, bool host)
+                               double* x, const skl_opts* opts, skl_info* info, bool host,
+                               bool sample_rows = false)
 {
     skl_opts o;
     if (opts) o = *opts;
     else fill_default(&o);
+    if (sample_rows) {
+        // Blendenpik: unpivoted QR, no early exit, one "bucket" per sampled row
+        o.k = 1;
+        o.use_cpqr = 0;
+        o.abs_tol = 0.0;
+    }
     check_opts(o);
     if (n < 0 || d < 0) fail(SKL_ERR_INVALID, "negative dimension");
     if (n < d) fail(SKL_ERR_NOT_OVERDETERMINED, "Matrix is not overdetermined.");
@@ -1101,11 +1120,13 @@ static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t 
     const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
     if (o.k > m) fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
     if (N > 0x7fffffff || m > 0x7fffffff) fail(SKL_ERR_INVALID, "problem too large");
+    if (sample_rows && m > N)
+        fail(SKL_ERR_INVALID, "the sample has more rows (ceil(gamma*d)) than the transform");
     // signs then hash from one reseeded stream (srand(time(NULL)) in the
     // reference, src/dense_helpers.cpp:92 and :12; seed 0 selects time)
     const uint32_t seed = o.seed ? o.seed : (uint32_t)time(nullptr);
     std::vector<double> hD((size_t)n);
-    std::vector<uint32_t> hh((size_t)(N * o.k));
+    std::vector<uint32_t> hh((size_t)(sample_rows ? m : N * o.k));
     double hash_ms = 0.0;
     const bool hqrrp_stream = o.use_cpqr && std::min(m, d) >= 1000;
     std::thread th([&]() {
@@ -1113,7 +1134,15 @@ static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t 
         rng_srand(seed);
         rng_lock();
         gen_signs(n, hD.data());
-        gen_hash_packed(m, N, o.k, hh.data());
+        if (sample_rows) {
+            // random_sample reseeds before its draw (src/dense_helpers.cpp:26)
+            rng_unlock();
+            rng_srand(seed);
+            rng_lock();
+            gen_subsample(N, m, hh.data());
+        } else {
+            gen_hash_packed(m, N, o.k, hh.data());
+        }
         rng_unlock();
         hash_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
@@ -1136,11 +1165,11 @@ static void dense_solve_common(const double* A, int64_t lda, int64_t n, int64_t 
             SKL_CUDA(cudaMemcpy2DAsync(Ad, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double),
                                        d, cudaMemcpyHostToDevice, st));
         SKL_CUDA(cudaMemcpyAsync(bd, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
-        dense_pipeline_any(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N);
+        dense_pipeline_any(C, st, Ad, n, n, d, bd, xd, o, inf, true, &th, &hD, &hh, N, sample_rows);
         SKL_CUDA(cudaMemcpyAsync(x, xd, d * sizeof(double), cudaMemcpyDeviceToHost, st));
         SKL_CUDA(cudaStreamSynchronize(st));
     } else {
-        dense_pipeline_any(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N);
+        dense_pipeline_any(C, st, A, lda, n, d, b, x, o, inf, false, &th, &hD, &hh, N, sample_rows);
     }
     // HQRRP reseeds the C library stream with srand(12) and draws its Gaussian
     // sample (hqrrp/.../NoFLA_HQRRP_WY_blk_var4_skint.c:390,414) when
@@ -1195,6 +1224,20 @@ skl_status skl_dense_solve_device(const double* A, int64_t lda, int64_t n, int64
                                   const double* b, double* x, const skl_opts* opts, skl_info* info)
 {
     return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, false); });
+}
+
+skl_status skl_dense_blendenpik_solve(const double* A, int64_t lda, int64_t n, int64_t d,
+                                      const double* b, double* x, const skl_opts* opts,
+                                      skl_info* info)
+{
+    return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, true, true); });
+}
+
+skl_status skl_dense_blendenpik_solve_device(const double* A, int64_t lda, int64_t n, int64_t d,
+                                             const double* b, double* x, const skl_opts* opts,
+                                             skl_info* info)
+{
+    return guarded([&] { dense_solve_common(A, lda, n, d, b, x, opts, info, false, true); });
 }
 
 void skl_finalize(void)

@@ -307,6 +307,10 @@ void rng_srand(uint32_t seed);
 void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx);
 // n random signs (+-1) as in gen_scaled_rand_signs (dense_helpers.cpp:7-16).
 void gen_signs(int64_t n, double* D);
+// The m rows random_sample keeps of N (dense_helpers.cpp:19-39): the first m
+// entries of 0..N-1 after select_k_from_n's partial Fisher-Yates shuffle
+// (sparse_helpers.cpp:74-86) on the library stream.  Caller holds the lock.
+void gen_subsample(int64_t N, int64_t m, uint32_t* rows);
 // Leaves the library stream where HQRRP leaves the C library's: srand(12),
 // then the rand() calls of Marsaglia's polar method for rows*cols normals.
 void rng_hqrrp_advance(int64_t rows, int64_t cols);

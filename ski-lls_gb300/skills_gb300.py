@@ -112,13 +112,16 @@ def lib():
         L.skl_batched_sparse_solve.argtypes = [i64, ctypes.POINTER(SklCsc), vp, vp,
                                                ctypes.POINTER(SklOpts), ctypes.POINTER(SklInfo), vp]
         L.skl_batched_sparse_solve.restype = ctypes.c_int
-        for name in ("skl_dense_solve", "skl_dense_solve_device"):
+        for name in ("skl_dense_solve", "skl_dense_solve_device", "skl_dense_blendenpik_solve",
+                     "skl_dense_blendenpik_solve_device"):
             f = getattr(L, name)
             f.argtypes = [vp, i64, i64, i64, vp, vp, ctypes.POINTER(SklOpts),
                           ctypes.POINTER(SklInfo)]
             f.restype = ctypes.c_int
         L.skl_hash_generate.argtypes = [i64, i64, i64, ctypes.c_int, ctypes.c_uint32, vp, vp]
         L.skl_hash_generate.restype = ctypes.c_int
+        L.skl_subsample_rows.argtypes = [i64, i64, ctypes.c_int, ctypes.c_uint32, vp]
+        L.skl_subsample_rows.restype = ctypes.c_int
         L.skl_sketch_sparse.argtypes = [ctypes.POINTER(SklCsc), vp, i64, i64, vp, vp, ctypes.c_int,
                                         ctypes.c_int, vp, vp]
         L.skl_sketch_sparse.restype = ctypes.c_int
@@ -330,6 +333,53 @@ def ls_dense_hashing_blendenpik_noCPQR(A, b, gamma=OVER_SAMPLING_RATIO, k=NNZ_PE
     (src/ls_dense_hashing_blendenpik_noCPQR.cpp:23-60): unpivoted QR, LSQR from 0."""
     return ls_dense_hashing_blendenpik(A, b, gamma, k, abs_tol=0.0, rcond=0.0, it_tol=it_tol,
                                        max_it=max_it, debug=debug, wisdom=wisdom, use_cpqr=0, **kw)
+
+
+def ls_dense_blendenpik(A, b, gamma=2.2, it_tol=IT_TOL, max_it=MAX_IT, debug=0, wisdom=0, *,
+                        precision="mixed", seed=0, device=0, stream=None, profile=0) -> Result:
+    """GPU counterpart of Blendenpik, ls_dense_blendenpik (src/ls_dense_blendenpik.cpp:21-70):
+    m = ceil(gamma*d) rows of the randomized DHT of A drawn without replacement
+    (rand_subsampled_dct, src/dense_helpers.cpp:42-59), unpivoted QR, LSQR
+    preconditioned by R from 0, rank = d.  gamma defaults to the reference
+    driver's 2.2 (test/ls_blendenpik.cpp:61).  seed=0 seeds from time(NULL)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, d = A.shape
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if b.shape != (n,):
+        raise ValueError("b must have A.m entries")
+    x = np.zeros(d, dtype=np.float64)
+    o = default_opts()
+    o.gamma, o.it_tol, o.max_it, o.wisdom = gamma, it_tol, max_it, wisdom
+    o.precision, o.seed_mode, o.seed = PREC[precision], 1, int(seed) & 0xFFFFFFFF
+    o.device, o.stream, o.profile = device, stream, profile
+    info = SklInfo()
+    _check(lib().skl_dense_blendenpik_solve(_ptr(A), max(n, 1), n, d, _ptr(b), _ptr(x),
+                                            ctypes.byref(o), ctypes.byref(info)))
+    return Result(x, info.rank, info.flag, info.it, info.as_dict())
+
+
+def dense_blendenpik_device(n, d, a_ptr, lda, b_ptr, xout_ptr, gamma, *, precision="mixed",
+                            seed=1, it_tol=IT_TOL, max_it=MAX_IT, stream=None, profile=0,
+                            device=0) -> SklInfo:
+    """skl_dense_blendenpik_solve_device on device pointers (column-major A, lda >= n)."""
+    o = default_opts()
+    o.gamma, o.it_tol, o.max_it = gamma, it_tol, max_it
+    o.precision = PREC[precision]
+    o.seed_mode, o.seed = 1, int(seed) & 0xFFFFFFFF
+    o.device, o.stream, o.profile = device, stream, profile
+    info = SklInfo()
+    _check(lib().skl_dense_blendenpik_solve_device(ctypes.c_void_p(a_ptr), lda, n, d,
+                                                   ctypes.c_void_p(b_ptr), ctypes.c_void_p(xout_ptr),
+                                                   ctypes.byref(o), ctypes.byref(info)))
+    return info
+
+
+def subsample_rows(N, m, seed=None):
+    """The m rows (of N, int64, draw order) random_sample keeps (src/dense_helpers.cpp:19-39)."""
+    rows = np.empty(m, dtype=np.int64)
+    mode, sd = (0, 0) if seed is None else (1, int(seed) & 0xFFFFFFFF)
+    _check(lib().skl_subsample_rows(N, m, mode, sd, _ptr(rows)))
+    return rows
 
 
 def hash_generate(m, n, k, seed=None):

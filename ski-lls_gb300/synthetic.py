@@ -133,4 +133,8 @@ WORKLOADS = {
     "sparse_illcond_120000x5000": dict(kind="sparse", gen=lambda: sparse_illcond()[:2],
                                        gamma=1.7, k=2),
     "sparse_zipf_1000000x10000": dict(kind="sparse", gen=lambda: sparse_zipf(), gamma=1.5, k=3),
+    # the Blendenpik comparison solver on the dense matrix above, at its
+    # driver's gamma (test/ls_blendenpik.cpp:61): 8,800 sampled rows
+    "dense_blendenpik_40000x4000": dict(kind="dense", gen=lambda: dense_kappa(), gamma=2.2, k=1,
+                                        solver="blendenpik"),
 }

@@ -3,6 +3,7 @@
 // Prints the solution, rank, flag and iterations on one line.
 #include <cstdio>
 #include "ski-lls.h"
+#include "blendenpik.hpp"
 
 int main()
 {
@@ -24,5 +25,11 @@ int main()
     Vec_d x2(A.n());
     ls_dense_hashing_blendenpik_noCPQR(A, b, x2, rank2, flag2, it2, 1.7, 1, 1e-12, MAX_IT, 0, WISDOM);
     std::printf("x2 %.10f %.10f rank %ld\n", x2(0), x2(1), rank2);
+    // Blendenpik (include/blendenpik.hpp:31-33): 3 of the 4 transformed rows
+    long rank3 = 0, it3 = 0;
+    int flag3 = 0;
+    Vec_d x3(A.n());
+    ls_dense_blendenpik(A, b, x3, rank3, flag3, it3, 1.5, 1e-12, MAX_IT, 0, WISDOM);
+    std::printf("x3 %.10f %.10f rank %ld\n", x3(0), x3(1), rank3);
     return 0;
 }

@@ -84,6 +84,24 @@ def test_hash_stream_large_draws_split_across_threads():
     np.testing.assert_array_equal(b_vals, v2)
 
 
+def test_subsample_rows_bit_exact_vs_oracle():
+    # random_sample's draw (src/dense_helpers.cpp:19-39): select_k_from_n over
+    # 0..N-1 on the reseeded stream; the stream then continues like rand()
+    for (N, m, seed) in ((10, 10, 1), (4000, 340, 5), (40000, 6800, 77)):
+        rows = skl.subsample_rows(N, m, seed=seed)
+        np.testing.assert_array_equal(rows, orc.random_sample_rows(orc.Rng(seed), N, m))
+        assert len(np.unique(rows)) == m and rows.min() >= 0 and rows.max() < N
+    skl.srand(3)
+    a = skl.subsample_rows(500, 40)
+    b = skl.subsample_rows(500, 40)
+    g = orc.Rng(3)
+    np.testing.assert_array_equal(a, orc.random_sample_rows(g, 500, 40))
+    np.testing.assert_array_equal(b, orc.random_sample_rows(g, 500, 40))
+    with pytest.raises(skl.SklError) as e:
+        skl.subsample_rows(10, 11, seed=1)
+    assert e.value.status == skl.SKL_ERR_INVALID
+
+
 def test_hash_stream_chunked_draws_k3():
     # n*k = 300,009: up to 16 worker chunks whose starts fall inside a column
     # (chunk start not a multiple of k), then the stream continues

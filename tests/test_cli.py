@@ -1,5 +1,6 @@
 """Command-line drivers (ski-lls_gb300/cli): the equivalents of the
-reference's test/ls_qr.cpp and test/ls_blendenpik_hashing.cpp, run the way
+reference's test/ls_qr.cpp, test/ls_blendenpik_hashing.cpp and
+test/ls_blendenpik.cpp, run the way
 test/test_solvers.sh runs its solvers (MatrixMarket input, b = ones, the
 "Residual of ... is:" line), with the script's expected residuals asserted."""
 import os
@@ -64,6 +65,23 @@ def test_ls_blendenpik_hashing_full_rank_dense(tools, fixtures, tmp_path, tag):
                        text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     res = _residual(r.stdout, "ls_blendenpik_hashing")
+    b = np.ones(n)
+    ref = np.linalg.norm(A @ np.linalg.lstsq(A, b, rcond=None)[0] - b)
+    assert abs(res - ref) <= 1e-6 * ref, (res, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", FULL_RANK_TAGS)
+def test_ls_blendenpik_full_rank_dense(tools, fixtures, tmp_path, tag):
+    # test/test_solvers.sh runs ls_blendenpik on the same six dense fixtures
+    A = np.asarray(fixtures[f"{tag}DenseFullRank/dense"], dtype=np.float64)
+    n = A.shape[0]
+    path = tmp_path / (tag + ".mtx")
+    scipy.io.mmwrite(str(path), A)
+    r = subprocess.run([tools["ls_blendenpik"], str(path)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    res = _residual(r.stdout, "ls_blendenpik")
     b = np.ones(n)
     ref = np.linalg.norm(A @ np.linalg.lstsq(A, b, rcond=None)[0] - b)
     assert abs(res - ref) <= 1e-6 * ref, (res, ref)

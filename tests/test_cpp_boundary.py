@@ -53,6 +53,10 @@ def test_drop_in_programs_run(tmp_path, fixtures):
     line2 = [ln for ln in out.stdout.splitlines() if ln.startswith("x2 ")][0]
     np.testing.assert_allclose(np.array([float(v) for v in line2.split()[1:3]]),
                                fixtures["dense_example/x_expected"], atol=5e-5)
+    line3 = [ln for ln in out.stdout.splitlines() if ln.startswith("x3 ")][0]
+    np.testing.assert_allclose(np.array([float(v) for v in line3.split()[1:3]]),
+                               fixtures["dense_example/x_expected"], atol=5e-5)
+    assert line3.split()[4] == "2"   # rank = n
     exe = _build(os.path.join(ROOT, "tests", "cpp", "sparse_drop_in.cpp"), str(tmp_path / "s"))
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr

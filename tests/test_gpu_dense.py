@@ -108,6 +108,44 @@ def test_dense_noCPQR():
     assert np.linalg.norm(res.x - ref["x"]) <= XTOL * np.linalg.norm(xr)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_dense_blendenpik_vs_oracle(precision):
+    """ls_dense_blendenpik (src/ls_dense_blendenpik.cpp:21-70): same seed, so the
+    same signs and sampled rows as the oracle; x to 1e-8 of LAPACK and the
+    oracle, and LSQR's iteration count within 2 of the oracle's."""
+    A, b = _dense(3000, 100, 2.0, 21)
+    xr = np.linalg.lstsq(A, b, rcond=None)[0]
+    res = skl.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-12, seed=6, precision=precision)
+    ref = orc.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-12, seed=6, N=skl.dht_length(3000))
+    assert res.rank == 100 and res.flag == 0
+    assert res.info["sketch_rows"] == ref["m"] == 221   # ceil(2.2 * 100) in FP64 arithmetic
+    assert np.linalg.norm(res.x - xr) <= XTOL * np.linalg.norm(xr)
+    assert np.linalg.norm(res.x - ref["x"]) <= XTOL * np.linalg.norm(xr)
+    assert abs(res.it - ref["it"]) <= 2
+
+
+def test_dense_blendenpik_padded_transform_and_errors():
+    # n = 1,001: the transform pads to an even smooth length and the sample is
+    # drawn from all N rows (zero rows of D A included)
+    A, b = _dense(1001, 60, 1.0, 3)
+    N = skl.dht_length(1001)
+    assert N > 1001
+    xr = np.linalg.lstsq(A, b, rcond=None)[0]
+    res = skl.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-12, seed=2)
+    ref = orc.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-12, seed=2, N=N)
+    assert np.linalg.norm(res.x - xr) <= XTOL * np.linalg.norm(xr)
+    assert np.linalg.norm(res.x - ref["x"]) <= XTOL * np.linalg.norm(xr)
+    r1 = skl.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-10, seed=9)
+    r2 = skl.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-10, seed=9)
+    assert np.array_equal(r1.x, r2.x)
+    with pytest.raises(skl.SklError) as e:
+        skl.ls_dense_blendenpik(A[:40], b[:40], seed=1)
+    assert e.value.status == skl.SKL_ERR_NOT_OVERDETERMINED
+    with pytest.raises(skl.SklError) as e:
+        skl.ls_dense_blendenpik(A[:100], b[:100], 2.0, seed=1)   # 120 rows of 100
+    assert e.value.status == skl.SKL_ERR_INVALID
+
+
 def test_dense_rank_deficient_absolute_rule():
     # duplicated columns: the absolute |R_ii| > rcond rule drops them when rcond
     # sits above the working precision's noise on |R_ii| (~1e-7 |R_00| in FP32)

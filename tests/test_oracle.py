@@ -131,3 +131,45 @@ def test_noCPQR_full_rank_fixtures_vs_lstsq(fixtures, tag):
 def test_noCPQR_rejects_underdetermined():
     with pytest.raises(RuntimeError, match="Matrix is not overdetermined."):
         orc.ls_dense_hashing_blendenpik_noCPQR(np.ones((3, 5)), np.ones(3), 1.7, 1)
+
+
+def test_random_sample_rows_match_live_libc():
+    """select_k_from_n over 0..N-1 (src/sparse_helpers.cpp:74-86) driven by the C
+    library's own rand(), against the oracle's draw from its restated stream."""
+    try:
+        libc = ctypes.CDLL("libc.so.6")
+    except OSError:
+        pytest.skip("no glibc")
+    for (N, m, s) in ((50, 33, 5), (1000, 250, 41)):
+        libc.srand(ctypes.c_uint(s))
+        idx = list(range(N))
+        for i in range(m):
+            j = libc.rand() % (N - i) + i
+            idx[i], idx[j] = idx[j], idx[i]
+        assert list(orc.random_sample_rows(orc.Rng(s), N, m)) == idx[:m]
+
+
+@pytest.mark.parametrize("tag", FULL_RANK_TAGS)
+def test_blendenpik_full_rank_fixtures_vs_lstsq(fixtures, tag):
+    """The ls_dense_blendenpik restatement on the dense full-rank fixtures the
+    reference's test/test_solvers.sh runs ls_blendenpik on, at its driver's
+    gamma = 2.2 (test/ls_blendenpik.cpp:61), against LAPACK least squares; the
+    sketch is exactly the sampled rows of the randomized DHT."""
+    Ad = fixtures[f"{tag}DenseFullRank/dense"]
+    n, d = Ad.shape
+    b = np.ones(n)
+    xr = np.linalg.lstsq(Ad, b, rcond=None)[0]
+    out = orc.ls_dense_blendenpik(Ad, b, 2.2, it_tol=1e-12, seed=5)
+    assert out["rank"] == d and out["flag"] == 0 and out["m"] == math.ceil(2.2 * d)
+    assert np.linalg.norm(out["x"] - xr) <= 1e-8 * np.linalg.norm(xr)
+    D = orc.rand_signs(orc.Rng(5), n)
+    Y = orc.unitary_dht(Ad, D)
+    np.testing.assert_array_equal(out["rows"], orc.random_sample_rows(orc.Rng(5), n, out["m"]))
+    np.testing.assert_array_equal(out["SA"], Y[out["rows"]])
+
+
+def test_blendenpik_rejects_underdetermined_and_oversized_sample():
+    with pytest.raises(RuntimeError, match="Matrix is not overdetermined."):
+        orc.ls_dense_blendenpik(np.ones((3, 5)), np.ones(3), 2.2)
+    with pytest.raises(ValueError):
+        orc.ls_dense_blendenpik(np.eye(10, 6), np.ones(10), 2.0)   # 12 rows of 10
