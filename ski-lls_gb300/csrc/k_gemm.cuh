@@ -430,9 +430,11 @@ inline void launch_sgemm(bool ta, bool tb, dim3 grid, cudaStream_t st, int M, in
 }
 
 // Split-K factor for the FP32 kernel (tile bm x 128): fill about two waves.
-inline int sgemm_splits(int M, int N, int K, int bm)
+// A triangular operand leaves half the tile-K work, so it counts half the tiles.
+inline int sgemm_splits(int M, int N, int K, int bm, int tri)
 {
     int tiles = ((M + bm - 1) / bm) * ((N + kSBN - 1) / kSBN);
+    if (tri) tiles = (tiles + 1) / 2;
     int s = 1;
     while (tiles * s < 2 * 152 && K / (s * 2) >= kSplitMinK && s < kSplitMax) s *= 2;
     return s;
@@ -488,14 +490,16 @@ inline void gemm_launch<float>(bool ta, bool tb, int M, int N, int K, float alph
         // small outputs with a short K: the 64 x 64 kernel spreads them over
         // more CTAs than the 128-wide tiles would
         const int64_t tiles = (int64_t)((M + bm - 1) / bm) * ((N + kSBN - 1) / kSBN);
-        const bool can_split = K > 0 && partial && tri == 0 && K >= 512;
+        const bool can_split = K > 0 && partial && K >= 512;
         if (!can_split && tiles < 152) {
             gemm_launch_generic<float>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, partial,
                                        partial_cap, tri, st);
             return;
         }
     }
-    int splits = (K > 0 && partial && tri == 0) ? sgemm_splits(M, N, K, bm) : 1;
+    // triangular operands split K too: a split's range is intersected with the
+    // triangle's per tile (an empty intersection writes a zero partial)
+    int splits = (K > 0 && partial) ? sgemm_splits(M, N, K, bm, tri) : 1;
     while (splits > 1 && (int64_t)splits * M * N > partial_cap) splits >>= 1;
     int kchunk = K;
     if (splits > 1) {
@@ -530,12 +534,14 @@ void gemm(bool ta, bool tb, int M, int N, int K, T alpha, const T* A, int64_t ld
 }
 
 // C = alpha * A * B + beta * C with A upper triangular (tri = 1) or B upper
-// triangular (tri = 2); no transposes, no split-K.
+// triangular (tri = 2); no transposes; split-K (FP32) when a partial buffer
+// is given.
 template <typename T>
 void trmm(int tri, int M, int N, int K, T alpha, const T* A, int64_t lda, const T* B, int64_t ldb,
-          T beta, T* C, int64_t ldc, cudaStream_t st)
+          T beta, T* C, int64_t ldc, cudaStream_t st, T* partial = nullptr, int64_t partial_cap = 0)
 {
-    gemm_launch<T>(false, false, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nullptr, 0, tri, st);
+    gemm_launch<T>(false, false, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, partial, partial_cap, tri,
+                   st);
 }
 
 // batch products C_z = alpha op(A_z) op(B_z) + beta C_z, z = 0..batch-1, with

@@ -74,7 +74,9 @@ __global__ void k_zero_lower(T* __restrict__ M, int64_t ldm, int r)
 template <typename T>
 size_t trinv_workspace_bytes(int64_t r)
 {
-    const size_t a = (size_t)r * r * sizeof(T) / 2 + (size_t)kTB * kTB * sizeof(T);
+    // B C^{-1} of one pair (at most r^2 / 4) and the split-K partials of the
+    // pair's two products behind it
+    const size_t a = (size_t)r * r * sizeof(T) + (size_t)kTB * kTB * sizeof(T);
     const size_t b = (size_t)((r + 127) / 128) * r * sizeof(double);   // row-sum partials
     return (a > b ? a : b) + 4096;
 }
@@ -128,6 +130,7 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
     k_inv_diag_blocks<T><<<nblk, kTB, 0, st>>>(R, ld, (int)r, (T)perturb, M, ldm);
     SKL_LAUNCHED();
     T* tmp = (T*)work;   // holds B * C^{-1} for one pair (s x s')
+    const size_t ws_elems = (trinv_workspace_bytes<T>(r) - 4096) / sizeof(T);
     // recursive doubling: blocks of size s are inverted; combine neighbours
     for (int64_t s = kTB; s < r; s *= 2) {
         int64_t a_first = 0;
@@ -151,9 +154,12 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
             const T* Cinv = M + c0 + c0 * ldm;
             const T* Bblk = R + a0 + c0 * ld;
             T* X = M + a0 + c0 * ldm;
-            // tmp = B * Cinv (Cinv upper), then X = -Ainv * tmp (Ainv upper)
-            trmm<T>(2, (int)sa, (int)sc, (int)sc, T(1), Bblk, ld, Cinv, ldm, T(0), tmp, sa, st);
-            trmm<T>(1, (int)sa, (int)sc, (int)sa, T(-1), Ainv, ldm, tmp, sa, T(0), X, ldm, st);
+            // tmp = B * Cinv (Cinv upper), then X = -Ainv * tmp (Ainv upper);
+            // the K-split partials sit behind tmp (FP32 products only)
+            T* part = tmp + (sa * sc + 3) / 4 * 4;
+            const int64_t cap = (int64_t)(ws_elems - (size_t)(part - tmp));
+            trmm<T>(2, (int)sa, (int)sc, (int)sc, T(1), Bblk, ld, Cinv, ldm, T(0), tmp, sa, st, part, cap);
+            trmm<T>(1, (int)sa, (int)sc, (int)sa, T(-1), Ainv, ldm, tmp, sa, T(0), X, ldm, st, part, cap);
         }
     }
     k_zero_lower<T><<<1024, 256, 0, st>>>(M, ldm, (int)r);
