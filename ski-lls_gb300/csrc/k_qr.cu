@@ -1424,9 +1424,12 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     const size_t ysm_max = YqrpSmem<T>::bytes(yldp, nbp, ycn_max);
     const size_t psm = panel_smem_bytes<T>(p.R, nb);
 
-    // CholeskyQR2 panels: pivoted factorisations only, not the last panel (it
-    // has no sample QRP ordering), rows 0..b-1 of a panel inside CTA 0
-    const bool use_chol = pivoting && nb <= 64 && std::is_same<T, float>::value && qr_chol_enabled<T>();
+    // CholeskyQR2 panels, not the last panel (it has no sample QRP ordering),
+    // rows 0..b-1 of a panel inside CTA 0.  Unpivoted factorisations (the
+    // full-rank noCPQR and Blendenpik sketches) use them too: a panel whose
+    // Cholesky breaks down or whose second Gram strays from the identity
+    // falls back to the Householder panel (chol_fail)
+    const bool use_chol = nb <= 64 && std::is_same<T, float>::value && qr_chol_enabled<T>();
 
     // Two streams.  The sample work of panel j (Y downdate, the sample QRP of
     // panel j+1) needs only V, T and R12 = A12 - V1 Z, so it runs on a
