@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 
 namespace skl {
 
@@ -25,6 +26,7 @@ k_gemm(int M, int N, int K, T alpha, const T* __restrict__ A, int64_t lda,
        const T* __restrict__ B, int64_t ldb, T beta, T* __restrict__ C, int64_t ldc, int kchunk,
        T* __restrict__ partial, int64_t bsa = 0, int64_t bsb = 0, int64_t bsc = 0)
 {
+    pdl_wait();
     __shared__ T As[kGBK][kGBM + 1];
     __shared__ T Bs[kGBK][kGBN + 1];
     const int tid = threadIdx.x;
@@ -228,6 +230,7 @@ k_sgemm(int M, int N, int K, float alpha, const float* __restrict__ A, int64_t l
         const float* __restrict__ B, int64_t ldb, float beta, float* __restrict__ C, int64_t ldc,
         int kchunk, float* __restrict__ partial)
 {
+    pdl_wait();
     constexpr int BM = 64 * MT;
     __shared__ __align__(16) float As[2][kSBK][BM + kSPad];
     __shared__ __align__(16) float Bs[2][kSBK][kSBN + kSPad];
@@ -344,6 +347,7 @@ __global__ void __launch_bounds__(256)
 k_splitk_reduce_warp(int M, int N, int splits, T alpha, const T* __restrict__ partial, T beta,
                      T* __restrict__ C, int64_t ldc)
 {
+    pdl_wait();
     const int64_t total = (int64_t)M * N;
     const int lane = threadIdx.x & 31;
     const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -364,6 +368,7 @@ template <typename T>
 __global__ void k_splitk_reduce(int M, int N, int splits, T alpha, const T* __restrict__ partial,
                                 T beta, T* __restrict__ C, int64_t ldc)
 {
+    pdl_wait();
     int64_t total = (int64_t)M * N;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -395,11 +400,11 @@ inline void splitk_reduce_launch(int M, int N, int splits, T alpha, const T* par
     const int64_t total = (int64_t)M * N;
     if (splits >= 16 && total <= 65536) {
         const unsigned g = (unsigned)((total * 32 + 255) / 256);
-        k_splitk_reduce_warp<T><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
+        launch_k(k_splitk_reduce_warp<T>, g, 256, 0, st, M, N, splits, alpha, partial, beta, C, ldc);
     } else {
         unsigned g = (unsigned)((total + 255) / 256);
         if (g > 152 * 8) g = 152 * 8;
-        k_splitk_reduce<T><<<g, 256, 0, st>>>(M, N, splits, alpha, partial, beta, C, ldc);
+        launch_k(k_splitk_reduce<T>, g, 256, 0, st, M, N, splits, alpha, partial, beta, C, ldc);
     }
     SKL_LAUNCHED();
 }
@@ -423,10 +428,10 @@ inline void launch_sgemm(bool ta, bool tb, dim3 grid, cudaStream_t st, int M, in
                          const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C,
                          int64_t ldc, int kchunk, float* part)
 {
-    if (!ta && !tb) k_sgemm<MT, false, false, TRI><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (ta && !tb) k_sgemm<MT, true, false, TRI><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (!ta && tb) k_sgemm<MT, false, true, TRI><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else k_sgemm<MT, true, true, TRI><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
+    if (!ta && !tb) launch_k(k_sgemm<MT, false, false, TRI>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
+    else if (ta && !tb) launch_k(k_sgemm<MT, true, false, TRI>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
+    else if (!ta && tb) launch_k(k_sgemm<MT, false, true, TRI>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
+    else launch_k(k_sgemm<MT, true, true, TRI>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
 }
 
 // Split-K factor for the FP32 kernel (tile bm x 128): fill about two waves.
@@ -457,12 +462,18 @@ inline void gemm_launch_generic(bool ta, bool tb, int M, int N, int K, T alpha, 
     if (K <= 0) { kchunk = 0; splits = 1; }
     dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, splits);
     T* part = splits > 1 ? partial : nullptr;
-    if (tri == 1) k_gemm<T, false, false, 1><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (tri == 2) k_gemm<T, false, false, 2><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (!ta && !tb) k_gemm<T, false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (ta && !tb) k_gemm<T, true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else if (!ta && tb) k_gemm<T, false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
-    else k_gemm<T, true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part);
+    if (tri == 1) launch_k(k_gemm<T, false, false, 1>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
+    else if (tri == 2) launch_k(k_gemm<T, false, false, 2>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
+    else if (!ta && !tb) launch_k(k_gemm<T, false, false>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
+    else if (ta && !tb) launch_k(k_gemm<T, true, false>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
+    else if (!ta && tb) launch_k(k_gemm<T, false, true>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
+    else launch_k(k_gemm<T, true, true>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk, part,
+                                  (int64_t)0, (int64_t)0, (int64_t)0);
     SKL_LAUNCHED();
     if (splits > 1) {
         splitk_reduce_launch<T>(M, N, splits, alpha, partial, beta, C, ldc, st);
@@ -554,13 +565,13 @@ void trmm_batched(int tri, int M, int N, int K, T alpha, const T* A, int64_t lda
     if (M <= 0 || N <= 0 || batch <= 0) return;
     dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, batch);
     if (tri == 1)
-        k_gemm<T, false, false, 1, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+        launch_k(k_gemm<T, false, false, 1, true>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                                                 ldc, K, nullptr, bsa, bsb, bsc);
     else if (tri == 2)
-        k_gemm<T, false, false, 2, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+        launch_k(k_gemm<T, false, false, 2, true>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                                                 ldc, K, nullptr, bsa, bsb, bsc);
     else
-        k_gemm<T, false, false, 0, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+        launch_k(k_gemm<T, false, false, 0, true>, grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                                                 ldc, K, nullptr, bsa, bsb, bsc);
     SKL_LAUNCHED();
 }

@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 #include "k_gemm.cuh"
 
@@ -66,6 +67,7 @@ SKL_DEV unsigned long long splitmix64(unsigned long long x)
 template <typename T>
 __global__ void k_gaussian(T* __restrict__ G, int64_t count, unsigned long long seed)
 {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x) {
         unsigned long long r = splitmix64(seed ^ splitmix64((unsigned long long)i));
@@ -277,6 +279,7 @@ k_yqrp(const T* __restrict__ Y, int ldy, int nbp, int ldp, int j0, int N, int b,
        int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
        unsigned* __restrict__ status)
 {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned crank = cluster_ctarank();
     const int cn = (N + kCluster - 1) / kCluster;
@@ -525,6 +528,7 @@ k_yqrp_reg(const float* __restrict__ Y, int ldy, int nbp, int j0, int N, int b, 
            int* __restrict__ plan_src, int* __restrict__ plan_dst, int* __restrict__ plan_n,
            unsigned* __restrict__ status)
 {
+    pdl_wait();
     constexpr int kQuads = kYThreads / 4;
     constexpr int kYRegPairs = NP;                                      // row pairs per lane
     constexpr int kGran = 2 * NP;                                       // 16-byte row groups
@@ -755,6 +759,7 @@ __global__ void k_perm_gather(const T* __restrict__ A, int64_t ld, int m, const 
                               const int* __restrict__ plan_src, const int* __restrict__ plan_n,
                               T* __restrict__ tmpA, T* __restrict__ tmpY, int* __restrict__ tmpI)
 {
+    pdl_wait();
     const int q = blockIdx.y;
     if (q >= *plan_n) return;
     const int64_t c = j0 + plan_src[q];
@@ -775,6 +780,7 @@ __global__ void k_perm_scatter(T* __restrict__ A, int64_t ld, int m, T* __restri
                                const T* __restrict__ tmpA, const T* __restrict__ tmpY,
                                const int* __restrict__ tmpI)
 {
+    pdl_wait();
     const int q = blockIdx.y;
     if (q >= *plan_n) return;
     const int64_t c = j0 + plan_dst[q];
@@ -846,6 +852,7 @@ k_panel(T* __restrict__ A, int64_t ld, int j0, int M, int b, int R, T* __restric
         T* __restrict__ Tout, int ldt, T* __restrict__ V, int64_t ldv, int* __restrict__ jpvt,
         T* __restrict__ Y, int ldy, int nbp, int pivot_panel, const int* __restrict__ chol_fail)
 {
+    pdl_wait();
     // runs only when the CholeskyQR2 panel (if any) declined this panel
     if (chol_fail && *chol_fail == 0) return;
     using V4 = typename Vec4T<T>::type;
@@ -1117,6 +1124,7 @@ template <typename T>
 __global__ void k_qt_w(const T* __restrict__ V, int64_t ldv, int M, int b,
                        const double* __restrict__ c, double* __restrict__ w)
 {
+    pdl_wait();
     __shared__ double red[32];
     const int a = blockIdx.x;
     const T* va = V + (int64_t)a * ldv;
@@ -1131,6 +1139,7 @@ __global__ void k_qt_update(const T* __restrict__ V, int64_t ldv, int M, int b,
                             const T* __restrict__ Tm, int ldt, const double* __restrict__ w,
                             double* __restrict__ c)
 {
+    pdl_wait();
     __shared__ double z[kMaxNb];
     if (threadIdx.x < b) {
         const int i = threadIdx.x;
@@ -1151,6 +1160,7 @@ template <typename T>
 __global__ void k_copy_block(const T* __restrict__ src, int64_t lds, T* __restrict__ dst,
                              int64_t ldd, int rows, int cols)
 {
+    pdl_wait();
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
         int r = e % rows, c = e / rows;
         dst[r + (int64_t)c * ldd] = src[r + (int64_t)c * lds];
@@ -1159,6 +1169,7 @@ __global__ void k_copy_block(const T* __restrict__ src, int64_t lds, T* __restri
 
 __global__ void k_iota_int(int* v, int n)
 {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
 }
 
@@ -1288,13 +1299,15 @@ static void launch_cluster(const void* fn, dim3 block, size_t smem, cudaStream_t
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = kCluster;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;   // see launch.cuh
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl_enabled() ? 2 : 1;
     SKL_CUDA(cudaLaunchKernelExC(&cfg, fn, args));
     SKL_LAUNCHED();
 }
@@ -1405,11 +1418,11 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
     QrBuffers<T> B = qr_carve<T>(work, m, d, p, nullptr);
     const int nb = p.nb, nbp = p.nbp;
     const int64_t mn = m < d ? m : d;
-    k_iota_int<<<(unsigned)((d + 255) / 256), 256, 0, st>>>(jpvt, (int)d);
+    launch_k(k_iota_int, (unsigned)((d + 255) / 256), 256, 0, st, jpvt, (int)d);
     SKL_LAUNCHED();
     if (pivoting) {
         int64_t cnt = (int64_t)nbp * m;
-        k_gaussian<T><<<(unsigned)((cnt + 255) / 256 < 2048 ? (cnt + 255) / 256 : 2048), 256, 0, st>>>(
+        launch_k(k_gaussian<T>, (unsigned)((cnt + 255) / 256 < 2048 ? (cnt + 255) / 256 : 2048), 256, 0, st, 
             B.G, cnt, 0x5eed000000000012ull);
         SKL_LAUNCHED();
         cudaEvent_t t0 = tm.begin();
@@ -1506,9 +1519,9 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
             cudaEvent_t t0 = tm.begin();
             // the sample QRP planned the moves (plan_src/plan_dst/plan_n)
             dim3 gA((unsigned)std::min<int64_t>((m + 255) / 256, 64), 2 * b);
-            k_perm_gather<T><<<gA, 256, 0, st>>>(A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_src,
+            launch_k(k_perm_gather<T>, gA, 256, 0, st, A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_src,
                                                  B.plan_n, B.tmp, B.tmpY, B.tmpI);
-            k_perm_scatter<T><<<gA, 256, 0, st>>>(A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_dst,
+            launch_k(k_perm_scatter<T>, gA, 256, 0, st, A, ld, (int)m, B.Y, nbp, nbp, jpvt, jj, B.plan_dst,
                                                   B.plan_n, B.tmp, B.tmpY, B.tmpI);
             SKL_LAUNCHED();
             SKL_LAUNCHED();
@@ -1551,7 +1564,7 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
                     B.part2_cap, side);
             gemm<T>(false, false, nbp, b, b, T(1), B.GU, nbp, B.Tm, nb, T(0), B.GUT, nbp, nullptr,
                     0, side);
-            k_copy_block<T><<<16, 256, 0, side>>>(Gj, nbp, B.Bm, nbp, nbp, b);
+            launch_k(k_copy_block<T>, 16, 256, 0, side, Gj, nbp, B.Bm, nbp, nbp, b);
             SKL_LAUNCHED();
             gemm<T>(false, true, nbp, b, b, T(-1), B.GUT, nbp, B.V, m, T(1), B.Bm, nbp, nullptr, 0,
                     side);
@@ -1630,8 +1643,8 @@ static void qr_core(T* A, int64_t m, int64_t d, int64_t ld, int* jpvt, T* tau, v
         }
         if (c) {
             cudaEvent_t t0 = tm.begin();
-            k_qt_w<T><<<b, 256, 0, st>>>(B.V, m, M, b, c + j, B.qw);
-            k_qt_update<T><<<(unsigned)std::max<int64_t>(1, (M + 127) / 128), 128, 0, st>>>(
+            launch_k(k_qt_w<T>, b, 256, 0, st, B.V, m, M, b, c + j, B.qw);
+            launch_k(k_qt_update<T>, (unsigned)std::max<int64_t>(1, (M + 127) / 128), 128, 0, st, 
                 B.V, m, M, b, B.Tm, nb, B.qw, c + j);
             SKL_LAUNCHED();
             SKL_LAUNCHED();

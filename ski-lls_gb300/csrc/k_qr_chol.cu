@@ -8,6 +8,7 @@
 #include <type_traits>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 #include "k_gemm.cuh"
 
@@ -679,6 +680,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
 k_chol_small1(const T* __restrict__ G, int b, T* __restrict__ R1, T* __restrict__ X1,
               int* __restrict__ fail)
 {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int np = small_np(b);
     const int LDX = np + 4;
@@ -717,6 +719,7 @@ k_chol_small2(const T* __restrict__ G, int b, const T* __restrict__ R1g, const T
               T* __restrict__ Tout, int ldt, T* __restrict__ tau_out, T* __restrict__ Wg,
               int* __restrict__ fail)
 {
+    pdl_wait();
     if (*fail) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int np = small_np(b);
@@ -779,6 +782,7 @@ template <typename T>
 __global__ void k_chol_copy_down(const T* __restrict__ V, int64_t ldv, T* __restrict__ A, int64_t ld,
                                  int j0, int M, int b, const int* __restrict__ fail)
 {
+    pdl_wait();
     if (*fail) return;
     const int rows = M - b;
     const int c = blockIdx.y;
@@ -796,18 +800,18 @@ void chol_panel(T* P, int64_t ld, int M, int b, int j0, T* A, T* cg, T* cr1, T* 
     allow_max_dynamic_smem((const void*)k_chol_small1<T>);
     allow_max_dynamic_smem((const void*)k_chol_small2<T>);
     gemm<T>(true, false, b, b, M, T(1), P, ld, P, ld, T(0), cg, b, part, part_cap, st);
-    k_chol_small1<T><<<1, kSmallThreads, ssm, st>>>(cg, b, cr1, cx1, fail);
+    launch_k(k_chol_small1<T>, 1, kSmallThreads, ssm, st, cg, b, cr1, cx1, fail);
     SKL_CUDA(cudaGetLastError());
     SKL_LAUNCHED();
     gemm<T>(false, false, M, b, b, T(1), P, ld, cx1, b, T(0), tmp, M, nullptr, 0, st);
     gemm<T>(true, false, b, b, M, T(1), tmp, M, tmp, M, T(0), cg, b, part, part_cap, st);
-    k_chol_small2<T><<<1, kSmallThreads, ssm, st>>>(cg, b, cr1, tmp, M, A, ld, j0, V, ldv, Tm, ldt,
+    launch_k(k_chol_small2<T>, 1, kSmallThreads, ssm, st, cg, b, cr1, tmp, M, A, ld, j0, V, ldv, Tm, ldt,
                                                     tau, cw, fail);
     SKL_CUDA(cudaGetLastError());
     SKL_LAUNCHED();
     gemm<T>(false, false, M - b, b, b, T(1), tmp + b, M, cw, b, T(0), V + b, ldv, nullptr, 0, st);
     dim3 gc((unsigned)std::max<int64_t>(1, std::min<int64_t>((M - b + 255) / 256, 64)), b);
-    k_chol_copy_down<T><<<gc, 256, 0, st>>>(V, ldv, A, ld, j0, M, b, fail);
+    launch_k(k_chol_copy_down<T>, gc, 256, 0, st, V, ldv, A, ld, j0, M, b, fail);
     SKL_LAUNCHED();
 }
 

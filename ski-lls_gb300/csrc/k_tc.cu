@@ -37,6 +37,7 @@
 #include <mutex>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 #include "k_gemm.cuh"
 
@@ -198,6 +199,7 @@ k_tc_vta(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
          const __grid_constant__ CUtensorMap mapVl, int N, int b, int kb_per, int kb_total,
          float* __restrict__ partial, unsigned* __restrict__ status)
 {
+    pdl_wait();
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
@@ -374,6 +376,7 @@ k_tc_vta(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
 __global__ void k_tc_split_v(const float* __restrict__ V, int64_t ldv, int M, int b,
                              float* __restrict__ Vh, float* __restrict__ Vl, int64_t ldvs)
 {
+    pdl_wait();
     const int64_t total = (int64_t)M * b;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -419,6 +422,7 @@ k_tc_update(const __grid_constant__ CUtensorMap mapVh, const __grid_constant__ C
             const __grid_constant__ CUtensorMap mapC, int r0, int nct, int ct_per,
             unsigned* __restrict__ status)
 {
+    pdl_wait();
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* vbuf = smem;                                   // [hi0, hi1, lo0, lo1] x 16 KB
@@ -585,6 +589,7 @@ __global__ void k_tc_split_vz(const float* __restrict__ V, int64_t ldv, int M, i
                               const float* __restrict__ Z, int64_t ldz, int N, float* __restrict__ Vth,
                               float* __restrict__ Vtl, float* __restrict__ Zth, float* __restrict__ Ztl)
 {
+    pdl_wait();
     const int64_t nv = (int64_t)M * b, total = nv + (int64_t)N * b;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -680,7 +685,7 @@ void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, in
     {
         const int64_t total = (int64_t)M * b;
         const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 8);
-        k_tc_split_v<<<g, 256, 0, st>>>(V, ldv, M, b, Vh, Vl, ldvs);
+        launch_k(k_tc_split_v, g, 256, 0, st, V, ldv, M, b, Vh, Vl, ldvs);
         SKL_LAUNCHED();
     }
     const int ntile = (N + kTM - 1) / kTM;
@@ -698,7 +703,7 @@ void tc_vta(int M, int N, int b, const float* V, int64_t ldv, const float* A, in
     std::call_once(attr_once, [] {
         cudaFuncSetAttribute((const void*)k_tc_vta, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     });
-    k_tc_vta<<<dim3(ntile, splits), kTcThreads, kSmemBytes, st>>>(mA, mVh, mVl, N, b, kb_per, kb_total,
+    launch_k(k_tc_vta, dim3(ntile, splits), kTcThreads, kSmemBytes, st, mA, mVh, mVl, N, b, kb_per, kb_total,
                                                                 out, status);
     SKL_LAUNCHED();
     if (splits > 1) splitk_reduce_launch<float>(b, N, splits, 1.0f, partial, 0.0f, W, b, st);
@@ -721,7 +726,7 @@ void tc_update(int M, int N, int b, int r0, const float* V, int64_t ldv, const f
     {
         const int64_t total = (int64_t)(M + N) * b;
         const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 8);
-        k_tc_split_vz<<<g, 256, 0, st>>>(V, ldv, M, b, Z, ldz, N, Vth, Vtl, Zth, Ztl);
+        launch_k(k_tc_split_vz, g, 256, 0, st, V, ldv, M, b, Z, ldz, N, Vth, Vtl, Zth, Ztl);
         SKL_LAUNCHED();
     }
     // K-major operands: dims {K = b, rows}, rows 64 floats apart; C: {rows, cols}
@@ -762,7 +767,7 @@ void tc_update(int M, int N, int b, int r0, const float* V, int64_t ldv, const f
         cudaFuncSetAttribute((const void*)k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kUSmemBytes);
     });
-    k_tc_update<<<dim3(nrt, splits), kUpdThreads, kUSmemBytes, st>>>(mVh, mVl, mZh, mZl, mC, r0, nct, ct_per,
+    launch_k(k_tc_update, dim3(nrt, splits), kUpdThreads, kUSmemBytes, st, mVh, mVl, mZh, mZl, mC, r0, nct, ct_per,
                                                                      status);
     SKL_LAUNCHED();
 }

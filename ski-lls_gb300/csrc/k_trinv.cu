@@ -16,6 +16,7 @@
 #include <cmath>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 #include "k_gemm.cuh"
 
@@ -30,6 +31,7 @@ template <typename T>
 __global__ void k_inv_diag_blocks(const T* __restrict__ R, int64_t ld, int r, T perturb,
                                   T* __restrict__ M, int64_t ldm)
 {
+    pdl_wait();
     __shared__ T U[kTB][kTB + 1];
     __shared__ T X[kTB][kTB + 1];
     const int b0 = blockIdx.x * kTB;
@@ -63,6 +65,7 @@ __global__ void k_inv_diag_blocks(const T* __restrict__ R, int64_t ld, int r, T 
 template <typename T>
 __global__ void k_zero_lower(T* __restrict__ M, int64_t ldm, int r)
 {
+    pdl_wait();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)r * r;
          e += (int64_t)gridDim.x * blockDim.x) {
         int i = (int)(e % r);
@@ -87,6 +90,7 @@ constexpr int kInfRows = 128, kInfCols = 128;
 template <typename T>
 __global__ void k_inf_rowsum_tiles(const T* __restrict__ X, int64_t ld, int r, double* __restrict__ part)
 {
+    pdl_wait();
     const int i = blockIdx.x * kInfRows + threadIdx.x;
     const int j0 = blockIdx.y * kInfCols;
     double s = 0.0;
@@ -99,6 +103,7 @@ __global__ void k_inf_rowsum_tiles(const T* __restrict__ X, int64_t ld, int r, d
 
 __global__ void k_inf_rowsum_max(const double* __restrict__ part, int nchunks, int r, double* out)
 {
+    pdl_wait();
     __shared__ double red[32];
     double mx = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
@@ -115,8 +120,8 @@ static void inf_norm_upper(const T* X, int64_t ld, int64_t r, double* part, doub
 {
     const int nchunks = (int)((r + kInfCols - 1) / kInfCols);
     dim3 g((unsigned)((r + kInfRows - 1) / kInfRows), nchunks);
-    k_inf_rowsum_tiles<T><<<g, kInfRows, 0, st>>>(X, ld, (int)r, part);
-    k_inf_rowsum_max<<<(unsigned)std::min<int64_t>((r + 255) / 256, 64), 256, 0, st>>>(part, nchunks, (int)r, out);
+    launch_k(k_inf_rowsum_tiles<T>, g, kInfRows, 0, st, X, ld, (int)r, part);
+    launch_k(k_inf_rowsum_max, (unsigned)std::min<int64_t>((r + 255) / 256, 64), 256, 0, st, part, nchunks, (int)r, out);
     SKL_LAUNCHED();
     SKL_LAUNCHED();
 }
@@ -127,7 +132,7 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
 {
     if (r <= 0) return;
     const int nblk = (int)((r + kTB - 1) / kTB);
-    k_inv_diag_blocks<T><<<nblk, kTB, 0, st>>>(R, ld, (int)r, (T)perturb, M, ldm);
+    launch_k(k_inv_diag_blocks<T>, nblk, kTB, 0, st, R, ld, (int)r, (T)perturb, M, ldm);
     SKL_LAUNCHED();
     T* tmp = (T*)work;   // holds B * C^{-1} for one pair (s x s')
     const size_t ws_elems = (trinv_workspace_bytes<T>(r) - 4096) / sizeof(T);
@@ -162,7 +167,7 @@ void trinv_upper(const T* R, int64_t ld, int64_t r, double perturb, T* M, int64_
             trmm<T>(1, (int)sa, (int)sc, (int)sa, T(-1), Ainv, ldm, tmp, sa, T(0), X, ldm, st, part, cap);
         }
     }
-    k_zero_lower<T><<<1024, 256, 0, st>>>(M, ldm, (int)r);
+    launch_k(k_zero_lower<T>, 1024, 256, 0, st, M, ldm, (int)r);
     SKL_LAUNCHED();
     cudaMemsetAsync(norms, 0, 2 * sizeof(double), st);
     // row-sum partials reuse the inverse's scratch (free again here)
@@ -176,6 +181,7 @@ template <typename T>
 __global__ void k_rank(const T* __restrict__ R, int64_t ld, int dmin, double abs_thresh,
                        double rel_thresh, int* out)
 {
+    pdl_wait();
     __shared__ int red[32];
     const double r00 = dmin > 0 ? fabs((double)R[0]) : 0.0;
     const double th = fmax(abs_thresh, rel_thresh * r00);
@@ -202,7 +208,7 @@ template <typename T>
 int64_t count_rank(const T* R, int64_t ld, int64_t dmin, double abs_thresh, double rel_thresh,
                    int* dev_out, int* host_pinned, cudaStream_t st)
 {
-    k_rank<T><<<1, 1024, 0, st>>>(R, ld, (int)dmin, abs_thresh, rel_thresh, dev_out);
+    launch_k(k_rank<T>, 1, 1024, 0, st, R, ld, (int)dmin, abs_thresh, rel_thresh, dev_out);
     SKL_LAUNCHED();
     SKL_CUDA(cudaMemcpyAsync(host_pinned, dev_out, sizeof(int), cudaMemcpyDeviceToHost, st));
     SKL_CUDA(cudaStreamSynchronize(st));
@@ -230,6 +236,7 @@ template <typename T>
 __global__ void k_trmv_upper(const T* __restrict__ M, int64_t ldm, int r, int trans,
                              const double* __restrict__ x, double* __restrict__ y)
 {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r; i += gridDim.x * blockDim.x) {
         double acc = 0.0;
         if (!trans)
@@ -245,7 +252,7 @@ void trmv_upper(const T* M, int64_t ldm, int64_t r, int trans, const double* x, 
                 cudaStream_t st)
 {
     if (r <= 0) return;
-    k_trmv_upper<T><<<(unsigned)((r + 127) / 128), 128, 0, st>>>(M, ldm, (int)r, trans, x, y);
+    launch_k(k_trmv_upper<T>, (unsigned)((r + 127) / 128), 128, 0, st, M, ldm, (int)r, trans, x, y);
     SKL_LAUNCHED();
 }
 template void trmv_upper<float>(const float*, int64_t, int64_t, int, const double*, double*,
