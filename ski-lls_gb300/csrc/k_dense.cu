@@ -19,6 +19,7 @@
 #include <cmath>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 
 namespace skl {
@@ -340,6 +341,7 @@ k_dht_hash(const double* __restrict__ A, int64_t lda, int n, int d, const double
            int m, double alpha_v, T* __restrict__ SA, int64_t ld, double* __restrict__ Yout,
            int64_t ldy, typename Cplx<T>::type* __restrict__ gscratch)
 {
+    pdl_wait();
     using C = typename Cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf;
@@ -453,14 +455,14 @@ static void launch_dht(const double* A, int64_t lda, int64_t n, int64_t d, const
     unsigned grid = (unsigned)std::min<int64_t>(d, 152);
     if (in_smem) {
         allow_max_dynamic_smem((const void*)k_dht_hash<T>);
-        k_dht_hash<T><<<grid, kFftThreads, need, st>>>(A, lda, (int)n, (int)d, D, P, scale, bptr,
+        launch_k(k_dht_hash<T>, grid, kFftThreads, need, st, A, lda, (int)n, (int)d, D, P, scale, bptr,
                                                         bent, (int)m, alpha_v, SA, ld, Yout, ldy,
                                                         nullptr);
     } else {
         const size_t per = 2 * (size_t)P.L * sizeof(C);
         grid = (unsigned)std::min<int64_t>(grid, (int64_t)(gscratch_bytes / per));
         if (grid == 0) fail(SKL_ERR_ALLOC, "DHT scratch too small");
-        k_dht_hash<T><<<grid, kFftThreads, 0, st>>>(A, lda, (int)n, (int)d, D, P, scale, bptr, bent,
+        launch_k(k_dht_hash<T>, grid, kFftThreads, 0, st, A, lda, (int)n, (int)d, D, P, scale, bptr, bent,
                                                      (int)m, alpha_v, SA, ld, Yout, ldy,
                                                      (C*)gscratch_buf);
     }
@@ -510,6 +512,7 @@ void dht_hash_rhs(const double* b, int64_t n, const double* D, int64_t N, const 
 __global__ void k_fro_partial(const double* __restrict__ A, int64_t lda, int64_t n, int64_t d,
                               double* __restrict__ out)
 {
+    pdl_wait();
     __shared__ double red[32];
     double acc = 0.0;
     for (int64_t j = blockIdx.x; j < d; j += gridDim.x) {
@@ -528,7 +531,7 @@ void fro_partials(const double* A, int64_t lda, int64_t n, int64_t d, double* ou
                   cudaStream_t st)
 {
     SKL_CUDA(cudaMemsetAsync(out512, 0, 512 * sizeof(double), st));
-    k_fro_partial<<<512, 256, 0, st>>>(A, lda, n, d, out512);
+    launch_k(k_fro_partial, 512, 256, 0, st, A, lda, n, d, out512);
     SKL_LAUNCHED();
 }
 

@@ -7,6 +7,7 @@
 //    fixed order and results are bitwise reproducible) and the bucket lists of
 //    the hashing matrix S (rows of S with their source rows in order).
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 
 namespace skl {
@@ -17,6 +18,7 @@ namespace skl {
 __global__ void k_csc_narrow_colptr(const int64_t* __restrict__ Ap, int64_t ncol, int64_t nnz,
                                     int* __restrict__ cp, unsigned* __restrict__ bad)
 {
+    pdl_wait();
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j <= ncol;
          j += (int64_t)gridDim.x * blockDim.x) {
         int64_t v = Ap[j];
@@ -33,6 +35,7 @@ __global__ void k_csc_narrow_rows(const int64_t* __restrict__ Ai, const double* 
                                   int64_t nnz, int64_t nrow, int* __restrict__ ri,
                                   unsigned* __restrict__ bad)
 {
+    pdl_wait();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz;
          p += (int64_t)gridDim.x * blockDim.x) {
         int64_t r = Ai[p];
@@ -48,6 +51,7 @@ __global__ void k_csc_narrow_rows(const int64_t* __restrict__ Ai, const double* 
 // col index of every nonzero (CSC order) from the column pointers.
 __global__ void k_expand_colptr(const int* __restrict__ cp, int ncol, int* __restrict__ colof)
 {
+    pdl_wait();
     int j = blockIdx.x;
     if (j >= ncol) return;
     for (int p = cp[j] + threadIdx.x; p < cp[j + 1]; p += blockDim.x) colof[p] = j;
@@ -55,6 +59,7 @@ __global__ void k_expand_colptr(const int* __restrict__ cp, int ncol, int* __res
 
 __global__ void k_iota(unsigned* __restrict__ v, int64_t n)
 {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         v[i] = (unsigned)i;
@@ -70,6 +75,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 __global__ void k_scan_tiles(const int* __restrict__ in, int64_t n, int* __restrict__ out,
                              int* __restrict__ tile_sums)
 {
+    pdl_wait();
     __shared__ int s_warp[kScanThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -113,6 +119,7 @@ __global__ void k_scan_tiles(const int* __restrict__ in, int64_t n, int* __restr
 
 __global__ void k_scan_add(int* __restrict__ out, int64_t n, const int* __restrict__ tile_off)
 {
+    pdl_wait();
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     const int add = tile_off[blockIdx.x];
     for (int t = threadIdx.x; t < kScanTile; t += blockDim.x) {
@@ -123,6 +130,7 @@ __global__ void k_scan_add(int* __restrict__ out, int64_t n, const int* __restri
 
 __global__ void k_set_last(int* out, int64_t n, const int* tile_sums_scanned, int ntiles)
 {
+    pdl_wait();
     // total = exclusive prefix of the last tile + its sum (stored at index ntiles)
     out[n] = tile_sums_scanned[ntiles];
 }
@@ -141,7 +149,7 @@ void scan_exclusive(const int* in, int64_t n, int* out, int* scratch, cudaStream
     if (tiles < 1) tiles = 1;
     int* sums = scratch;                 // tiles+1
     int* sums_scan = scratch + tiles + 1;  // tiles+1
-    k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, n, out, sums);
+    launch_k(k_scan_tiles, (unsigned)tiles, kScanThreads, 0, st, in, n, out, sums);
     SKL_LAUNCHED();
     if (tiles == 1) {
         // sums[0] is the total
@@ -150,9 +158,9 @@ void scan_exclusive(const int* in, int64_t n, int* out, int* scratch, cudaStream
     }
     // scan the tile sums (tiles entries) -> sums_scan[0..tiles], sums_scan[tiles] = total
     scan_exclusive(sums, tiles, sums_scan, scratch + 2 * (tiles + 1), st);
-    k_scan_add<<<(unsigned)tiles, kScanThreads, 0, st>>>(out, n, sums_scan);
+    launch_k(k_scan_add, (unsigned)tiles, kScanThreads, 0, st, out, n, sums_scan);
     SKL_LAUNCHED();
-    k_set_last<<<1, 1, 0, st>>>(out, n, sums_scan, (int)tiles);
+    launch_k(k_set_last, 1, 1, 0, st, out, n, sums_scan, (int)tiles);
     SKL_LAUNCHED();
 }
 
@@ -166,6 +174,7 @@ constexpr int kRsBins = 256;
 __global__ void k_rs_hist(const unsigned* __restrict__ keys, int64_t n, int shift,
                           int* __restrict__ hist /* [bins][tiles] */, int tiles)
 {
+    pdl_wait();
     __shared__ int h[kRsBins];
     for (int b = threadIdx.x; b < kRsBins; b += blockDim.x) h[b] = 0;
     __syncthreads();
@@ -183,6 +192,7 @@ __global__ void k_rs_scatter(const unsigned* __restrict__ keys, const unsigned* 
                              int tiles, unsigned* __restrict__ keys_out,
                              unsigned* __restrict__ vals_out)
 {
+    pdl_wait();
     __shared__ int cnt[kRsBins][kRsChunks + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
@@ -246,10 +256,10 @@ void radix_sort_pairs(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsign
     int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
-        k_rs_hist<<<(unsigned)tiles, kRsThreads, 0, st>>>(ka, n, shift, hist, (int)tiles);
+        launch_k(k_rs_hist, (unsigned)tiles, kRsThreads, 0, st, ka, n, shift, hist, (int)tiles);
         SKL_LAUNCHED();
         scan_exclusive(hist, h, offs, sscr, st);
-        k_rs_scatter<<<(unsigned)tiles, kRsThreads, 0, st>>>(ka, va, n, shift, offs, (int)tiles, kb, vb);
+        launch_k(k_rs_scatter, (unsigned)tiles, kRsThreads, 0, st, ka, va, n, shift, offs, (int)tiles, kb, vb);
         SKL_LAUNCHED();
         unsigned* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
@@ -270,6 +280,7 @@ int bits_for(int64_t maxval)
 // ------------------------------------------------------------- CSR build --
 __global__ void k_count_rows(const int* __restrict__ ri, int64_t nnz, int* __restrict__ cnt)
 {
+    pdl_wait();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz;
          p += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(&cnt[ri[p]], 1);
@@ -279,6 +290,7 @@ __global__ void k_csr_gather(const unsigned* __restrict__ perm, int64_t nnz,
                              const int* __restrict__ colof, const double* __restrict__ Ax,
                              int* __restrict__ ci, double* __restrict__ cx)
 {
+    pdl_wait();
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz;
          q += (int64_t)gridDim.x * blockDim.x) {
         unsigned p = perm[q];
@@ -299,10 +311,10 @@ static unsigned grid_for(int64_t n, int threads, int cap = 152 * 16)
 void csc_narrow(const int64_t* Ap, const int64_t* Ai, const double* Ax, int64_t nrow, int64_t ncol,
                 int64_t nnz, int* cp, int* ri, unsigned* bad, cudaStream_t st)
 {
-    k_csc_narrow_colptr<<<grid_for(ncol + 1, 256), 256, 0, st>>>(Ap, ncol, nnz, cp, bad);
+    launch_k(k_csc_narrow_colptr, grid_for(ncol + 1, 256), 256, 0, st, Ap, ncol, nnz, cp, bad);
     SKL_LAUNCHED();
     if (nnz > 0) {
-        k_csc_narrow_rows<<<grid_for(nnz, 256), 256, 0, st>>>(Ai, Ax, nnz, nrow, ri, bad);
+        launch_k(k_csc_narrow_rows, grid_for(nnz, 256), 256, 0, st, Ai, Ax, nnz, nrow, ri, bad);
         SKL_LAUNCHED();
     }
 }
@@ -327,18 +339,18 @@ void build_csr(const int* cp, const int* ri, const double* Ax, int64_t nrow, int
     int* rest = colof + nnz;
     cudaMemsetAsync(cnt, 0, (nrow + 1) * sizeof(int), st);
     if (nnz > 0) {
-        k_count_rows<<<grid_for(nnz, 256), 256, 0, st>>>(ri, nnz, cnt);
+        launch_k(k_count_rows, grid_for(nnz, 256), 256, 0, st, ri, nnz, cnt);
         SKL_LAUNCHED();
     }
     scan_exclusive(cnt, nrow, rp, rest, st);
     if (nnz == 0) return;
     cudaMemcpyAsync(keys, ri, nnz * sizeof(int), cudaMemcpyDeviceToDevice, st);
-    k_iota<<<grid_for(nnz, 256), 256, 0, st>>>(perm, nnz);
+    launch_k(k_iota, grid_for(nnz, 256), 256, 0, st, perm, nnz);
     SKL_LAUNCHED();
-    k_expand_colptr<<<(unsigned)ncol, 128, 0, st>>>(cp, (int)ncol, colof);
+    launch_k(k_expand_colptr, (unsigned)ncol, 128, 0, st, cp, (int)ncol, colof);
     SKL_LAUNCHED();
     radix_sort_pairs(keys, perm, ktmp, vtmp, nnz, bits_for(nrow - 1), rest, st);
-    k_csr_gather<<<grid_for(nnz, 256), 256, 0, st>>>(perm, nnz, colof, Ax, ci, cx);
+    launch_k(k_csr_gather, grid_for(nnz, 256), 256, 0, st, perm, nnz, colof, Ax, ci, cx);
     SKL_LAUNCHED();
 }
 
@@ -349,6 +361,7 @@ __global__ void k_hash_keys(const unsigned* __restrict__ hidx, int64_t nk, int k
                             unsigned* __restrict__ keys, unsigned* __restrict__ vals,
                             int* __restrict__ cnt)
 {
+    pdl_wait();
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nk;
          q += (int64_t)gridDim.x * blockDim.x) {
         unsigned e = hidx[q];
@@ -364,6 +377,7 @@ __global__ void k_hash_keys(const unsigned* __restrict__ hidx, int64_t nk, int k
 __global__ void k_check_hash_rows(const unsigned* __restrict__ hidx, int64_t nk, unsigned m,
                                   unsigned* __restrict__ status)
 {
+    pdl_wait();
     bool bad = false;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nk;
          q += (int64_t)gridDim.x * blockDim.x)
@@ -374,7 +388,7 @@ __global__ void k_check_hash_rows(const unsigned* __restrict__ hidx, int64_t nk,
 void check_hash_rows(const unsigned* hidx, int64_t nk, int64_t m, unsigned* status, cudaStream_t st)
 {
     if (nk <= 0) return;
-    k_check_hash_rows<<<grid_for(nk, 256), 256, 0, st>>>(hidx, nk, (unsigned)m, status);
+    launch_k(k_check_hash_rows, grid_for(nk, 256), 256, 0, st, hidx, nk, (unsigned)m, status);
     SKL_LAUNCHED();
 }
 
@@ -395,7 +409,7 @@ void build_buckets(const unsigned* hidx, int64_t n, int k, int64_t m, int* bptr,
     unsigned* vtmp = ktmp + nk;
     int* rest = (int*)(vtmp + nk);
     cudaMemsetAsync(cnt, 0, (m + 1) * sizeof(int), st);
-    k_hash_keys<<<grid_for(nk, 256), 256, 0, st>>>(hidx, nk, k, keys, bent, cnt);
+    launch_k(k_hash_keys, grid_for(nk, 256), 256, 0, st, hidx, nk, k, keys, bent, cnt);
     SKL_LAUNCHED();
     scan_exclusive(cnt, m, bptr, rest, st);
     radix_sort_pairs(keys, bent, ktmp, vtmp, nk, bits_for(m - 1), rest, st);

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 
 namespace skl {
@@ -266,6 +267,7 @@ k_tri_n(const MatT<MIXED>* __restrict__ Mr, int64_t ldm, int r, const ValT<MIXED
         ValT<MIXED>* __restrict__ z, const LsqrState* __restrict__ S, int plain_out,
         double* __restrict__ zplain)
 {
+    pdl_wait();
     if (S && S->done) return;
     __shared__ Acc<MIXED> sm[2 * kTriThreads / 32];
     const int npairs = (r + 1) / 2;
@@ -298,6 +300,7 @@ __global__ void __launch_bounds__(kTriThreads, MIXED ? kTriMinBlocks : 1)
 k_tri_t(const MatT<MIXED>* __restrict__ Mc, int64_t ldm, int r, const ValT<MIXED>* __restrict__ t,
         double* __restrict__ vh, LsqrState* __restrict__ S, int init, double* __restrict__ partials)
 {
+    pdl_wait();
     if (S->done) return;
     __shared__ Acc<MIXED> sm[2 * kTriThreads / 32];
     const double coef = init ? 0.0 : S->coef_t;
@@ -399,6 +402,7 @@ k_spmv_n_csr(const int* __restrict__ rp, const int* __restrict__ ci, const ValT<
              double* __restrict__ uh, ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S,
              double* __restrict__ partials)
 {
+    pdl_wait();
     using V = ValT<MIXED>;
     if (S->done) return;
     __shared__ double wsum[kLThreads / 32];
@@ -546,6 +550,7 @@ k_spmv_t_csc(const int* __restrict__ cp, const int* __restrict__ ri, const ValT<
              const ValT<MIXED>* __restrict__ us, ValT<MIXED>* __restrict__ t,
              const LsqrState* __restrict__ S)
 {
+    pdl_wait();
     using V = ValT<MIXED>;
     if (S->done) return;
     const int lane = threadIdx.x % L;
@@ -611,6 +616,7 @@ k_spmv_n_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int*
                int r, int chunk, const ValT<MIXED>* __restrict__ z, double* __restrict__ part,
                const LsqrState* __restrict__ S)
 {
+    pdl_wait();
     using V = ValT<MIXED>;
     if (S->done) return;
     __shared__ int scol[kDenseChunk];
@@ -659,6 +665,7 @@ k_spmv_n_dense_reduce(const double* __restrict__ part, int nchunks, int n, doubl
                       ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S,
                       double* __restrict__ partials)
 {
+    pdl_wait();
     if (S->done) return;
     __shared__ double red[kLThreads / 32];
     const double coef = S->coef_n;
@@ -694,6 +701,7 @@ k_spmv_t_dense(const ValT<MIXED>* __restrict__ A, int64_t lda, int n, const int*
                const double* __restrict__ colscale, int r, const ValT<MIXED>* __restrict__ us,
                ValT<MIXED>* __restrict__ t, const LsqrState* __restrict__ S)
 {
+    pdl_wait();
     using V = ValT<MIXED>;
     if (S->done) return;
     __shared__ Acc<MIXED> red[kDtCols][kLThreads / 32];
@@ -751,6 +759,7 @@ __global__ void __launch_bounds__(kLThreads)
 k_lsqr_init_u(const double* __restrict__ b, int n, double* __restrict__ uh,
               ValT<MIXED>* __restrict__ us, LsqrState* __restrict__ S, double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double ss = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -776,6 +785,7 @@ __global__ void __launch_bounds__(kLThreads)
 k_lsqr_init_v(int r, double* __restrict__ vh, ValT<MIXED>* __restrict__ vs, double* __restrict__ w,
               double* __restrict__ y, LsqrState* __restrict__ S)
 {
+    pdl_wait();
     const double alpha = S->alpha_new;
     const double beta = S->beta;
     const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
@@ -808,6 +818,7 @@ k_lsqr_update(int r, const double* __restrict__ vh, ValT<MIXED>* __restrict__ vs
               double* __restrict__ w, double* __restrict__ y, LsqrState* __restrict__ S,
               const double* __restrict__ partials, int npart)
 {
+    pdl_wait();
     if (S->done) return;
     // alpha' = ||vh|| from tri_t's per-block partials, reduced by every block in
     // the same fixed order (so every block agrees bit for bit), then the
@@ -970,10 +981,9 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
         const int chunk = B.dense_chunk;
         const int nchunks = (int)((P.r + chunk - 1) / chunk);
         dim3 g((unsigned)((P.n + kDnRows - 1) / kDnRows), nchunks);
-        k_spmv_n_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
+        launch_k(k_spmv_n_dense<MIXED>, g, kLThreads, 0, st, (const V*)P.Ad, P.lda, (int)P.n, P.cols,
                                                        (int)P.r, chunk, (const V*)B.z, B.dpart, B.S);
-        k_spmv_n_dense_reduce<MIXED><<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 1024), kLThreads,
-                                       0, st>>>(B.dpart, nchunks, (int)P.n, B.uh, (V*)B.us, B.S,
+        launch_k(k_spmv_n_dense_reduce<MIXED>, (unsigned)std::min<int64_t>((P.n + 255) / 256, 1024), kLThreads, 0, st, B.dpart, nchunks, (int)P.n, B.uh, (V*)B.us, B.S,
                                                 B.partials);
         SKL_LAUNCHED();
         SKL_LAUNCHED();
@@ -990,7 +1000,7 @@ static void launch_spmv_n(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     const unsigned g = (unsigned)((P.n + rpb - 1) / rpb);
 #define SPMV_N(LL) do { \
         if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_spmv_n_csr<MIXED, LL>); \
-        k_spmv_n_csr<MIXED, LL><<<g, kLThreads, smem, st>>>(P.rp, P.ci, (const V*)P.cx, (int)P.n, rpb, (const V*)B.z, stage, B.uh, (V*)B.us, B.S, B.partials); \
+        launch_k(k_spmv_n_csr<MIXED, LL>, g, kLThreads, smem, st, P.rp, P.ci, (const V*)P.cx, (int)P.n, rpb, (const V*)B.z, stage, B.uh, (V*)B.us, B.S, B.partials); \
     } while (0)
     if (L == 32) SPMV_N(32);
     else if (L == 16) SPMV_N(16);
@@ -1006,7 +1016,7 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     using V = ValT<MIXED>;
     if (P.Ad) {
         unsigned g = (unsigned)std::min<int64_t>((P.r + kDtCols - 1) / kDtCols, 152 * 16);
-        k_spmv_t_dense<MIXED><<<g, kLThreads, 0, st>>>((const V*)P.Ad, P.lda, (int)P.n, P.cols,
+        launch_k(k_spmv_t_dense<MIXED>, g, kLThreads, 0, st, (const V*)P.Ad, P.lda, (int)P.n, P.cols,
                                                        P.opscale, (int)P.r, (const V*)B.us,
                                                        (V*)B.t, B.S);
         SKL_LAUNCHED();
@@ -1016,7 +1026,7 @@ static void launch_spmv_t(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st)
     const int L = P.lanes_t ? P.lanes_t : lanes_for(avg);
     const int64_t threads = (int64_t)P.r * L;
     unsigned g = (unsigned)std::min<int64_t>((threads + kLThreads - 1) / kLThreads, 152 * 32);
-#define SPMV_T(LL) k_spmv_t_csc<MIXED, LL><<<g, kLThreads, 0, st>>>(P.cp, P.ri, (const V*)P.rx, P.cols, P.opscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
+#define SPMV_T(LL) launch_k(k_spmv_t_csc<MIXED, LL>, g, kLThreads, 0, st, P.cp, P.ri, (const V*)P.rx, P.cols, P.opscale, (int)P.r, (const V*)B.us, (V*)B.t, B.S)
     if (L == 32) SPMV_T(32);
     else if (L == 16) SPMV_T(16);
     else if (L == 8) SPMV_T(8);
@@ -1043,7 +1053,7 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     };
     const unsigned gt = tri_blocks(P.r);
     mark(4);
-    k_tri_n<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
+    launch_k(k_tri_n<MIXED>, gt, kTriThreads, 0, st, (const MT*)P.Mrow, P.ldm, (int)P.r, (const V*)B.vs,
                                               P.cols, P.opscale, (V*)B.z, B.S, 0, nullptr);
     SKL_LAUNCHED();
     mark(5);
@@ -1054,12 +1064,12 @@ static void launch_iteration(const LsqrProblem& P, LsqrBufs& B, cudaStream_t st,
     launch_spmv_t<MIXED>(P, B, st);
     mark(3);
     mark(6);
-    k_tri_t<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+    launch_k(k_tri_t<MIXED>, gt, kTriThreads, 0, st, (const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
                                               B.S, 0, B.partials);
     SKL_LAUNCHED();
     mark(7);
     unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
-    k_lsqr_update<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S,
+    launch_k(k_lsqr_update<MIXED>, gu, kLThreads, 0, st, (int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S,
                                                    B.partials, (int)gt);
     SKL_LAUNCHED();
 }
@@ -1079,15 +1089,15 @@ static LsqrResult run_impl(const LsqrProblem& P, const double* b, double tol, in
     SKL_CUDA(cudaMemsetAsync(B.z, 0, P.d * sizeof(V), st));
     // beta_1 u_1 = b ; alpha_1 v_1 = Abar^T u_1
     unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.n + 255) / 256, 1024));
-    k_lsqr_init_u<MIXED><<<gi, kLThreads, 0, st>>>(b, (int)P.n, B.uh, (V*)B.us, B.S, B.partials);
+    launch_k(k_lsqr_init_u<MIXED>, gi, kLThreads, 0, st, b, (int)P.n, B.uh, (V*)B.us, B.S, B.partials);
     SKL_LAUNCHED();
     launch_spmv_t<MIXED>(P, B, st);
     const unsigned gt = tri_blocks(P.r);
-    k_tri_t<MIXED><<<gt, kTriThreads, 0, st>>>((const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
+    launch_k(k_tri_t<MIXED>, gt, kTriThreads, 0, st, (const MT*)P.M, P.ldm, (int)P.r, (const V*)B.t, B.vh,
                                               B.S, 1, B.partials);
     SKL_LAUNCHED();
     unsigned gu = (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152));
-    k_lsqr_init_v<MIXED><<<gu, kLThreads, 0, st>>>((int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
+    launch_k(k_lsqr_init_v<MIXED>, gu, kLThreads, 0, st, (int)P.r, B.vh, (V*)B.vs, B.w, B.y, B.S);
     SKL_LAUNCHED();
 
     // Capture a block of iterations once, replay until the device says done.
@@ -1234,6 +1244,7 @@ template <bool MIXED>
 __global__ void k_prod_in(const double* __restrict__ x, int64_t len, const double* __restrict__ vscale,
                           ValT<MIXED>* __restrict__ out)
 {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
          i += (int64_t)gridDim.x * blockDim.x)
         out[i] = store_val<MIXED>(vscale ? x[i] / vscale[i] : x[i]);
@@ -1243,6 +1254,7 @@ template <bool MIXED>
 __global__ void k_prod_out(const ValT<MIXED>* __restrict__ v, const double* __restrict__ vplain,
                            int64_t len, const double* __restrict__ vscale, double* __restrict__ y)
 {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
          i += (int64_t)gridDim.x * blockDim.x) {
         double val;
@@ -1256,6 +1268,7 @@ __global__ void k_prod_out(const ValT<MIXED>* __restrict__ v, const double* __re
 __global__ void __launch_bounds__(kLThreads)
 k_beta_norm(const double* __restrict__ x, int64_t n, LsqrState* __restrict__ S)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double ss = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss += x[i] * x[i];
@@ -1277,15 +1290,15 @@ static void product_impl(const LsqrProblem& P, char trans, const double* x, doub
     SKL_CUDA(cudaMemsetAsync(B.us, 0, P.n * sizeof(V), st));
     const unsigned g = 152 * 8;
     if (trans == 'n') {
-        k_prod_in<MIXED><<<g, 256, 0, st>>>(x, P.d, vscale, (V*)B.z);
+        launch_k(k_prod_in<MIXED>, g, 256, 0, st, x, P.d, vscale, (V*)B.z);
         launch_spmv_n<MIXED>(P, B, st);
-        k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.us, MIXED ? nullptr : B.uh, P.n, nullptr, y);
+        launch_k(k_prod_out<MIXED>, g, 256, 0, st, (const V*)B.us, MIXED ? nullptr : B.uh, P.n, nullptr, y);
     } else {
-        k_prod_in<MIXED><<<g, 256, 0, st>>>(x, P.n, nullptr, (V*)B.us);
-        k_beta_norm<<<1, kLThreads, 0, st>>>(x, P.n, B.S);
+        launch_k(k_prod_in<MIXED>, g, 256, 0, st, x, P.n, nullptr, (V*)B.us);
+        launch_k(k_beta_norm, 1, kLThreads, 0, st, x, P.n, B.S);
         SKL_LAUNCHED();
         launch_spmv_t<MIXED>(P, B, st);
-        k_prod_out<MIXED><<<g, 256, 0, st>>>((const V*)B.t, nullptr, P.r, vscale, y);
+        launch_k(k_prod_out<MIXED>, g, 256, 0, st, (const V*)B.t, nullptr, P.r, vscale, y);
     }
     SKL_LAUNCHED();
     SKL_LAUNCHED();
@@ -1307,6 +1320,7 @@ k_tri_n_f64acc(const MT* __restrict__ Mr, int64_t ldm, int r, const double* __re
                const int* __restrict__ cols, const double* __restrict__ colscale,
                double* __restrict__ xfull)
 {
+    pdl_wait();
     __shared__ double red[kTriThreads / 32];
     for (int i = blockIdx.x; i < r; i += gridDim.x) {
         const MT* row = Mr + (int64_t)i * ldm;
@@ -1328,10 +1342,10 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
     (void)scratch;
     const unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
     if (P.precision == SKL_PREC_MIXED)
-        k_tri_n_f64acc<float><<<g, kTriThreads, 0, st>>>((const float*)P.Mrow, P.ldm, (int)P.r, yv,
+        launch_k(k_tri_n_f64acc<float>, g, kTriThreads, 0, st, (const float*)P.Mrow, P.ldm, (int)P.r, yv,
                                                          P.cols, P.colscale, xfull);
     else
-        k_tri_n_f64acc<double><<<g, kTriThreads, 0, st>>>((const double*)P.Mrow, P.ldm, (int)P.r, yv,
+        launch_k(k_tri_n_f64acc<double>, g, kTriThreads, 0, st, (const double*)P.Mrow, P.ldm, (int)P.r, yv,
                                                           P.cols, P.colscale, xfull);
     SKL_LAUNCHED();
 }
@@ -1353,6 +1367,7 @@ void precond_apply(const LsqrProblem& P, const double* yv, double* xfull, void* 
 __global__ void k_hash_t(const unsigned* __restrict__ hidx, int n, int k, double v,
                          const double* __restrict__ g, double* __restrict__ h)
 {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double acc = 0.0;
         for (int t = 0; t < k; ++t) {
@@ -1370,6 +1385,7 @@ k_atr_sel(const int* __restrict__ cp, const int* __restrict__ ri, const double* 
           const int* __restrict__ cols, const double* __restrict__ colscale, int r,
           const double* __restrict__ h, double* __restrict__ t)
 {
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -1394,6 +1410,7 @@ __global__ void __launch_bounds__(kTriThreads)
 k_tri_t_f64(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restrict__ t,
             double* __restrict__ dc)
 {
+    pdl_wait();
     __shared__ double red[kTriThreads / 32];
     for (int j = blockIdx.x; j < r; j += gridDim.x) {
         const MT* col = Mc + (int64_t)j * ldm;
@@ -1408,6 +1425,7 @@ k_tri_t_f64(const MT* __restrict__ Mc, int64_t ldm, int r, const double* __restr
 __global__ void __launch_bounds__(kLThreads)
 k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ part)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double ss = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -1420,6 +1438,7 @@ k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ part)
 // c[i] += sgn * dc[i]
 __global__ void k_axpy_sign(int n, double sgn, const double* __restrict__ dc, double* __restrict__ c)
 {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         c[i] = fma(sgn, dc[i], c[i]);
 }
@@ -1433,8 +1452,8 @@ __global__ void k_sum_parts(const double* __restrict__ part, int np, double* __r
 static void vec_norm(const double* x, int64_t n, double* part, double* out, cudaStream_t st)
 {
     const int np = 256;
-    k_sumsq<<<np, kLThreads, 0, st>>>(x, n, part);
-    k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
+    launch_k(k_sumsq, np, kLThreads, 0, st, x, n, part);
+    launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, out);
     SKL_LAUNCHED();
     SKL_LAUNCHED();
 }
@@ -1447,15 +1466,14 @@ void sketch_refine_direction(const LsqrProblem& P, const int* bptr, const unsign
     if (P.r <= 0 || P.Ad64 || P.Ad) fail(SKL_ERR_INVALID, "sketch refinement: sparse problems only");
     sketch_rhs(bptr, bent, m, k, rs, gm, st);
     const double v = 1.0 / std::sqrt((double)k);
-    k_hash_t<<<(unsigned)std::min<int64_t>((P.n + 255) / 256, 152 * 16), 256, 0, st>>>(
+    launch_k(k_hash_t, (unsigned)std::min<int64_t>((P.n + 255) / 256, 152 * 16), 256, 0, st, 
         hidx, (int)P.n, k, v, gm, h);
-    k_atr_sel<<<(unsigned)std::min<int64_t>((P.r * 32 + kLThreads - 1) / kLThreads, 152 * 32),
-                kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, P.cols, P.colscale, (int)P.r, h, t);
+    launch_k(k_atr_sel, (unsigned)std::min<int64_t>((P.r * 32 + kLThreads - 1) / kLThreads, 152 * 32), kLThreads, 0, st, P.cp, P.ri, P.rx64, P.cols, P.colscale, (int)P.r, h, t);
     const unsigned g = (unsigned)std::min<int64_t>(P.r, 152 * 16);
     if (P.precision == SKL_PREC_MIXED)
-        k_tri_t_f64<float><<<g, kTriThreads, 0, st>>>((const float*)P.M, P.ldm, (int)P.r, t, dc);
+        launch_k(k_tri_t_f64<float>, g, kTriThreads, 0, st, (const float*)P.M, P.ldm, (int)P.r, t, dc);
     else
-        k_tri_t_f64<double><<<g, kTriThreads, 0, st>>>((const double*)P.M, P.ldm, (int)P.r, t, dc);
+        launch_k(k_tri_t_f64<double>, g, kTriThreads, 0, st, (const double*)P.M, P.ldm, (int)P.r, t, dc);
     for (int q = 0; q < 3; ++q) SKL_LAUNCHED();
     vec_norm(gm, m, part, norms, st);
     vec_norm(dc, P.r, part + 256, norms + 1, st);
@@ -1465,14 +1483,13 @@ void sketch_refine_apply(const LsqrProblem& P, double sgn, const double* dc, dou
                          const double* b, double* x, double* rs, double* part, double* rnorm,
                          cudaStream_t st)
 {
-    k_axpy_sign<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152)), 256,
-                  0, st>>>((int)P.r, sgn, dc, c);
+    launch_k(k_axpy_sign, (unsigned)std::max<int64_t>(1, std::min<int64_t>((P.r + 255) / 256, 152)), 256, 0, st, (int)P.r, sgn, dc, c);
     SKL_LAUNCHED();
     SKL_CUDA(cudaMemsetAsync(x, 0, P.d * sizeof(double), st));
     precond_apply(P, c, x, nullptr, st);
     const int np = 512;
-    k_residual_csr<<<np, kLThreads, 0, st>>>(P.rp, P.ci, P.cx64, (int)P.n, x, b, rs, part);
-    k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, rnorm);
+    launch_k(k_residual_csr, np, kLThreads, 0, st, P.rp, P.ci, P.cx64, (int)P.n, x, b, rs, part);
+    launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, rnorm);
     SKL_LAUNCHED();
     SKL_LAUNCHED();
 }
@@ -1484,6 +1501,7 @@ k_residual_csr(const int* __restrict__ rp, const int* __restrict__ ci, const dou
                int n, const double* __restrict__ x, const double* __restrict__ b,
                double* __restrict__ r, double* __restrict__ part)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1508,6 +1526,7 @@ k_residual_dense(const double* __restrict__ A, int64_t lda, int n, int d,
                  const double* __restrict__ x, const double* __restrict__ b,
                  double* __restrict__ r, double* __restrict__ part)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double ss = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1526,6 +1545,7 @@ __global__ void __launch_bounds__(kLThreads)
 k_atr_csc(const int* __restrict__ cp, const int* __restrict__ ri, const double* __restrict__ rx,
           int d, const double* __restrict__ r, double* __restrict__ part)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1545,6 +1565,7 @@ __global__ void __launch_bounds__(kLThreads)
 k_atr_dense(const double* __restrict__ A, int64_t lda, int n, int d, const double* __restrict__ r,
             double* __restrict__ part)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double ss = 0.0;
     for (int j = blockIdx.x; j < d; j += gridDim.x) {
@@ -1558,6 +1579,7 @@ k_atr_dense(const double* __restrict__ A, int64_t lda, int n, int d, const doubl
 
 __global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out)
 {
+    pdl_wait();
     __shared__ double red[kLThreads / 32];
     double s = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
@@ -1571,15 +1593,15 @@ void residual_and_backward(const LsqrProblem& P, const double* x, const double* 
 {
     const int np = 512;
     if (P.Ad64) {
-        k_residual_dense<<<np, kLThreads, 0, st>>>(P.Ad64, P.lda64, (int)P.n, (int)P.d, x, b, r, part);
-        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
-        k_atr_dense<<<np, kLThreads, 0, st>>>(P.Ad64, P.lda64, (int)P.n, (int)P.d, r, part);
-        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out + 1);
+        launch_k(k_residual_dense, np, kLThreads, 0, st, P.Ad64, P.lda64, (int)P.n, (int)P.d, x, b, r, part);
+        launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, out);
+        launch_k(k_atr_dense, np, kLThreads, 0, st, P.Ad64, P.lda64, (int)P.n, (int)P.d, r, part);
+        launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, out + 1);
     } else {
-        k_residual_csr<<<np, kLThreads, 0, st>>>(P.rp, P.ci, P.cx64, (int)P.n, x, b, r, part);
-        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out);
-        k_atr_csc<<<np, kLThreads, 0, st>>>(P.cp, P.ri, P.rx64, (int)P.d, r, part);
-        k_sum_parts<<<1, kLThreads, 0, st>>>(part, np, out + 1);
+        launch_k(k_residual_csr, np, kLThreads, 0, st, P.rp, P.ci, P.cx64, (int)P.n, x, b, r, part);
+        launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, out);
+        launch_k(k_atr_csc, np, kLThreads, 0, st, P.cp, P.ri, P.rx64, (int)P.d, r, part);
+        launch_k(k_sum_parts, 1, kLThreads, 0, st, part, np, out + 1);
     }
     for (int q = 0; q < 4; ++q) SKL_LAUNCHED();
 }
@@ -1592,6 +1614,7 @@ __global__ void k_split_csr_scaled(const int* __restrict__ ci, const double* __r
                                    int64_t nnz, const double* __restrict__ colscale,
                                    float2* __restrict__ out)
 {
+    pdl_wait();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz;
          p += (int64_t)gridDim.x * blockDim.x) {
         ff f = ff_from_double(cx[p] * colscale[ci[p]]);
@@ -1604,7 +1627,7 @@ void split_csr_scaled(const int* ci, const double* cx, int64_t nnz, const double
 {
     if (nnz <= 0) return;
     unsigned g = (unsigned)std::min<int64_t>((nnz + 255) / 256, 152 * 32);
-    k_split_csr_scaled<<<g, 256, 0, st>>>(ci, cx, nnz, colscale, out);
+    launch_k(k_split_csr_scaled, g, 256, 0, st, ci, cx, nnz, colscale, out);
     SKL_LAUNCHED();
 }
 
@@ -1613,6 +1636,7 @@ __global__ void __launch_bounds__(kLThreads)
 k_split_csc_scaled(const int* __restrict__ cp, const double* __restrict__ Ax, int d,
                    const double* __restrict__ colscale, float2* __restrict__ out)
 {
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -1630,7 +1654,7 @@ void split_csc_scaled(const int* cp, const double* Ax, int64_t d, const double* 
 {
     if (d <= 0) return;
     unsigned g = (unsigned)std::min<int64_t>((d * 32 + kLThreads - 1) / kLThreads, 152 * 16);
-    k_split_csc_scaled<<<g, kLThreads, 0, st>>>(cp, Ax, (int)d, colscale, out);
+    launch_k(k_split_csc_scaled, g, kLThreads, 0, st, cp, Ax, (int)d, colscale, out);
     SKL_LAUNCHED();
 }
 
@@ -1640,6 +1664,7 @@ void split_csc_scaled(const int* cp, const double* Ax, int64_t d, const double* 
 __global__ void k_split_dense(const double* __restrict__ A, int64_t lda, int64_t n, int64_t d,
                               float2* __restrict__ out, unsigned* __restrict__ status)
 {
+    pdl_wait();
     const int64_t total = n * d;
     bool bad = false;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -1658,12 +1683,13 @@ void split_dense(const double* A, int64_t lda, int64_t n, int64_t d, float2* out
                  unsigned* status, cudaStream_t st)
 {
     if (n * d <= 0) return;
-    k_split_dense<<<152 * 32, 256, 0, st>>>(A, lda, n, d, out, status);
+    launch_k(k_split_dense, 152 * 32, 256, 0, st, A, lda, n, d, out, status);
     SKL_LAUNCHED();
 }
 
 __global__ void k_vec_add(double* __restrict__ x, const double* __restrict__ a, int64_t n)
 {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         x[i] += a[i];
@@ -1673,13 +1699,14 @@ void vec_add(double* x, const double* a, int64_t n, cudaStream_t st)
 {
     if (n <= 0) return;
     unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
-    k_vec_add<<<g, 256, 0, st>>>(x, a, n);
+    launch_k(k_vec_add, g, 256, 0, st, x, a, n);
     SKL_LAUNCHED();
 }
 
 template <typename T>
 __global__ void k_extend_identity(T* __restrict__ Mc, int64_t ldm, int r, int r2)
 {
+    pdl_wait();
     for (int j = r + blockIdx.x; j < r2; j += gridDim.x) {
         T* col = Mc + (int64_t)j * ldm;
         for (int i = threadIdx.x; i <= j; i += blockDim.x) col[i] = (i == j) ? T(1) : T(0);
@@ -1691,7 +1718,7 @@ void extend_identity(T* Mc, int64_t ldm, int64_t r, int64_t r2, cudaStream_t st)
 {
     if (r2 <= r) return;
     unsigned g = (unsigned)std::min<int64_t>(r2 - r, 152 * 8);
-    k_extend_identity<T><<<g, 256, 0, st>>>(Mc, ldm, (int)r, (int)r2);
+    launch_k(k_extend_identity<T>, g, 256, 0, st, Mc, ldm, (int)r, (int)r2);
     SKL_LAUNCHED();
 }
 template void extend_identity<float>(float*, int64_t, int64_t, int64_t, cudaStream_t);
@@ -1701,6 +1728,7 @@ template void extend_identity<double>(double*, int64_t, int64_t, int64_t, cudaSt
 template <typename T>
 __global__ void k_transpose_upper(const T* __restrict__ Mc, int64_t ldm, int r, T* __restrict__ Mr)
 {
+    pdl_wait();
     __shared__ T tile[32][33];
     const int bi = blockIdx.x * 32, bj = blockIdx.y * 32;
     if (bi > bj + 31) return;   // tile entirely below the diagonal
@@ -1720,7 +1748,7 @@ void transpose_upper(const T* Mc, int64_t ldm, int64_t r, T* Mr, cudaStream_t st
 {
     if (r <= 0) return;
     dim3 g((unsigned)((r + 31) / 32), (unsigned)((r + 31) / 32));
-    k_transpose_upper<T><<<g, dim3(32, 8), 0, st>>>(Mc, ldm, (int)r, Mr);
+    launch_k(k_transpose_upper<T>, g, dim3(32, 8), 0, st, Mc, ldm, (int)r, Mr);
     SKL_LAUNCHED();
 }
 template void transpose_upper<float>(const float*, int64_t, int64_t, float*, cudaStream_t);

@@ -14,6 +14,7 @@
 #include <cmath>
 
 #include "skl_internal.hpp"
+#include "launch.cuh"
 #include "common.cuh"
 
 namespace skl {
@@ -27,6 +28,7 @@ k_sketch_sparse_smem(const int* __restrict__ cp, const int* __restrict__ ri,
                      int m, T* __restrict__ SA, int64_t ld, int equilibrate, double inv_sqrt_k,
                      double* __restrict__ colnorm, double* __restrict__ colscale)
 {
+    pdl_wait();
     extern __shared__ unsigned long long acc[];   // m entries
     __shared__ double s_red[NT / 32];
     const int j = blockIdx.x;
@@ -82,6 +84,7 @@ k_sketch_sparse_global(const int* __restrict__ cp, const int* __restrict__ ri,
                        double* __restrict__ colnorm, double* __restrict__ colscale,
                        unsigned long long* __restrict__ scratch, int col0)
 {
+    pdl_wait();
     __shared__ double s_red[kSketchThreads / 32];
     const int j = col0 + blockIdx.x;
     unsigned long long* acc = scratch + (int64_t)blockIdx.x * m;
@@ -144,7 +147,7 @@ static void launch_sketch_smem(const int* cp, const int* ri, const double* Ax, i
                                size_t smem, cudaStream_t st)
 {
     allow_max_dynamic_smem((const void*)k_sketch_sparse_smem<T, NT>);
-    k_sketch_sparse_smem<T, NT><<<(unsigned)d, NT, smem, st>>>(cp, ri, Ax, hidx, k, (int)m, SA, ld,
+    launch_k(k_sketch_sparse_smem<T, NT>, (unsigned)d, NT, smem, st, cp, ri, Ax, hidx, k, (int)m, SA, ld,
                                                                equilibrate, isk, colnorm, colscale);
     SKL_LAUNCHED();
 }
@@ -179,7 +182,7 @@ void sketch_sparse(const int* cp, const int* ri, const double* Ax, int64_t n, in
     SKL_CUDA(cudaMallocAsync(&scratch, (size_t)slice * m * sizeof(unsigned long long), st));
     for (int64_t c0 = 0; c0 < d; c0 += slice) {
         int nc = (int)((d - c0) < slice ? (d - c0) : slice);
-        k_sketch_sparse_global<T><<<nc, kSketchThreads, 0, st>>>(
+        launch_k(k_sketch_sparse_global<T>, nc, kSketchThreads, 0, st, 
             cp, ri, Ax, hidx, k, (int)m, SA, ld, equilibrate, isk, colnorm, colscale, scratch,
             (int)c0);
         SKL_LAUNCHED();
@@ -200,6 +203,7 @@ __global__ void k_sketch_rhs(const int* __restrict__ bptr, const unsigned* __res
                              int m, double v, const double* __restrict__ b,
                              double* __restrict__ Sb)
 {
+    pdl_wait();
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < m; h += gridDim.x * blockDim.x) {
         double acc = 0.0;
         for (int q = bptr[h]; q < bptr[h + 1]; ++q) {
@@ -216,7 +220,7 @@ void sketch_rhs(const int* bptr, const unsigned* bent, int64_t m, int k, const d
 {
     const double v = 1.0 / std::sqrt((double)k);
     unsigned g = (unsigned)((m + 255) / 256);
-    k_sketch_rhs<<<g, 256, 0, st>>>(bptr, bent, (int)m, v, b, Sb);
+    launch_k(k_sketch_rhs, g, 256, 0, st, bptr, bent, (int)m, v, b, Sb);
     SKL_LAUNCHED();
 }
 
