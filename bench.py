@@ -189,6 +189,17 @@ def make_workload(name):
     return w, A, b, time.perf_counter() - t0
 
 
+def oracle_sample_text(kind):
+    """What the CPU oracle restates for a workload kind (for the baseline's `sample`)."""
+    if kind == "blendenpik":
+        return ("restatement of ls_dense_blendenpik: the random signs and row sample from the C "
+                "library's stream, numpy's FFT for the DHT, LAPACK dgeqrf through numpy's OpenBLAS "
+                "on all cores, LSQR in C loops single-threaded")
+    return ("restatement of the reference algorithm: C loops single-threaded as the reference's "
+            "MAX_NUM_THREADS = 1, LAPACK dgeqp3/dormqr/dtrcon through numpy's OpenBLAS on all "
+            "cores; SPQR replaced by dense CPQR of the sketch")
+
+
 def oracle_kind(w):
     """Which oracle solver a workload runs: "sparse", "dense" or "blendenpik"."""
     return "blendenpik" if w.get("solver") == "blendenpik" else w["kind"]
@@ -270,10 +281,7 @@ def cpu_baseline_run(kind, name, A, b, gamma, k):
                 one = {"error": str(e)[:300]}
     cpu = {"value": t_all, "unit": "s", "cores": os.cpu_count(), "kind": "port",
            "cpu_model": cpu_model(),
-           "sample": "one full solve of the workload by the CPU oracle (restatement of the "
-                     "reference algorithm: C loops single-threaded as the reference's "
-                     "MAX_NUM_THREADS = 1, LAPACK dgeqp3/dormqr/dtrcon through numpy's "
-                     "OpenBLAS on all cores; SPQR replaced by dense CPQR of the sketch)",
+           "sample": "one full solve of the workload by the CPU oracle (%s)" % oracle_sample_text(kind),
            "phases_s": out["phases_s"], "it": int(out["it"]), "rank": int(out["rank"]),
            "blas_one_thread": one}
     return cpu, out
@@ -307,11 +315,7 @@ def run_reference(args, rank):
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
                          "cpu_model": cpu_model(),
                          "sample": "full solve of the workload per step, median of the timed "
-                                   "steps; CPU oracle (restatement of the reference algorithm: "
-                                   "C loops single-threaded as the reference's "
-                                   "MAX_NUM_THREADS = 1, LAPACK dgeqp3/dormqr/dtrcon through "
-                                   "numpy's OpenBLAS on all cores; SPQR replaced by dense CPQR "
-                                   "of the sketch)"},
+                                   "steps; CPU oracle (%s)" % oracle_sample_text(oracle_kind(w))},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "solve": {"rank": int(out["rank"]), "it": int(out["it"]), "flag": int(out["flag"]),
                   "phases_s": out["phases_s"], "step_s": times,
