@@ -179,6 +179,17 @@ def test_argument_errors_come_before_any_device_work(L):
     assert dense(8, 3, 5) == skl.SKL_ERR_INVALID
     assert "lda" in skl.last_error()
     assert dense(8, 0, 8) == skl.SKL_OK
+    # Blendenpik (src/ls_dense_blendenpik.cpp:38-40): the same checks, before the device
+    def blendenpik(n, d, lda):
+        o = skl.default_opts()
+        a, bb, xx = np.zeros(max(lda * d, 1)), np.ones(max(n, 1)), np.zeros(max(d, 1))
+        info = skl.SklInfo()
+        return L.skl_dense_blendenpik_solve(vp(a.ctypes.data), lda, n, d, vp(bb.ctypes.data),
+                                            vp(xx.ctypes.data), ctypes.byref(o), ctypes.byref(info))
+    assert blendenpik(4, 5, 4) == skl.SKL_ERR_NOT_OVERDETERMINED
+    assert skl.last_error() == "Matrix is not overdetermined."
+    assert blendenpik(8, 3, 5) == skl.SKL_ERR_INVALID
+    assert blendenpik(8, 0, 8) == skl.SKL_OK
 
 
 def test_python_structs_match_the_c_header(tmp_path):
