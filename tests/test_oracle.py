@@ -173,3 +173,18 @@ def test_blendenpik_rejects_underdetermined_and_oversized_sample():
         orc.ls_dense_blendenpik(np.ones((3, 5)), np.ones(3), 2.2)
     with pytest.raises(ValueError):
         orc.ls_dense_blendenpik(np.eye(10, 6), np.ones(10), 2.0)   # 12 rows of 10
+
+
+def test_blendenpik_padded_transform_vs_lstsq():
+    """The transform padded to a smooth even length (the reference pads in its
+    wisdom mode, src/fast_unitary_transform.cpp:63-64): the sample is drawn from
+    all N rows, including rows that come from the zero padding."""
+    rng = np.random.default_rng(12)
+    A = rng.standard_normal((1001, 40))
+    b = rng.standard_normal(1001)
+    N = 1050   # even, N / 2 = 525 = 3 * 5^2 * 7
+    out = orc.ls_dense_blendenpik(A, b, 2.2, it_tol=1e-12, seed=3, N=N)
+    xr = np.linalg.lstsq(A, b, rcond=None)[0]
+    assert out["rank"] == 40 and out["flag"] == 0
+    assert out["rows"].max() < N and len(np.unique(out["rows"])) == out["m"]
+    assert np.linalg.norm(out["x"] - xr) <= 1e-8 * np.linalg.norm(xr)
