@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <array>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -137,12 +138,53 @@ void rng_srand(uint32_t seed)
     g_seeded = true;
 }
 
+// x mod d for 32-bit x and d >= 1 with the precomputed M = floor((2^64 - 1) / d) + 1
+// (the direct remainder computation of Lemire, Kaser and Kurz, "Faster
+// remainder by direct computation", 2019): exact for every 32-bit x, two
+// multiplies instead of a division.
+static inline uint32_t fastmod_u32(uint32_t x, uint64_t M, uint32_t d)
+{
+    const uint64_t low = M * x;
+    return (uint32_t)(((unsigned __int128)low * d) >> 64);
+}
+
+// The serial Fisher-Yates swaps over precomputed targets (tt[s]: target of
+// draw s, sign in bit 31).  For small k the head of the array (positions
+// 0..k-1, the only positions a draw writes besides its target) stays in
+// registers, so a draw costs one load and one store of the array.
+template <int K>
+static void swaps_head(uint32_t* pa, const uint32_t* tp, int64_t n, uint32_t* hidx)
+{
+    uint32_t h[K];
+    for (int j = 0; j < K; ++j) h[j] = pa[j];
+    for (int64_t i = 0; i < n; ++i) {
+        const uint32_t* w = tp + i * K;
+        uint32_t* out = hidx + i * K;
+#pragma GCC unroll 4
+        for (int j = 0; j < K; ++j) {
+            const uint32_t t = w[j] & 0x7fffffffu;
+            uint32_t a;
+            if (t < (uint32_t)K) {   // t >= j: both ends in the head
+                a = h[0];
+                for (int q = 1; q < K; ++q) a = (t == (uint32_t)q) ? h[q] : a;
+                for (int q = 0; q < K; ++q) h[q] = (t == (uint32_t)q) ? h[j] : h[q];
+            } else {
+                a = pa[t];
+                pa[t] = h[j];
+            }
+            h[j] = a;
+            out[j] = a | (w[j] & 0x80000000u);
+        }
+    }
+    for (int j = 0; j < K; ++j) pa[j] = h[j];
+}
+
 // Caller holds the lock (rng_lock).  The stream gives n*k row draws, then
 // n*k sign draws.  Only the Fisher-Yates swaps are serial; the draws
-// themselves are not, so for large n*k worker threads start from the state
-// jumped to their chunk of the stream and turn its words into swap targets
-// t = word % (m - j) + j and sign bits, and this thread then runs the swaps
-// over the precomputed targets.
+// themselves are not, so for large n*k worker threads start from the states
+// jumped to their chunk of both draw sequences and turn their words into swap
+// targets t = word % (m - j) + j with the sign bit, and this thread then runs
+// the swaps over the precomputed targets.
 void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
 {
     const int64_t nk = n * k;
@@ -164,8 +206,13 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
             if ((g_rng.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
         return;
     }
-    // tt[s]: swap target of draw s, with the sign in bit 31 (set = -1)
-    std::vector<uint32_t> tt((size_t)nk);
+    // tt[s]: swap target of draw s, with the sign in bit 31 (set = -1); left
+    // uninitialised here, every entry is written once by the worker whose chunk
+    // holds it (the pages are first touched by those workers)
+    std::unique_ptr<uint32_t[]> tt(new uint32_t[(size_t)nk]);
+    // the divisors m - j and their remainder constants
+    std::vector<uint64_t> magic((size_t)k);
+    for (int64_t j = 0; j < k; ++j) magic[(size_t)j] = UINT64_C(0xFFFFFFFFFFFFFFFF) / (uint64_t)(m - j) + 1;
     const unsigned hw = std::thread::hardware_concurrency();
     const int64_t nthr = std::max<int64_t>(1, std::min<int64_t>({(int64_t)(hw ? hw : 4), 16, nk >> 14}));
     const int64_t chunk = (nk + nthr - 1) / nthr;
@@ -174,28 +221,30 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
         const int64_t s0 = c * chunk, s1 = std::min(nk, s0 + chunk);
         if (s0 >= s1) return;
         Rng rows = base.jumped((uint64_t)s0);
+        Rng signs = base.jumped((uint64_t)(nk + s0));
         int64_t j = s0 % k;
+        uint32_t* out = tt.get();
         for (int64_t s = s0; s < s1; ++s) {
-            tt[(size_t)s] = (uint32_t)(rows.next() % (uint32_t)(m - j)) + (uint32_t)j;
+            const uint32_t d = (uint32_t)(m - j);
+            const uint32_t t = fastmod_u32(rows.next(), magic[(size_t)j], d) + (uint32_t)j;
+            const uint32_t neg = (signs.next() & 1u) == 0u ? 0x80000000u : 0u;   // rand()%2 == 0 -> -1
+            out[s] = t | neg;
             if (++j == k) j = 0;
         }
-        Rng signs = base.jumped((uint64_t)(nk + s0));
-        for (int64_t s = s0; s < s1; ++s)
-            if ((signs.next() & 1u) == 0u) tt[(size_t)s] |= 0x80000000u;   // rand()%2 == 0 -> -1
     };
     std::vector<std::thread> pool;
     for (int64_t c = 1; c < nthr; ++c) pool.emplace_back(work, c);
     work(0);
     for (auto& t : pool) t.join();
-    const uint32_t* tp = tt.data();
+    const uint32_t* tp = tt.get();
     if (k == 1) {
-        for (int64_t s = 0; s < nk; ++s) {
-            const uint32_t w = tp[s], t = w & 0x7fffffffu;
-            const uint32_t a = pa[t];
-            pa[t] = pa[0];
-            pa[0] = a;
-            hidx[s] = a | (w & 0x80000000u);
-        }
+        swaps_head<1>(pa, tp, n, hidx);
+    } else if (k == 2) {
+        swaps_head<2>(pa, tp, n, hidx);
+    } else if (k == 3) {
+        swaps_head<3>(pa, tp, n, hidx);
+    } else if (k == 4) {
+        swaps_head<4>(pa, tp, n, hidx);
     } else {
         int64_t j = 0;
         for (int64_t s = 0; s < nk; ++s) {
