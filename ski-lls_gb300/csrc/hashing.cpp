@@ -179,6 +179,11 @@ static void swaps_head(uint32_t* pa, const uint32_t* tp, int64_t n, uint32_t* hi
     for (int j = 0; j < K; ++j) pa[j] = h[j];
 }
 
+// Draw counts below this run on the calling thread alone (thread start-up
+// costs more than the parallel draws save there; measured: 2^15 is better
+// than 2^17 to 2^20 on the 512-problem batch).
+constexpr int64_t kHashSerialMax = (int64_t)1 << 15;
+
 // Caller holds the lock (rng_lock).  The stream gives n*k row draws, then
 // n*k sign draws.  Only the Fisher-Yates swaps are serial; the draws
 // themselves are not, so for large n*k worker threads start from the states
@@ -191,11 +196,16 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
     std::vector<uint32_t> perm((size_t)m);
     for (int64_t i = 0; i < m; ++i) perm[(size_t)i] = (uint32_t)i;
     uint32_t* pa = perm.data();
-    if (nk < ((int64_t)1 << 15)) {
+    if (nk < kHashSerialMax) {
+        // a local copy of the generator (the global one would be reloaded and
+        // stored around every draw: the output writes may alias it)
+        Rng g = g_rng;
+        std::vector<uint64_t> mg((size_t)k);
+        for (int64_t j = 0; j < k; ++j) mg[(size_t)j] = UINT64_C(0xFFFFFFFFFFFFFFFF) / (uint64_t)(m - j) + 1;
         for (int64_t i = 0; i < n; ++i) {
             uint32_t* out = hidx + i * k;
             for (int64_t j = 0; j < k; ++j) {
-                uint32_t t = (uint32_t)(g_rng.next() % (uint32_t)(m - j)) + (uint32_t)j;
+                uint32_t t = fastmod_u32(g.next(), mg[(size_t)j], (uint32_t)(m - j)) + (uint32_t)j;
                 uint32_t a = pa[t];
                 pa[t] = pa[j];
                 pa[j] = a;
@@ -203,7 +213,8 @@ void gen_hash_packed(int64_t m, int64_t n, int64_t k, uint32_t* hidx)
             }
         }
         for (int64_t q = 0; q < nk; ++q)
-            if ((g_rng.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
+            if ((g.next() & 1u) == 0u) hidx[q] |= 0x80000000u;   // rand()%2 == 0 -> -1
+        g_rng = g;
         return;
     }
     // tt[s]: swap target of draw s, with the sign in bit 31 (set = -1); left
