@@ -23,6 +23,7 @@
 #include <mutex>
 #include <thread>
 #include <atomic>
+#include <condition_variable>
 #include <type_traits>
 #include <vector>
 
@@ -789,21 +790,54 @@ static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double*
         if (A[p].n > 0 && o.k > (int64_t)std::ceil((double)A[p].n * o.gamma))
             fail(SKL_ERR_INVALID, "k exceeds the sketch size m = ceil(gamma*d)");
     }
-    // hash streams, in problem order
+    // hash streams, in problem order, drawn by one producer thread while the
+    // workers already solve the problems whose streams are ready (problem p
+    // waits for hashed >= p + 1; the producer also releases everyone if it
+    // fails, with hash_failed set)
     std::vector<std::vector<uint32_t>> hh((size_t)nprob);
     std::vector<double> hash_ms((size_t)nprob, 0.0);
-    for (int64_t p = 0; p < nprob; ++p) {
-        const int64_t n = A[p].m, d = A[p].n;
-        if (d == 0) continue;
-        const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
-        hh[(size_t)p].resize((size_t)(n * o.k));
-        auto t0 = std::chrono::steady_clock::now();
-        if (o.seed_mode) rng_srand(o.seed);
-        rng_lock();
-        gen_hash_packed(m, n, o.k, hh[(size_t)p].data());
-        rng_unlock();
-        hash_ms[(size_t)p] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    }
+    std::mutex hash_mu;
+    std::condition_variable hash_cv;
+    int64_t hashed = 0;
+    bool hash_failed = false;
+    std::string hash_msg;
+    std::thread producer([&] {
+        try {
+            for (int64_t p = 0; p < nprob; ++p) {
+                const int64_t n = A[p].m, d = A[p].n;
+                if (d > 0) {
+                    const int64_t m = (int64_t)std::ceil((double)d * o.gamma);
+                    hh[(size_t)p].resize((size_t)(n * o.k));
+                    auto t0 = std::chrono::steady_clock::now();
+                    if (o.seed_mode) rng_srand(o.seed);
+                    {
+                        struct Held {
+                            Held() { rng_lock(); }
+                            ~Held() { rng_unlock(); }
+                        } held;
+                        gen_hash_packed(m, n, o.k, hh[(size_t)p].data());
+                    }
+                    hash_ms[(size_t)p] =
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                }
+                {
+                    std::lock_guard<std::mutex> lk(hash_mu);
+                    hashed = p + 1;
+                }
+                hash_cv.notify_all();
+            }
+        } catch (const std::exception& e) {
+            std::lock_guard<std::mutex> lk(hash_mu);
+            hash_failed = true;
+            hash_msg = e.what();
+            hashed = nprob;
+        }
+        hash_cv.notify_all();
+    });
+    struct ProducerJoin {
+        std::thread& t;
+        ~ProducerJoin() { if (t.joinable()) t.join(); }
+    } producer_join{producer};
     int workers = 8;
     if (const char* e = std::getenv("SKILLS_BATCH_STREAMS")) workers = std::max(1, std::atoi(e));
     workers = (int)std::min<int64_t>(workers, nprob);
@@ -819,7 +853,14 @@ static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double*
             std::memset(&inf, 0, sizeof inf);
             skl_status rc = SKL_OK;
             std::string msg;
+            bool stream_ok;
+            {
+                std::unique_lock<std::mutex> lk(hash_mu);
+                hash_cv.wait(lk, [&] { return hashed > p; });
+                stream_ok = !hash_failed;
+            }
             try {
+                if (!stream_ok) fail(SKL_ERR_ALLOC, "skl_batched_sparse_solve: hash stream: " + hash_msg);
                 if (A[p].n > 0) {
                     Context& C = context(o.device, 1 + slot);
                     reset_launch_count();
@@ -849,6 +890,7 @@ static void batched_sparse_common(int64_t nprob, const skl_csc* A, const double*
     std::vector<std::thread> pool;
     for (int w = 0; w < workers; ++w) pool.emplace_back(work, w);
     for (auto& t : pool) t.join();
+    producer.join();
     if (first_status != SKL_OK) fail(first_status, first_msg);
 }
 

@@ -1,4 +1,5 @@
 """C-ABI library: builds, loads, exports every declared symbol; host-side pieces (no GPU)."""
+import math
 import os
 import re
 
@@ -223,3 +224,28 @@ def test_python_structs_match_the_c_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_batched_draws_every_stream_in_problem_order():
+    """skl_batched_sparse_solve draws each problem's hashing from the library
+    stream in problem order (a producer thread, while the workers solve), so
+    afterwards the stream stands exactly where a loop of single solves leaves
+    it -- also when every solve fails (here: no GPU), since the draws do not
+    depend on the solves.  Mixed sizes cover the serial and threaded draws."""
+    import scipy.sparse as sp
+    shapes = [(3000, 60), (20000, 400), (2500, 50), (40000, 300), (5000, 100)]
+    probs = []
+    for i, (n, d) in enumerate(shapes):
+        A = sp.random(n, d, density=0.01, random_state=i, format="csc")
+        probs.append((A, np.ones(n)))
+    skl.srand(21)
+    try:
+        skl.batched_sparse_spqr(probs, 1.7, 2)
+    except skl.SklError:
+        pass
+    rows, _ = skl.hash_generate(100, 10, 2)
+    g = orc.Rng(21)
+    for (n, d) in shapes:
+        orc.gen_hashing(g, int(math.ceil(1.7 * d)), n, 2)
+    ref, _ = orc.gen_hashing(g, 100, 10, 2)
+    np.testing.assert_array_equal(rows, ref)
